@@ -1,0 +1,485 @@
+#!/usr/bin/env python3
+"""Benchmark: gridded Mvis/s on one GB300 for the multi-facet Jones + w-projection workload.
+
+Workload (one "step" = one pass of the facet-imaging hot path over the whole visibility set):
+  27 antennas (351 baselines) on a seeded Y layout, 2000 timesteps of Earth rotation, 64 channels
+  1.0-1.5 GHz -> 702,000 rows x 64 channels = 44.93 M visibilities (4 correlations, complex64);
+  50 seeded point sources + noise; seeded per-antenna, per-time, per-facet 2x2 gains; 16 facets
+  of 1024^2 within 3 deg; w-projection with 64 planes, supports 15..63 (ABI table padded to 63,
+  oversampling 15); uniform weighting, so each step grids the visibilities (facet_4_cor_corrections)
+  and the sampling function (facet_sampling_function).  Throughput counts (visibility x facet)
+  pairs that pass flags: 44.93 M x 16 = 718.8 M per step.
+
+Lines printed (rank 0, one JSON line):
+  value     Mvis/s with inputs resident in HBM (device pointers through the C-ABI), CUDA events
+            on the library stream around each step;
+  e2e       the same metric through the reference-facing C-ABI with host buffers: initLibrary,
+            facet_4_cor_corrections + facet_sampling_function (pinned host inputs, final-chunk
+            copy-back), weight_uniformly, normalize, finalize, releaseLibrary every step;
+  roofline  the gridder kernel against the measured FP32 FMA rate of this GPU (the gridder is
+            FP32-issue bound; HBM traffic is reported alongside);
+  cpu_baseline  the oracle port of the reference CPU library (OpenMP over facets) on a bounded
+            sample of rows, on this machine's host cores.
+
+--impl reference prints the reference arm: the oracle port of the reference's CPU path, timed on
+bounded row samples of the same workload, all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+N_ANT, N_TIMES, N_CHAN, N_FACETS, NX = 27, 2000, 64, 16, 1024
+WPLANES, S_HALF, MIN_SUPPORT, OS = 64, 31, 15, 15
+CELL = 5.0
+N_SRC = 50
+WORKLOAD = ("facet_4_cor_corrections+facet_sampling_function, 27 ant x 2000 t x 64 ch (44.93M vis, 4 corr), "
+            "16 facets 1024^2, w-proj 64 planes support 15-63 (padded 63), os 15, Jones, uniform")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--time-frac", type=float, default=1.0, help="fraction of timesteps (quick runs)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------------------- workload
+def geometry(n_times):
+    from bullseye_gb300 import synth
+    dec = np.deg2rad(-30.0)
+    enu = synth.y_layout(N_ANT, 600.0, seed=2)
+    xyz = synth.enu_to_equatorial(enu, np.deg2rad(34.0))
+    uvw, a1, a2, tid = synth.earth_rotation_rows(xyz, n_times, dec, np.deg2rad(120.0))
+    freqs = np.linspace(1.0e9, 1.5e9, N_CHAN)
+    lam = synth.C_LIGHT / freqs
+    rng = np.random.default_rng(9)
+    lim = np.deg2rad(3.0)
+    fl, fm = rng.uniform(-lim, lim, N_FACETS), rng.uniform(-lim, lim, N_FACETS)
+    dec0 = dec / synth.ARCSEC
+    facets = np.stack([fl / np.cos(dec) / synth.ARCSEC, dec0 + fm / synth.ARCSEC], axis=1)
+    # baseline-major order (what repack_input_data produces), stable in time
+    from bullseye_gb300.imaging import baseline_index
+    b = baseline_index(a1, a2, N_ANT)
+    order = np.argsort(b, kind="stable")
+    nb = N_ANT * (N_ANT - 1) // 2 + N_ANT
+    starts = np.zeros(nb + 1, dtype=np.uintp)
+    np.add.at(starts, b + 1, 1)
+    starts = np.cumsum(starts).astype(np.uintp)
+    maxb = np.max(np.linalg.norm(uvw, axis=1))
+    wmax = maxb / lam.min()
+    return dict(uvw=uvw[order], a1=a1[order], a2=a2[order], tid=tid[order], lam=lam, facets=facets,
+                starts=starts, dec0=dec0, wmax=wmax, n_times=n_times, nb=nb)
+
+
+def kernel_stack(wmax):
+    from bullseye_gb300.filters import wproj_kernels
+    fov = NX * CELL * np.pi / (180 * 3600)
+    stack, supports = wproj_kernels(S_HALF, OS, WPLANES, wmax, fov, min_support=MIN_SUPPORT)
+    return stack.astype(np.complex64), supports
+
+
+def device_inputs(geo, torch):
+    """Visibilities, weights, flags and gains generated on the GPU (float32 phases)."""
+    dev = torch.device("cuda")
+    R = geo["uvw"].shape[0]
+    rng = np.random.default_rng(7)
+    lim = np.deg2rad(3.0)
+    l = torch.tensor(rng.uniform(-lim, lim, N_SRC), dtype=torch.float32, device=dev)
+    m = torch.tensor(rng.uniform(-lim, lim, N_SRC), dtype=torch.float32, device=dev)
+    flux = torch.tensor(rng.uniform(0.1, 2.0, N_SRC), dtype=torch.complex64, device=dev)
+    nm1 = torch.sqrt(1 - l * l - m * m) - 1
+    uvw = torch.tensor(geo["uvw"], dtype=torch.float32, device=dev)
+    vis = torch.empty((R, N_CHAN, 4), dtype=torch.complex64, device=dev)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(11)
+    step = 1 << 15
+    for ci, lam in enumerate(geo["lam"]):
+        for lo in range(0, R, step):
+            hi = min(R, lo + step)
+            u, v, w = uvw[lo:hi, 0:1], uvw[lo:hi, 1:2], uvw[lo:hi, 2:3]
+            ph = (u * l + v * m + w * nm1) * (-2 * np.pi / lam)
+            s = torch.polar(torch.ones_like(ph), ph) @ flux
+            vis[lo:hi, ci, 0] = s
+            vis[lo:hi, ci, 3] = s
+            vis[lo:hi, ci, 1] = 0
+            vis[lo:hi, ci, 2] = 0
+    vis += (torch.randn(vis.shape, dtype=torch.complex64, device=dev, generator=gen) * 0.01)
+    weights = torch.ones((R, N_CHAN, 4), dtype=torch.float32, device=dev)
+    flags = torch.zeros((R, N_CHAN, 4), dtype=torch.uint8, device=dev)
+    T = geo["n_times"]
+    shape = (T, N_ANT, N_FACETS, 1, N_CHAN)
+    jones = torch.zeros(shape + (4,), dtype=torch.complex64, device=dev)
+    for k in (0, 3):
+        amp = 1 + (torch.rand(shape, device=dev, generator=gen) * 0.2 - 0.1)
+        phase = (torch.rand(shape, device=dev, generator=gen) * 2 - 1) * np.pi
+        jones[..., k] = torch.polar(amp, phase)
+    for k in (1, 2):
+        jones[..., k] = 0.05 * torch.randn(shape, dtype=torch.complex64, device=dev, generator=gen)
+    return dict(
+        vis=vis, weights=weights, flags=flags, uvw=uvw, jones=jones,
+        flagged_rows=torch.zeros(R, dtype=torch.uint8, device=dev),
+        field=torch.zeros(R, dtype=torch.int32, device=dev),
+        spw=torch.zeros(R, dtype=torch.int32, device=dev),
+        a1=torch.tensor(geo["a1"].astype(np.int32), device=dev),
+        a2=torch.tensor(geo["a2"].astype(np.int32), device=dev),
+        tid=torch.tensor(geo["tid"].astype(np.int64), device=dev),
+        starts=torch.tensor(geo["starts"].astype(np.int64), device=dev),
+    )
+
+
+class Tables:
+    """Host-side tables and output buffers handed to initLibrary (kept alive by this object)."""
+
+    def __init__(self, geo, conv):
+        self.conv = np.ascontiguousarray(conv)
+        self.lam = geo["lam"].astype(np.float32).reshape(1, -1)
+        self.enabled = np.ones(N_CHAN, dtype=np.bool_)
+        self.cgi = np.zeros(N_CHAN, dtype=np.uintp)
+        self.sfcgi = np.zeros(N_CHAN, dtype=np.uintp)
+        self.facets = geo["facets"].astype(np.float32)
+        self.grid = np.zeros((N_FACETS, 1, 4, NX, NX), dtype=np.complex64)
+        self.sf = np.zeros((N_FACETS, 1, 1, NX, NX), dtype=np.complex64)
+
+    def fill(self, st, geo, rows):
+        P = ctypes.c_void_p
+        st.chunk_max_row_count = rows
+        st.nx = st.ny = NX
+        st.cell_size_x = st.cell_size_y = CELL
+        st.conv = self.conv.ctypes.data_as(P)
+        st.conv_support = S_HALF
+        st.conv_oversample = OS
+        st.phase_centre_ra = 0.0
+        st.phase_centre_dec = geo["dec0"]
+        st.should_invert_jones_terms = True
+        st.imaging_field = 0
+        st.channel_grid_indicies = self.cgi.ctypes.data_as(P)
+        st.cube_channel_dim_size = 1
+        st.output_buffer = self.grid.ctypes.data_as(P)
+        st.baseline_count = geo["nb"]
+        st.number_of_polarization_terms = 4
+        st.number_of_polarization_terms_being_gridded = 4
+        st.spw_count = 1
+        st.channel_count = N_CHAN
+        st.antenna_count = N_ANT
+        st.enabled_channels = self.enabled.ctypes.data_as(P)
+        st.reference_wavelengths = self.lam.ctypes.data_as(P)
+        st.should_grid_sampling_function = True
+        st.sampling_function_buffer = self.sf.ctypes.data_as(P)
+        st.sampling_function_channel_grid_indicies = self.sfcgi.ctypes.data_as(P)
+        st.sampling_function_channel_count = 1
+        st.num_facet_centres = N_FACETS
+        st.facet_centres = self.facets.ctypes.data_as(P)
+        st.wplanes = WPLANES
+        st.wmax_est = geo["wmax"]
+        st.no_timestamps_read = geo["n_times"]
+        st.row_count = rows
+
+
+def set_rows(st, d, ptr):
+    st.visibilities = ptr(d["vis"])
+    st.uvw_coords = ptr(d["uvw"])
+    st.visibility_weights = ptr(d["weights"])
+    st.flags = ptr(d["flags"])
+    st.flagged_rows = ptr(d["flagged_rows"])
+    st.field_array = ptr(d["field"])
+    st.spw_index_array = ptr(d["spw"])
+    st.antenna_1_ids = ptr(d["a1"])
+    st.antenna_2_ids = ptr(d["a2"])
+    st.timestamp_ids = ptr(d["tid"])
+    st.jones_terms = ptr(d["jones"])
+    st.baseline_starting_indexes = ptr(d["starts"])
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], [], set()
+        dev = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"),
+                                 parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- CPU (oracle port)
+def cpu_run(geo, conv1d, n_rows_sample, threads=None):
+    """Time the oracle port of the reference CPU library (single precision) on the first
+    ``n_rows_sample`` rows of every baseline-sorted track set (all facets, all channels)."""
+    from bullseye_gb300.abi import gridding_parameters_type
+    from bullseye_gb300.filters import outer_stack
+    from oracle.harness import load_oracle
+    lib = load_oracle("single")
+    idx = np.linspace(0, geo["uvw"].shape[0] - 1, n_rows_sample).astype(np.int64)
+    R = idx.size
+    rng = np.random.default_rng(3)
+    vis = (rng.normal(0, 1, (R, N_CHAN, 4)) + 1j * rng.normal(0, 1, (R, N_CHAN, 4))).astype(np.complex64)
+    wt = np.ones((R, N_CHAN, 4), np.float32)
+    fl = np.zeros((R, N_CHAN, 4), np.bool_)
+    uvw = geo["uvw"][idx].astype(np.float32)
+    T = 1
+    jones = np.zeros((T, N_ANT, N_FACETS, 1, N_CHAN, 4), np.complex64)
+    jones[..., 0] = 1.05 * np.exp(0.3j)
+    jones[..., 3] = 0.97 * np.exp(-0.2j)
+    jones[..., 1] = 0.02
+    conv2d = outer_stack(conv1d.astype(np.complex128)).astype(np.complex64)
+    tab = Tables(geo, conv2d)
+    st = gridding_parameters_type("single")()
+    tab.fill(st, geo, R)
+    P = ctypes.c_void_p
+    keep = dict(vis=vis, uvw=uvw, weights=wt, flags=fl, flagged_rows=np.zeros(R, np.bool_),
+                field=np.zeros(R, np.uint32), spw=np.zeros(R, np.uint32),
+                a1=geo["a1"][idx].astype(np.uint32), a2=geo["a2"][idx].astype(np.uint32),
+                tid=np.zeros(R, np.uintp), jones=jones, starts=np.zeros(2, np.uintp))
+    lib.initLibrary(ctypes.byref(st))
+    set_rows(st, keep, lambda a: a.ctypes.data_as(P))
+    st.no_timestamps_read = T
+    st.baseline_starting_indexes = None
+    t0 = time.perf_counter()
+    lib.facet_4_cor_corrections(ctypes.byref(st))
+    lib.facet_sampling_function(ctypes.byref(st))
+    dt = time.perf_counter() - t0
+    lib.releaseLibrary()
+    pairs = R * N_CHAN * N_FACETS
+    return pairs, dt
+
+
+def cpu_baseline(geo, conv1d, target_s):
+    threads = os.cpu_count() or 1
+    probe_rows = 16
+    pairs, dt = cpu_run(geo, conv1d, probe_rows)
+    per_row = dt / probe_rows
+    rows = int(max(probe_rows, min(20000, target_s / max(per_row, 1e-6))))
+    pairs, dt = cpu_run(geo, conv1d, rows)
+    return {"value": pairs / dt / 1e6, "unit": "Mvis/s", "cores": min(threads, N_FACETS), "kind": "port",
+            "sample": f"{rows} rows x 64 ch x 16 facets ({pairs} vis-facet pairs) of the same workload, "
+                      f"oracle port of the reference CPU library (FP32, OpenMP over facets, {os.cpu_count()} cores "
+                      f"available, one thread per facet), {dt:.1f} s"}
+
+
+# ----------------------------------------------------------------------------- main
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    n_times = max(8, int(N_TIMES * args.time_frac))
+    geo = geometry(n_times)
+    conv, supports = kernel_stack(geo["wmax"])
+    R = geo["uvw"].shape[0]
+    pairs_per_step = R * N_CHAN * N_FACETS
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        steps = []
+        per = max(2.0, min(20.0, 150.0 / max(1, args.steps + args.warmup)))
+        base = cpu_baseline(geo, conv, per)
+        for _ in range(args.steps):
+            steps.append(cpu_baseline(geo, conv, per)["value"])
+        v = float(np.median(steps))
+        line = {"impl": "reference", "metric": "gridded Mvis/s (vis x facet pairs)", "value": v, "unit": "Mvis/s",
+                "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": pairs_per_step / v / 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "l2": "inputs 4.2 GB > L2"},
+                "cpu_baseline": {"value": v, "unit": "Mvis/s", "cores": base["cores"], "kind": "port",
+                                 "sample": base["sample"]},
+                "e2e": {"value": v, "unit": "Mvis/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from bullseye_gb300.abi import gridding_parameters_type
+    from bullseye_gb300.library import check, load_library
+    lib = load_library("GPU", "single")
+    d = device_inputs(geo, torch)
+    torch.cuda.synchronize()
+
+    # ------------------------------------------------------------- device-resident value
+    tab = Tables(geo, conv)
+    st = gridding_parameters_type("single")()
+    tab.fill(st, geo, R)
+    lib.bullseye_set_device_inputs(1)
+    lib.initLibrary(ctypes.byref(st))
+    check(lib)
+    set_rows(st, d, lambda t: ctypes.c_void_p(t.data_ptr()))
+    st.is_final_data_chunk = False
+    stream = torch.cuda.ExternalStream(lib.bullseye_get_stream())
+
+    def step():
+        lib.facet_4_cor_corrections(ctypes.byref(st))
+        lib.facet_sampling_function(ctypes.byref(st))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    check(lib)
+    lib.bullseye_reset_counters()
+    clocks = ClockSampler(os.path.join(REPO, "gpurun_out", "clocks.csv") if os.path.isdir(os.path.join(REPO, "gpurun_out"))
+                          else "/tmp/bullseye_clocks.csv")
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    clk = clocks.stop()
+    launches = int(lib.bullseye_kernel_launches())
+    cnt = ctypes.c_longlong(0)
+    vis_kernel_ms = lib.bullseye_gridder_kernel_ms(0, ctypes.byref(cnt))
+    n_vis_launch = max(1, cnt.value)
+    sf_kernel_ms = lib.bullseye_gridder_kernel_ms(1, ctypes.byref(cnt))
+    check(lib)
+    ms_per_step = ms / args.steps
+    value = pairs_per_step * world / (ms_per_step * 1e-3) / 1e6
+    fp32_peak = lib.bullseye_fp32_fma_tflops(4096)
+    W = 2 * S_HALF + 1
+    flops_per_pair = 8 * 4 * W * W + 6 * 4 + 128
+    launch_ms = vis_kernel_ms / n_vis_launch
+    achieved = pairs_per_step * flops_per_pair / (launch_ms * 1e-3) / 1e12
+    bytes_per_pair = 8 * 4 + 4 * 4 + 4 + 12 + 64
+    hbm_gbs = pairs_per_step * bytes_per_pair / (launch_ms * 1e-3) / 1e9
+    peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(REPO, "MEASURED_PEAKS.json")) else {}
+    lib.releaseLibrary()
+    lib.bullseye_set_device_inputs(0)
+
+    # ------------------------------------------------------------- end to end through the C-ABI
+    e2e = None
+    if not args.no_e2e and rank == 0:
+        host = {k: v.cpu().pin_memory() for k, v in d.items()}
+        hnp = {k: v.numpy() for k, v in host.items()}
+        hnp["flagged_rows"] = hnp["flagged_rows"].view(np.bool_)
+        hnp["flags"] = hnp["flags"].view(np.bool_)
+        hnp["starts"] = hnp["starts"].view(np.uintp)
+        hnp["tid"] = hnp["tid"].view(np.uintp)
+        del d
+        torch.cuda.empty_cache()
+        P = ctypes.c_void_p
+
+        def e2e_step():
+            tab2 = Tables(geo, conv)
+            s2 = gridding_parameters_type("single")()
+            tab2.fill(s2, geo, R)
+            lib.initLibrary(ctypes.byref(s2))
+            set_rows(s2, hnp, lambda a: a.ctypes.data_as(P))
+            s2.is_final_data_chunk = True
+            lib.facet_4_cor_corrections(ctypes.byref(s2))
+            lib.facet_sampling_function(ctypes.byref(s2))
+            lib.gridding_barrier()
+            lib.weight_uniformly(ctypes.byref(s2))
+            lib.normalize(ctypes.byref(s2))
+            lib.finalize(ctypes.byref(s2))
+            img = float(tab2.grid.view(np.float32).reshape(-1)[0])
+            lib.releaseLibrary()
+            check(lib)
+            return img
+
+        e2e_step()
+        t0 = time.perf_counter()
+        n_e2e = max(1, min(args.steps, 3))
+        for _ in range(n_e2e):
+            e2e_step()
+        dt = (time.perf_counter() - t0) / n_e2e
+        h2d = sum(hnp[k].nbytes for k in ("vis", "weights", "flags", "uvw", "flagged_rows", "field", "spw", "a1",
+                                          "a2", "tid", "jones", "starts"))
+        h2d += tab.conv.nbytes + tab.grid.nbytes + tab.sf.nbytes  # tables and initial grids (initLibrary)
+        h2d += N_FACETS * NX * NX * 8  # finalize uploads the first cube slice of each facet
+        d2h = tab.grid.nbytes + tab.sf.nbytes + N_FACETS * NX * NX * (8 + 4)
+        e2e = {"value": pairs_per_step / dt / 1e6, "unit": "Mvis/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "s_per_step": dt,
+               "calls": "initLibrary, facet_4_cor_corrections, facet_sampling_function, weight_uniformly, normalize, "
+                        "finalize, releaseLibrary (host pinned buffers)"}
+
+    cpu = None
+    if not args.no_cpu and rank == 0 and world == 1:
+        cpu = cpu_baseline(geo, conv, args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": "gridded Mvis/s (vis x facet pairs)", "value": value, "unit": "Mvis/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "rows": R, "channels": N_CHAN, "facets": N_FACETS,
+                       "vis_facet_pairs_per_step": pairs_per_step, "l2": "inputs 4.2 GB per step > 129 MB L2",
+                       "form": "plain drop-in (per-call launches, compensated FP32)"},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                         "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
+                         "peak_source": "measured FP32 FMA probe on this GPU (MEASURED_PEAKS.json has no FP32 rate)",
+                         "kernel": "romein_grid_kernel<4,wproj,J=8> (visibilities)", "launch_ms": launch_ms,
+                         "flops_per_pair": flops_per_pair, "hbm_gbs": hbm_gbs,
+                         "hbm_frac_of_measured": hbm_gbs / peaks["hbm_gbs"] if peaks.get("hbm_gbs") else None,
+                         "sampling_kernel_ms": sf_kernel_ms / max(1, cnt.value)},
+            "clocks": clk, "gpu_launches": launches, "e2e": e2e, "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

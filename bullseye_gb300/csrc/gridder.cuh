@@ -1,0 +1,543 @@
+// Romein-strategy convolutional gridder for GB300 (sm_103a).
+//
+// Work decomposition.  One CTA grids one *track*: the visibilities of one (facet, baseline,
+// channel) in time order (rows of a baseline are contiguous after repack_input_data, as in
+// bullseye/mo/gpu_algorithm/wrapper.cu:367-454).  Consecutive samples of a track move slowly
+// across the uv grid, which is what Romein's ownership scheme exploits (J. W. Romein, "An
+// efficient work-distribution strategy for gridding radio-telescope data on GPUs", ICS 2012).
+//
+// Ownership.  For full support W, the W x W cells under any visibility's kernel footprint
+// contain exactly one cell of every (x mod W, y mod W) class.  Thread (du, strip) owns the
+// classes x = du (mod W) and y in {strip*J .. strip*J+J-1} (mod W): for each visibility it
+// updates exactly the J cells of its classes inside the footprint, accumulating in registers
+// while the owned cell stays the same and flushing with a global atomic when it changes.  The
+// reference GPU kernel instead binds each thread to a fixed footprint offset
+// (bullseye/mo/gpu_algorithm/templated_gridder.h:59-69), which flushes on every cell move.
+//
+// Per-visibility work (the prologue) is done once per CTA, not once per thread: V threads each
+// prepare one visibility (correlation selection, weights x flags, Jones J_p^-1 V J_q^-H, facet
+// phase rotation, planar uv transform, cell and tap-offset selection) into shared memory, the
+// CTA then gathers the 2W taps of each staged visibility from the kernel table, and all
+// threads grid the staged chunk.
+//
+// Numerics (matching the reference CPU library, bullseye/mo/cpu_algorithm/*):
+//  * uvw / lambda, the phase argument 2 pi (u dl + v dm + w dn), the uv transform and the
+//    cell/tap selection are evaluated in FP64 in both libraries;
+//  * 1-D AA kernels select cells and taps with floor (the reference sets FE_DOWNWARD,
+//    convolution_policies.h:73-75); w-projection uses round-half-even (FE_TONEAREST, :233);
+//  * tap index = trunc((1 - u + round(u)) * os) + j*os; a visibility is dropped when
+//    disc + W + 2 >= n or disc < 0 (convolution_policies.h:86-97);
+//  * single-precision library: visibilities, taps and the register accumulation are FP32,
+//    the phase is evaluated by sincosf on the FP64-reduced argument; grid flushes can be
+//    compensated (hi/lo pair, TwoSum on the value returned by the atomic);
+//  * normalisation: sum over taps of the real tap weight times weight x flag, in FP64
+//    (templated_gridder.h:97 and store_normalization_term), computed per visibility as
+//    Re(sum_j k_u[j] * sum_i k_v[i]).
+#pragma once
+#include "common.h"
+
+namespace bz {
+
+#if defined(BULLSEYE_SINGLE)
+typedef float acc_real;
+#else
+typedef double acc_real;
+#endif
+
+struct cplx {
+  acc_real re, im;
+};
+__device__ __forceinline__ cplx cmul(cplx a, cplx b) {
+  cplx r;
+  r.re = a.re * b.re - a.im * b.im;
+  r.im = a.re * b.im + a.im * b.re;
+  return r;
+}
+
+enum CorrMode { CORR_SINGLE = 0, CORR_DUAL = 1, CORR_QUAD = 2, CORR_QUAD_JONES = 3, CORR_SAMPLING = 4 };
+
+// Per-facet transform constants, evaluated on the host in FP64
+// (phase_transform_policies.h:110-134, baseline_transform_policies.h:117-149).
+struct FacetXform {
+  double u_term, v_term;  // planar uv transform: u -= w u_term, v -= w v_term
+  double dl, dm, dn;      // phase rotation offsets
+};
+
+struct GridArgs {
+  // row inputs (device)
+  const vis_complex *vis;
+  const vis_real *weights;
+  const uint8_t *flags;
+  const vis_real *uvw;
+  const uint8_t *flagged_rows;
+  const unsigned *field;
+  const unsigned *spw;
+  const unsigned *ant1;
+  const unsigned *ant2;
+  const size_t *time_ids;
+  const vis_complex *jones_inv;  // inverted 2x2 terms [T][A][F][S][Ch][4]
+  const size_t *starts;          // baseline row starts [slots + 1] or null (fixed segments)
+  // per-run tables (device)
+  const vis_real *wavelengths;
+  const uint8_t *enabled;
+  const size_t *cgi;
+  const void *conv;              // real [K] or complex [P][K]
+  const FacetXform *facets;
+  // outputs
+  vis_complex *grid;             // slices [(f*groups + g)*NC + k][ny][nx]
+  vis_complex *grid_lo;          // compensation slices (same layout) or null
+  double *norm;                  // [f][groups][NC] or null (sampling function)
+  int *error;                    // sticky device error word
+  // sizes and scalars
+  long long nrows;
+  int nchan, npol, pol0, pol1, nspw, nant, ntimes;
+  int facet_base;                // facet index of launch facet 0 in the ABI facet list
+  int nfacets_total;             // ABI num_facet_centres (Jones indexing)
+  int groups;                    // cube channels (or sampling-function channels)
+  int nx, ny, W, os, K, P;
+  int mode;                      // CorrMode
+  int phase, uvx;                // faceting phase rotation / planar uv transform
+  int nslots, seg;               // track slots (baselines or fixed segments), segment length
+  int V;                         // visibilities staged per chunk
+  unsigned imaging_field;
+  double u_scale, v_scale, gcx, gcy, wmax;
+};
+
+// Error bits written to GridArgs::error (host decodes them)
+enum DeviceError { DEV_ERR_GRID_INDEX = 1, DEV_ERR_JONES_INDEX = 2, DEV_ERR_SINGULAR = 4, DEV_ERR_POL_INDEX = 8 };
+
+template <bool WPROJ>
+struct TapT;
+template <>
+struct TapT<false> {
+  typedef acc_real type;
+};
+template <>
+struct TapT<true> {
+  typedef cplx type;
+};
+
+template <int NC>
+struct VisRec {
+  cplx vis[NC];
+  acc_real cw[NC];
+  int u0, v0, ru, rv;
+  int g, valid;
+  int fu, fv, plane;
+};
+
+__device__ __forceinline__ void load_tap(const void *conv, long long idx, acc_real &t) {
+  t = (acc_real)((const vis_real *)conv)[idx];
+}
+__device__ __forceinline__ void load_tap(const void *conv, long long idx, cplx &t) {
+  vis_complex c = ((const vis_complex *)conv)[idx];
+  t.re = (acc_real)c.re;
+  t.im = (acc_real)c.im;
+}
+
+__device__ __forceinline__ cplx tap_mul(acc_real a, acc_real b, cplx v) {
+  acc_real t = a * b;
+  cplx r;
+  r.re = v.re * t;
+  r.im = v.im * t;
+  return r;
+}
+__device__ __forceinline__ cplx tap_mul(cplx a, cplx b, cplx v) { return cmul(v, cmul(a, b)); }
+
+// 2x2 complex products on row-major [a b; c d] stored as 4 cplx
+__device__ __forceinline__ void jmul(const cplx *A, const cplx *B, cplx *O) {
+  cplx t0 = cmul(A[0], B[0]), t1 = cmul(A[1], B[2]);
+  cplx t2 = cmul(A[0], B[1]), t3 = cmul(A[1], B[3]);
+  cplx t4 = cmul(A[2], B[0]), t5 = cmul(A[3], B[2]);
+  cplx t6 = cmul(A[2], B[1]), t7 = cmul(A[3], B[3]);
+  O[0].re = t0.re + t1.re; O[0].im = t0.im + t1.im;
+  O[1].re = t2.re + t3.re; O[1].im = t2.im + t3.im;
+  O[2].re = t4.re + t5.re; O[2].im = t4.im + t5.im;
+  O[3].re = t6.re + t7.re; O[3].im = t6.im + t7.im;
+}
+
+// Phase factor e^{i x} for an FP64 argument.  The single-precision library reduces x to
+// [-pi, pi] in FP64 and evaluates sincosf on the reduced value; the double library uses sincos.
+__device__ __forceinline__ cplx phase_factor(double x) {
+  cplx r;
+#if defined(BULLSEYE_SINGLE)
+  const double two_pi = 6.283185307179586476925286766559;
+  double n = rint(x * (1.0 / two_pi));
+  double red = fma(-n, two_pi, x);
+  float s, c;
+  sincosf((float)red, &s, &c);
+  r.re = c;
+  r.im = s;
+#else
+  double s, c;
+  sincos(x, &s, &c);
+  r.re = c;
+  r.im = s;
+#endif
+  return r;
+}
+
+// Flush one owned cell's register accumulator into the grid.
+template <int NC, bool COMP>
+__device__ __forceinline__ void flush_cell(const GridArgs &a, long long slice0, long long nxy, int x, int y,
+                                           cplx (&acc)[NC]) {
+  long long cell = (long long)y * a.nx + x;
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
+    long long idx = (slice0 + k) * nxy + cell;
+#if defined(BULLSEYE_SINGLE)
+    float2 *dst = reinterpret_cast<float2 *>(a.grid + idx);
+    float2 val = make_float2(acc[k].re, acc[k].im);
+    if (COMP) {
+      float2 old = atomicAdd(dst, val);
+      float s0 = old.x + val.x, b0 = s0 - old.x;
+      float e0 = (old.x - (s0 - b0)) + (val.x - b0);
+      float s1 = old.y + val.y, b1 = s1 - old.y;
+      float e1 = (old.y - (s1 - b1)) + (val.y - b1);
+      if (e0 != 0.0f || e1 != 0.0f)
+        atomicAdd(reinterpret_cast<float2 *>(a.grid_lo + idx), make_float2(e0, e1));
+    } else {
+      atomicAdd(dst, val);
+    }
+#else
+    atomicAdd(&a.grid[idx].re, acc[k].re);
+    atomicAdd(&a.grid[idx].im, acc[k].im);
+#endif
+    acc[k].re = 0;
+    acc[k].im = 0;
+  }
+}
+
+template <int NC, bool WPROJ>
+__device__ __forceinline__ void prologue(const GridArgs &a, int f_local, int chan, long long row, bool in_range,
+                                         VisRec<NC> &rec) {
+  rec.valid = 0;
+  if (!in_range) return;
+  const int c = chan;
+  unsigned spw = a.spw[row];
+  if (spw >= (unsigned)a.nspw) {
+    atomicOr(a.error, DEV_ERR_GRID_INDEX);
+    return;
+  }
+  long long sc = (long long)spw * a.nchan + c;
+  if (!a.enabled[sc]) return;
+  size_t g = a.cgi[sc];
+  if (g >= (size_t)a.groups) {
+    atomicOr(a.error, DEV_ERR_GRID_INDEX);
+    return;
+  }
+  const int fglob = a.facet_base + f_local;
+  const FacetXform fx = a.facets[f_local];
+  double inv_lambda = 1.0 / (double)a.wavelengths[sc];
+  double u = (double)a.uvw[3 * row] * inv_lambda;
+  double v = (double)a.uvw[3 * row + 1] * inv_lambda;
+  double w = (double)a.uvw[3 * row + 2] * inv_lambda;
+  bool row_ok = !a.flagged_rows[row] && (a.field[row] == a.imaging_field);
+
+  cplx vis[NC];
+  acc_real wt[NC];
+  bool fl[NC];
+  const long long base = ((long long)row * a.nchan + c) * a.npol;
+  if (a.mode == CORR_SAMPLING) {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) { vis[k].re = 1; vis[k].im = 0; wt[k] = 1; fl[k] = false; }
+  } else if (NC == 1 || NC == 2) {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+      int pi = (k == 0) ? a.pol0 : a.pol1;
+      vis_complex vv = a.vis[base + pi];
+      vis[k].re = vv.re; vis[k].im = vv.im;
+      wt[k] = (acc_real)a.weights[base + pi];
+      fl[k] = a.flags[base + pi] != 0;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+      vis_complex vv = a.vis[base + k];
+      vis[k].re = vv.re; vis[k].im = vv.im;
+      wt[k] = (acc_real)a.weights[base + k];
+      fl[k] = a.flags[base + k] != 0;
+    }
+  }
+  if (NC == 4 && a.mode == CORR_QUAD_JONES) {
+    // V <- J_p^-1 (V J_q^-H)   (correlation_gridding_policies.h:523-542; terms pre-inverted)
+    long long t = (long long)a.time_ids[row];
+    unsigned a1 = a.ant1[row], a2 = a.ant2[row];
+    if (t < 0 || t >= a.ntimes || a1 >= (unsigned)a.nant || a2 >= (unsigned)a.nant) {
+      atomicOr(a.error, DEV_ERR_JONES_INDEX);
+      return;
+    }
+    long long i1 = ((((t * a.nant + a1) * a.nfacets_total + fglob) * a.nspw + spw) * a.nchan + c) * 4;
+    long long i2 = ((((t * a.nant + a2) * a.nfacets_total + fglob) * a.nspw + spw) * a.nchan + c) * 4;
+    cplx P[4], Q[4], T[4], O[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      vis_complex p = a.jones_inv[i1 + k], q = a.jones_inv[i2 + k];
+      P[k].re = p.re; P[k].im = p.im;
+      Q[k].re = q.re; Q[k].im = q.im;
+    }
+    // hermitian transpose of Q
+    cplx qh[4];
+    qh[0].re = Q[0].re; qh[0].im = -Q[0].im;
+    qh[1].re = Q[2].re; qh[1].im = -Q[2].im;
+    qh[2].re = Q[1].re; qh[2].im = -Q[1].im;
+    qh[3].re = Q[3].re; qh[3].im = -Q[3].im;
+    jmul(vis, qh, T);
+    jmul(P, T, O);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) vis[k] = O[k];
+  }
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
+    bool keep = !(fl[k] || !row_ok);
+    acc_real cw = keep ? wt[k] : (acc_real)0;
+    rec.cw[k] = cw;
+    vis[k].re *= cw;
+    vis[k].im *= cw;
+  }
+  if (a.phase) {
+    cplx ph = phase_factor(6.283185307179586476925286766559 * (u * fx.dl + v * fx.dm + w * fx.dn));
+#pragma unroll
+    for (int k = 0; k < NC; ++k) vis[k] = cmul(vis[k], ph);
+  }
+  if (a.uvx) {
+    u = u - w * fx.u_term;
+    v = v - w * fx.v_term;
+  }
+  u *= a.u_scale;
+  v *= a.v_scale;
+  if (WPROJ && w < 0) {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) vis[k].im = -vis[k].im;
+    u = -u; v = -v; w = -w;
+  }
+  double ru_ = WPROJ ? rint(u) : floor(u);
+  double rv_ = WPROJ ? rint(v) : floor(v);
+  double du_d = WPROJ ? rint(u + a.gcx) : floor(u + a.gcx);
+  double dv_d = WPROJ ? rint(v + a.gcy) : floor(v + a.gcy);
+  long long plane = 0;
+  if (WPROJ) {
+    double pl = rint(fabs(w) / a.wmax * (double)(a.P - 1));
+    plane = (pl >= 0.0 && pl < (double)a.P) ? (long long)pl : -1;  // NaN and out of range -> dropped
+  }
+  if (!(du_d >= 0.0 && dv_d >= 0.0 && du_d + (a.W + 2) < (double)a.nx && dv_d + (a.W + 2) < (double)a.ny &&
+        plane >= 0 && plane < a.P))
+    return;
+  int du = (int)du_d, dv = (int)dv_d;
+  rec.fu = (int)((1.0 - u + ru_) * (double)a.os);
+  rec.fv = (int)((1.0 - v + rv_) * (double)a.os);
+  rec.plane = (int)plane;
+  rec.u0 = du;
+  rec.v0 = dv;
+  rec.ru = du % a.W;
+  rec.rv = dv % a.W;
+  rec.g = (int)g;
+#pragma unroll
+  for (int k = 0; k < NC; ++k) rec.vis[k] = vis[k];
+  rec.valid = 1;
+}
+
+// Shared-memory bytes for a launch with V staged visibilities.
+template <int NC, bool WPROJ>
+__host__ __device__ inline size_t grid_smem_bytes(int V, int W) {
+  size_t recs = sizeof(VisRec<NC>) * (size_t)V;
+  size_t taps = sizeof(typename TapT<WPROJ>::type) * (size_t)V * W * 2;
+  return recs + taps + 64;
+}
+
+template <int NC, bool WPROJ, int J, bool COMP>
+__global__ void __launch_bounds__(512, 1) romein_grid_kernel(const GridArgs a) {
+  typedef typename TapT<WPROJ>::type tap_t;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  VisRec<NC> *recs = reinterpret_cast<VisRec<NC> *>(smem_raw);
+  tap_t *tu = reinterpret_cast<tap_t *>(smem_raw + sizeof(VisRec<NC>) * a.V);
+  tap_t *tv = tu + (size_t)a.V * a.W;
+  __shared__ int s_same_g;
+  __shared__ double s_norm[NC];
+
+  const int W = a.W;
+  const long long nxy = (long long)a.nx * a.ny;
+  long long track = blockIdx.x;
+  const int chan = (int)(track % a.nchan);
+  track /= a.nchan;
+  const int slot = (int)(track % a.nslots);
+  const int f_local = (int)(track / a.nslots);
+  long long r0, r1;
+  if (a.starts) {
+    r0 = (long long)a.starts[slot];
+    r1 = (long long)a.starts[slot + 1];
+  } else {
+    r0 = (long long)slot * a.seg;
+    r1 = min(a.nrows, r0 + a.seg);
+  }
+  if (r1 > a.nrows) r1 = a.nrows;
+  if (r0 >= r1) return;
+
+  const int tid = threadIdx.x;
+  const int nstrips = (W + J - 1) / J;
+  const bool owner = tid < W * nstrips;
+  const int du = tid % W;
+  const int strip = tid / W;
+
+  cplx acc[J][NC];
+  int cy[J];
+#pragma unroll
+  for (int j = 0; j < J; ++j) {
+    cy[j] = -1;
+#pragma unroll
+    for (int k = 0; k < NC; ++k) { acc[j][k].re = 0; acc[j][k].im = 0; }
+  }
+  unsigned dirty = 0;
+  int cx = -1, cg = -1;
+
+  // normalisation accumulators of this thread's staged visibilities
+  double nacc[NC];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) nacc[k] = 0;
+  int ng = -1;
+  bool ng_mixed = false;
+  const bool want_norm = a.norm != nullptr;
+
+  for (long long base = r0; base < r1; base += a.V) {
+    const int nv = (int)min((long long)a.V, r1 - base);
+    if (tid < a.V) {
+      VisRec<NC> rec;
+      prologue<NC, WPROJ>(a, f_local, chan, base + tid, tid < nv, rec);
+      recs[tid] = rec;
+    }
+    __syncthreads();
+    // gather the 2W taps of every staged visibility
+    const int per = 2 * W;
+    for (int idx = tid; idx < nv * per; idx += blockDim.x) {
+      int vi = idx / per, j = idx - vi * per;
+      const VisRec<NC> &r = recs[vi];
+      if (!r.valid) continue;
+      bool isv = j >= W;
+      int jj = isv ? j - W : j;
+      long long ti = (long long)r.plane * a.K + (isv ? r.fv : r.fu) + (long long)jj * a.os;
+      tap_t t;
+      load_tap(a.conv, ti, t);
+      (isv ? tv : tu)[(size_t)vi * W + jj] = t;
+    }
+    __syncthreads();
+    // normalisation: Re(sum_u k_u * sum_v k_v) * weight x flag, per staged visibility
+    if (want_norm && tid < nv && recs[tid].valid) {
+      const VisRec<NC> &r = recs[tid];
+      double nt;
+      if (WPROJ) {
+        double sur = 0, sui = 0, svr = 0, svi = 0;
+        const cplx *pu = reinterpret_cast<const cplx *>(tu) + (size_t)tid * W;
+        const cplx *pv = reinterpret_cast<const cplx *>(tv) + (size_t)tid * W;
+        for (int j = 0; j < W; ++j) { sur += pu[j].re; sui += pu[j].im; svr += pv[j].re; svi += pv[j].im; }
+        nt = sur * svr - sui * svi;
+      } else {
+        double su = 0, sv = 0;
+        const acc_real *pu = reinterpret_cast<const acc_real *>(tu) + (size_t)tid * W;
+        const acc_real *pv = reinterpret_cast<const acc_real *>(tv) + (size_t)tid * W;
+        for (int j = 0; j < W; ++j) { su += pu[j]; sv += pv[j]; }
+        nt = su * sv;
+      }
+      if (ng != r.g) {
+        if (ng >= 0) {
+          ng_mixed = true;
+#pragma unroll
+          for (int k = 0; k < NC; ++k)
+            if (nacc[k] != 0.0) atomicAdd(&a.norm[((long long)(a.facet_base + f_local) * a.groups + ng) * NC + k], nacc[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < NC; ++k) nacc[k] = 0;
+        ng = r.g;
+      }
+#pragma unroll
+      for (int k = 0; k < NC; ++k) nacc[k] += (double)r.cw[k] * nt;
+    }
+    // grid the staged chunk
+    if (owner) {
+      for (int vi = 0; vi < nv; ++vi) {
+        const VisRec<NC> &r = recs[vi];
+        if (!r.valid) continue;
+        int ou = du - r.ru;
+        ou += (ou < 0) ? W : 0;
+        const int x = r.u0 + ou;
+        if (x != cx || r.g != cg) {
+          if (dirty) {
+            long long slice0 = ((long long)(a.facet_base + f_local) * a.groups + cg) * NC;
+#pragma unroll
+            for (int j = 0; j < J; ++j)
+              if (dirty & (1u << j)) flush_cell<NC, COMP>(a, slice0, nxy, cx, cy[j], acc[j]);
+            dirty = 0;
+          }
+          cx = x;
+          cg = r.g;
+#pragma unroll
+          for (int j = 0; j < J; ++j) cy[j] = -1;
+        }
+        const tap_t tuv = tu[(size_t)vi * W + ou];
+        cplx vv[NC];
+#pragma unroll
+        for (int k = 0; k < NC; ++k) vv[k] = r.vis[k];
+#pragma unroll
+        for (int j = 0; j < J; ++j) {
+          const int dvj = strip * J + j;
+          if (dvj < W) {
+            int ov = dvj - r.rv;
+            ov += (ov < 0) ? W : 0;
+            const int y = r.v0 + ov;
+            if (y != cy[j]) {
+              if (dirty & (1u << j)) {
+                long long slice0 = ((long long)(a.facet_base + f_local) * a.groups + cg) * NC;
+                flush_cell<NC, COMP>(a, slice0, nxy, cx, cy[j], acc[j]);
+                dirty &= ~(1u << j);
+              }
+              cy[j] = y;
+            }
+            const tap_t tvv = tv[(size_t)vi * W + ov];
+#pragma unroll
+            for (int k = 0; k < NC; ++k) {
+              cplx m = tap_mul(tuv, tvv, vv[k]);
+              acc[j][k].re += m.re;
+              acc[j][k].im += m.im;
+            }
+            dirty |= (1u << j);
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // final flush of owned cells
+  if (owner && dirty) {
+    long long slice0 = ((long long)(a.facet_base + f_local) * a.groups + cg) * NC;
+#pragma unroll
+    for (int j = 0; j < J; ++j)
+      if (dirty & (1u << j)) flush_cell<NC, COMP>(a, slice0, nxy, cx, cy[j], acc[j]);
+  }
+  // normalisation: one reduction per CTA when every staged visibility shared a grid group
+  if (want_norm) {
+    if (tid == 0) s_same_g = -1;
+    if (tid < NC) s_norm[tid] = 0.0;
+    __syncthreads();
+    if (ng >= 0) atomicMax(&s_same_g, ng);
+    __syncthreads();
+    const int gmax = s_same_g;
+    __syncthreads();
+    bool uniform_here = !ng_mixed && (ng < 0 || ng == gmax);
+    int all_uniform = __syncthreads_and(uniform_here ? 1 : 0);
+    if (all_uniform) {
+      if (ng >= 0) {
+#pragma unroll
+        for (int k = 0; k < NC; ++k)
+          if (nacc[k] != 0.0) atomicAdd(&s_norm[k], nacc[k]);
+      }
+      __syncthreads();
+      if (tid < NC && gmax >= 0 && s_norm[tid] != 0.0)
+        atomicAdd(&a.norm[((long long)(a.facet_base + f_local) * a.groups + gmax) * NC + tid], s_norm[tid]);
+    } else if (ng >= 0) {
+#pragma unroll
+      for (int k = 0; k < NC; ++k)
+        if (nacc[k] != 0.0) atomicAdd(&a.norm[((long long)(a.facet_base + f_local) * a.groups + ng) * NC + k], nacc[k]);
+    }
+  }
+}
+
+}  // namespace bz

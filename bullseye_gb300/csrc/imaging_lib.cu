@@ -1,0 +1,978 @@
+// GB300 drop-in for the reference's GPU imaging libraries (libgpu_imaging32.so / 64.so).
+//
+// Exports the C-ABI of bullseye/mo/cpu_gpu_common/wrapper.h:41-61 with the call-sequencing
+// contract of bullseye/mo/gpu_algorithm/wrapper.cu:
+//   * initLibrary allocates device mirrors for chunk_max_row_count rows, uploads the tables and
+//     the caller's grids, and publishes a library-owned normalisation array through
+//     params.normalization_terms ([facets][cube][corr][W*W] float64, wrapper.cu:222-230; the sum
+//     lands in bin 0, so normalize() -- which sums the bins -- sees the same value);
+//   * gridding calls are asynchronous on one library stream; grids stay device resident and are
+//     copied back to the caller's buffers when is_final_data_chunk is set (wrapper.cu:293-314);
+//     gridding_barrier() synchronises;
+//   * weight_uniformly / normalize operate on the caller's host buffers after the copy-back,
+//     exactly as the reference (wrapper.cu:275-339);
+//   * finalize / finalize_psf run the inverse FFT on the device (cuFFT) with the reference's
+//     shift and float32 packing (fft_and_repacking_routines.cpp:83-161).
+// Deliberate differences (none changes results):
+//   * no cudaDeviceReset and no device selection: the current device is used (the reference
+//     resets and picks the device with most SMs, wrapper.cu:89-112);
+//   * errors never exit or throw: they are recorded (sticky) and readable through
+//     bullseye_last_error(); calls after an error return without work until initLibrary;
+//   * single/dual correlation selection happens on the device; caller arrays are not compacted
+//     in place (the reference compacts them, wrapper.cu:482-490, 666-680);
+//   * Jones terms are inverted on the device into a library buffer; the caller's array is left
+//     unmodified (the reference GPU library inverts a host copy, wrapper.cu:1088);
+//   * the Jones correction is applied (the reference GPU library launches the plain 4-correlation
+//     policy for facet_4_cor_corrections, wrapper.cu:1125, so its GPU results ignore the terms;
+//     the CPU library applies them, correlation_gridding_policies.h:523-542, and is the oracle).
+#include <cufft.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "common.h"
+#include "gridder.cuh"
+#include "kernels_misc.cuh"
+
+using namespace bz;
+
+// ------------------------------------------------------------------ error state
+static std::mutex g_err_mutex;
+static int g_err_code = BZ_OK;
+static std::string g_err_msg;
+
+void bz_record_error(int code, const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  std::lock_guard<std::mutex> lk(g_err_mutex);
+  if (g_err_code == BZ_OK) {  // keep the first error
+    g_err_code = code;
+    g_err_msg = buf;
+  }
+}
+int bz_error_code() {
+  std::lock_guard<std::mutex> lk(g_err_mutex);
+  return g_err_code;
+}
+static void bz_clear_error() {
+  std::lock_guard<std::mutex> lk(g_err_mutex);
+  g_err_code = BZ_OK;
+  g_err_msg.clear();
+}
+
+// ------------------------------------------------------------------ device buffer helper
+template <typename T>
+struct DevBuf {
+  T *ptr = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  bool alloc(size_t count) {
+    release();
+    if (count == 0) count = 1;
+    if (cudaMalloc((void **)&ptr, sizeof(T) * count) != cudaSuccess) {
+      ptr = nullptr;
+      bz_record_error(BZ_ERR_CUDA, "cudaMalloc of %zu bytes failed", sizeof(T) * count);
+      return false;
+    }
+    n = count;
+    return true;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    n = 0;
+  }
+};
+
+// ------------------------------------------------------------------ library context
+struct Context {
+  bool initialized = false;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev_g0 = nullptr, ev_g1 = nullptr, ev_i0 = nullptr, ev_i1 = nullptr;
+  bool grid_timing_pending = false, inv_timing_pending = false;
+  double grid_seconds = 0.0, inv_seconds = 0.0;
+  bool compensated = true;  // FP32: compensated (hi/lo) grid accumulation
+  bool device_inputs = false;  // row arrays, Jones terms and baseline starts are device pointers
+  long long launches = 0;      // kernels launched by this library since initLibrary
+  cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;  // around the last gridder launch
+  bool kernel_timing_pending = false;
+  int kernel_timing_kind = 0;  // 0 visibilities, 1 sampling function
+  double kernel_ms[2] = {0.0, 0.0};  // accumulated gridder kernel time (ms) per kind
+  long long kernel_count[2] = {0, 0};
+
+  // sizes fixed at init
+  size_t F = 1, cube = 1, C = 1, nx = 0, ny = 0, sf_count = 0, W = 1, os = 1, K = 1, P = 1;
+  size_t nchan = 1, nspw = 1, npol = 1, max_rows = 0, baselines = 0;
+  bool want_sf = false;
+
+  // device tables
+  DevBuf<vis_real> conv, wavelengths, facet_centres;
+  DevBuf<uint8_t> enabled;
+  DevBuf<size_t> cgi, sf_cgi;
+  // device row buffers (chunk_max_row_count rows)
+  DevBuf<vis_complex> vis;
+  DevBuf<vis_real> weights, uvw;
+  DevBuf<uint8_t> flags, flagged_rows;
+  DevBuf<unsigned> field, spw, ant1, ant2;
+  DevBuf<size_t> time_ids, starts;
+  DevBuf<vis_complex> jones_raw, jones_inv;
+  DevBuf<FacetXform> facets;
+  // grids
+  DevBuf<vis_complex> grid, grid_lo, sf, sf_lo, scratch;
+  DevBuf<double> norm;
+  DevBuf<int> dev_error;
+  std::vector<double> host_norm;  // published through params.normalization_terms
+  // gridding correction (detaper) factors for finalize, optional
+  DevBuf<double> corr_x, corr_y;
+  bool have_corr = false;
+};
+static Context g_ctx;
+
+static bool check_ready(const char *fn) {
+  if (!g_ctx.initialized) {
+    bz_record_error(BZ_ERR_NOT_INITIALISED, "%s called before initLibrary", fn);
+    return false;
+  }
+  return bz_error_code() == BZ_OK;
+}
+
+static void drain_device_error() {
+  int h = 0;
+  if (g_ctx.dev_error.ptr && cudaMemcpy(&h, g_ctx.dev_error.ptr, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess && h) {
+    if (h & DEV_ERR_SINGULAR) bz_record_error(BZ_ERR_SINGULAR_JONES, "Jones matrix set contains singular matrices");
+    if (h & DEV_ERR_GRID_INDEX) bz_record_error(BZ_ERR_INVALID_ARGUMENT, "channel grid index out of range of the cube");
+    if (h & DEV_ERR_JONES_INDEX) bz_record_error(BZ_ERR_INVALID_ARGUMENT, "timestamp or antenna id out of range of the Jones terms");
+    int z = 0;
+    cudaMemcpy(g_ctx.dev_error.ptr, &z, sizeof(int), cudaMemcpyHostToDevice);
+  }
+}
+
+// Fold the previous gridder launch's event interval into the per-kind totals.
+static void settle_kernel_timing() {
+  Context &c = g_ctx;
+  if (!c.kernel_timing_pending) return;
+  float ms = 0;
+  cudaEventSynchronize(c.ev_k1);
+  if (cudaEventElapsedTime(&ms, c.ev_k0, c.ev_k1) == cudaSuccess) c.kernel_ms[c.kernel_timing_kind] += ms;
+  c.kernel_timing_pending = false;
+}
+
+// ------------------------------------------------------------------ exported API
+
+extern "C" int bullseye_last_error(char *buf, size_t n) {
+  std::lock_guard<std::mutex> lk(g_err_mutex);
+  if (buf && n) {
+    snprintf(buf, n, "%s", g_err_msg.c_str());
+  }
+  return g_err_code;
+}
+
+extern "C" void bullseye_clear_error() { bz_clear_error(); }
+
+extern "C" int bullseye_precision_bits() { return BZ_PRECISION_BITS; }
+
+extern "C" void bullseye_set_compensated(int on) { g_ctx.compensated = on != 0; }
+
+// Device-resident inputs: when on, the row arrays (visibilities, weights, flags, uvw, flagged
+// rows, field, spw, antenna and timestamp ids), jones_terms and baseline_starting_indexes in
+// gridding_parameters are device pointers already in baseline-major order; the gridding calls
+// then copy nothing from the host.  Tables and grids are still owned by the library.
+extern "C" void bullseye_set_device_inputs(int on) { g_ctx.device_inputs = on != 0; }
+
+// The library's CUDA stream (all its work is ordered on it); null before initLibrary.
+extern "C" void *bullseye_get_stream() { return (void *)g_ctx.stream; }
+
+// Number of kernels this library launched since initLibrary (cuFFT's internal launches excluded).
+extern "C" long long bullseye_kernel_launches() { return g_ctx.launches; }
+
+// Accumulated device time of the gridder kernels (ms, CUDA events around each launch) and the
+// number of gridder launches timed, since initLibrary or the last reset.
+// kind 0: visibility gridding launches, kind 1: sampling-function launches.
+extern "C" double bullseye_gridder_kernel_ms(int kind, long long *count) {
+  Context &c = g_ctx;
+  if (kind < 0 || kind > 1) return 0.0;
+  settle_kernel_timing();
+  if (count) *count = c.kernel_count[kind];
+  return c.kernel_ms[kind];
+}
+
+extern "C" void bullseye_reset_counters() {
+  Context &c = g_ctx;
+  settle_kernel_timing();
+  c.kernel_ms[0] = c.kernel_ms[1] = 0;
+  c.kernel_count[0] = c.kernel_count[1] = 0;
+  c.launches = 0;
+}
+
+// Measured FP32 FMA throughput of this GPU (TFLOP/s): independent FMA chains in registers on
+// every SM, timed with CUDA events.  The denominator of the gridder's FP32 roofline.
+extern "C" double bullseye_fp32_fma_tflops(int iters) {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return 0.0;
+  const int threads = 256, blocks = sms * 8;
+  float *out = nullptr;
+  if (cudaMalloc(&out, sizeof(float) * threads * blocks) != cudaSuccess) return 0.0;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  fma_probe_kernel<<<blocks, threads>>>(out, iters);  // warm-up
+  cudaEventRecord(e0);
+  fma_probe_kernel<<<blocks, threads>>>(out, iters);
+  cudaEventRecord(e1);
+  cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  double flops = 2.0 * kFmaProbeChains * (double)iters * threads * blocks;
+  return ms > 0 ? flops / (ms * 1e-3) / 1e12 : 0.0;
+}
+
+// Zero the device-resident grids, compensation grids and normalisation sums (a fresh image
+// without reallocating; the caller's host buffers are untouched).
+extern "C" void bullseye_zero_grids() {
+  Context &c = g_ctx;
+  if (!check_ready("bullseye_zero_grids")) return;
+  const size_t nxy = c.nx * c.ny;
+  BZ_CUDA_TRY(cudaMemsetAsync(c.grid.ptr, 0, sizeof(vis_complex) * c.F * c.cube * c.C * nxy, c.stream));
+  if (c.grid_lo.ptr) BZ_CUDA_TRY(cudaMemsetAsync(c.grid_lo.ptr, 0, sizeof(vis_complex) * c.F * c.cube * c.C * nxy, c.stream));
+  if (c.sf.ptr) BZ_CUDA_TRY(cudaMemsetAsync(c.sf.ptr, 0, sizeof(vis_complex) * c.F * c.sf_count * nxy, c.stream));
+  if (c.sf_lo.ptr) BZ_CUDA_TRY(cudaMemsetAsync(c.sf_lo.ptr, 0, sizeof(vis_complex) * c.F * c.sf_count * nxy, c.stream));
+  BZ_CUDA_TRY(cudaMemsetAsync(c.norm.ptr, 0, sizeof(double) * c.F * c.cube * c.C, c.stream));
+}
+
+extern "C" double get_gridding_walltime() {
+  if (g_ctx.grid_timing_pending && g_ctx.ev_g1) {
+    cudaEventSynchronize(g_ctx.ev_g1);
+  }
+  return g_ctx.grid_seconds;
+}
+
+extern "C" double get_inversion_walltime() { return g_ctx.inv_seconds; }
+
+extern "C" void gridding_barrier() {
+  if (!g_ctx.initialized || !g_ctx.stream) return;
+  cudaError_t e = cudaStreamSynchronize(g_ctx.stream);
+  if (e != cudaSuccess) {
+    bz_record_error(BZ_ERR_CUDA, "gridding_barrier: %s", cudaGetErrorString(e));
+    return;
+  }
+  drain_device_error();
+}
+
+static void timer_start() {
+  if (g_ctx.grid_timing_pending) {
+    float ms = 0;
+    cudaEventSynchronize(g_ctx.ev_g1);
+    if (cudaEventElapsedTime(&ms, g_ctx.ev_g0, g_ctx.ev_g1) == cudaSuccess) g_ctx.grid_seconds += ms * 1e-3;
+    g_ctx.grid_timing_pending = false;
+  }
+  cudaEventRecord(g_ctx.ev_g0, g_ctx.stream);
+}
+static void timer_stop() {
+  cudaEventRecord(g_ctx.ev_g1, g_ctx.stream);
+  g_ctx.grid_timing_pending = true;
+}
+
+extern "C" void releaseLibrary();
+
+extern "C" void initLibrary(gridding_parameters *pp) {
+  if (g_ctx.initialized) return;  // as the reference (wrapper.cu:82)
+  bz_clear_error();
+  gridding_parameters &p = *pp;
+  Context &c = g_ctx;
+  if (cudaGetDevice(&c.device) != cudaSuccess) {
+    bz_record_error(BZ_ERR_CUDA, "no CUDA device available");
+    return;
+  }
+  if (p.nx == 0 || p.ny == 0 || p.conv_oversample == 0 || p.channel_count == 0 || p.spw_count == 0) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "initLibrary: nx, ny, conv_oversample, channel_count and spw_count must be > 0");
+    return;
+  }
+  c.F = std::max<size_t>(1, p.num_facet_centres);
+  c.cube = p.cube_channel_dim_size;
+  c.C = p.number_of_polarization_terms_being_gridded;
+  c.nx = p.nx;
+  c.ny = p.ny;
+  c.W = 2 * p.conv_support + 1;
+  c.os = p.conv_oversample;
+  c.K = (c.W + 2) + (c.W + 1) * (c.os - 1);
+  c.P = std::max<size_t>(1, p.wplanes);
+  c.nchan = p.channel_count;
+  c.nspw = p.spw_count;
+  c.npol = p.number_of_polarization_terms;
+  c.max_rows = p.chunk_max_row_count;
+  c.baselines = p.baseline_count;
+  c.want_sf = p.should_grid_sampling_function;
+  c.sf_count = c.want_sf ? p.sampling_function_channel_count : 0;
+  c.grid_seconds = c.inv_seconds = 0;
+  c.grid_timing_pending = c.inv_timing_pending = false;
+  if (c.C != 1 && c.C != 2 && c.C != 4) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "number_of_polarization_terms_being_gridded must be 1, 2 or 4");
+    return;
+  }
+  if (c.cube == 0) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "cube_channel_dim_size must be > 0");
+    return;
+  }
+  if (!p.conv) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "initLibrary: conv is null");
+    return;
+  }
+  BZ_CUDA_TRY(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+  BZ_CUDA_TRY(cudaEventCreate(&c.ev_g0));
+  BZ_CUDA_TRY(cudaEventCreate(&c.ev_g1));
+  BZ_CUDA_TRY(cudaEventCreate(&c.ev_i0));
+  BZ_CUDA_TRY(cudaEventCreate(&c.ev_i1));
+  BZ_CUDA_TRY(cudaEventCreate(&c.ev_k0));
+  BZ_CUDA_TRY(cudaEventCreate(&c.ev_k1));
+  c.launches = 0;
+  c.kernel_ms[0] = c.kernel_ms[1] = 0;
+  c.kernel_count[0] = c.kernel_count[1] = 0;
+  c.kernel_timing_pending = false;
+  const size_t sc = c.nchan * c.nspw;
+  const size_t nxy = c.nx * c.ny;
+  const bool wproj = p.wplanes > 1;
+  const size_t conv_elems = wproj ? c.P * c.K * 2 : c.K;
+  bool ok = c.conv.alloc(conv_elems) && c.wavelengths.alloc(sc) && c.enabled.alloc(sc) && c.cgi.alloc(sc) &&
+            c.sf_cgi.alloc(sc) && c.facet_centres.alloc(2 * c.F) && c.facets.alloc(c.F) &&
+            c.dev_error.alloc(1) && c.norm.alloc(c.F * c.cube * c.C);
+  if (!ok) return;
+  BZ_CUDA_TRY(cudaMemcpy(c.conv.ptr, p.conv, sizeof(vis_real) * conv_elems, cudaMemcpyHostToDevice));
+  BZ_CUDA_TRY(cudaMemcpy(c.wavelengths.ptr, p.reference_wavelengths, sizeof(vis_real) * sc, cudaMemcpyHostToDevice));
+  BZ_CUDA_TRY(cudaMemcpy(c.enabled.ptr, p.enabled_channels, sc, cudaMemcpyHostToDevice));
+  BZ_CUDA_TRY(cudaMemcpy(c.cgi.ptr, p.channel_grid_indicies, sizeof(size_t) * sc, cudaMemcpyHostToDevice));
+  if (c.want_sf && p.sampling_function_channel_grid_indicies)
+    BZ_CUDA_TRY(cudaMemcpy(c.sf_cgi.ptr, p.sampling_function_channel_grid_indicies, sizeof(size_t) * sc,
+                           cudaMemcpyHostToDevice));
+  if (p.facet_centres)
+    BZ_CUDA_TRY(cudaMemcpy(c.facet_centres.ptr, p.facet_centres, sizeof(vis_real) * 2 * c.F, cudaMemcpyHostToDevice));
+  BZ_CUDA_TRY(cudaMemset(c.dev_error.ptr, 0, sizeof(int)));
+  BZ_CUDA_TRY(cudaMemset(c.norm.ptr, 0, sizeof(double) * c.F * c.cube * c.C));
+  // row buffers are allocated on the first host-input gridding call (ensure_row_buffers)
+  // grids: the caller's initial contents are uploaded (wrapper.cu:179-186)
+  const size_t ng = c.F * c.cube * c.C * nxy;
+  if (!c.grid.alloc(ng) || !c.scratch.alloc(std::max(ng, c.F * std::max<size_t>(1, c.sf_count) * nxy))) return;
+  if (p.output_buffer)
+    BZ_CUDA_TRY(cudaMemcpy(c.grid.ptr, p.output_buffer, sizeof(vis_complex) * ng, cudaMemcpyHostToDevice));
+  else
+    BZ_CUDA_TRY(cudaMemset(c.grid.ptr, 0, sizeof(vis_complex) * ng));
+#if defined(BULLSEYE_SINGLE)
+  if (!c.grid_lo.alloc(ng)) return;
+  BZ_CUDA_TRY(cudaMemset(c.grid_lo.ptr, 0, sizeof(vis_complex) * ng));
+#endif
+  if (c.want_sf) {
+    const size_t ns = c.F * c.sf_count * nxy;
+    if (!c.sf.alloc(ns)) return;
+    if (p.sampling_function_buffer)
+      BZ_CUDA_TRY(cudaMemcpy(c.sf.ptr, p.sampling_function_buffer, sizeof(vis_complex) * ns, cudaMemcpyHostToDevice));
+    else
+      BZ_CUDA_TRY(cudaMemset(c.sf.ptr, 0, sizeof(vis_complex) * ns));
+#if defined(BULLSEYE_SINGLE)
+    if (!c.sf_lo.alloc(ns)) return;
+    BZ_CUDA_TRY(cudaMemset(c.sf_lo.ptr, 0, sizeof(vis_complex) * ns));
+#endif
+  }
+  // library-owned normalisation terms in the GPU library's layout
+  const size_t bins = c.W * c.W;
+  c.host_norm.assign(c.F * c.cube * c.C * bins, 0.0);
+  p.normalization_terms = c.host_norm.data();
+  c.have_corr = false;
+  c.initialized = true;
+}
+
+extern "C" void releaseLibrary() {
+  Context &c = g_ctx;
+  if (!c.initialized) return;
+  if (c.stream) cudaStreamSynchronize(c.stream);
+  c.conv.release(); c.wavelengths.release(); c.facet_centres.release(); c.enabled.release();
+  c.cgi.release(); c.sf_cgi.release(); c.vis.release(); c.weights.release(); c.uvw.release();
+  c.flags.release(); c.flagged_rows.release(); c.field.release(); c.spw.release(); c.ant1.release();
+  c.ant2.release(); c.time_ids.release(); c.starts.release(); c.jones_raw.release(); c.jones_inv.release();
+  c.facets.release(); c.grid.release(); c.grid_lo.release(); c.sf.release(); c.sf_lo.release();
+  c.scratch.release(); c.norm.release(); c.dev_error.release(); c.corr_x.release(); c.corr_y.release();
+  if (c.ev_g0) cudaEventDestroy(c.ev_g0);
+  if (c.ev_g1) cudaEventDestroy(c.ev_g1);
+  if (c.ev_i0) cudaEventDestroy(c.ev_i0);
+  if (c.ev_i1) cudaEventDestroy(c.ev_i1);
+  if (c.ev_k0) cudaEventDestroy(c.ev_k0);
+  if (c.ev_k1) cudaEventDestroy(c.ev_k1);
+  c.ev_g0 = c.ev_g1 = c.ev_i0 = c.ev_i1 = c.ev_k0 = c.ev_k1 = nullptr;
+  if (c.stream) cudaStreamDestroy(c.stream);
+  c.stream = nullptr;
+  c.host_norm.clear();
+  c.host_norm.shrink_to_fit();
+  c.initialized = false;
+}
+
+// ---------------------------------------------------------------- repack (host, as reference)
+static long baseline_slot(long a1, long a2, long n) {
+  long s = std::min(a1, a2);
+  return (s * (-s + (2 * n + 1))) / 2 + std::labs(a1 - a2);
+}
+
+// Stable counting sort of the chunk's rows into baseline-major order, in place on the caller's
+// arrays, filling baseline_starting_indexes (bullseye/mo/gpu_algorithm/wrapper.cu:367-454).
+extern "C" void repack_input_data(gridding_parameters *pp) {
+  gridding_parameters &p = *pp;
+  // pure host work: usable before initLibrary, like the reference (wrapper.cu:367)
+  if (bz_error_code() != BZ_OK) return;
+  if (!p.baseline_starting_indexes || !p.antenna_1_ids || !p.antenna_2_ids) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "repack_input_data: baseline_starting_indexes and antenna ids are required");
+    return;
+  }
+  const size_t R = p.row_count, B = p.baseline_count, per = p.channel_count * p.number_of_polarization_terms;
+  std::vector<size_t> slot(R);
+  std::fill(p.baseline_starting_indexes, p.baseline_starting_indexes + B + 1, 0);
+  for (size_t r = 0; r < R; ++r) {
+    long b = baseline_slot(p.antenna_1_ids[r], p.antenna_2_ids[r], (long)p.antenna_count);
+    if (b < 0 || (size_t)b >= B) {
+      bz_record_error(BZ_ERR_INVALID_ARGUMENT, "repack_input_data: antenna pair outside baseline_count");
+      return;
+    }
+    slot[r] = (size_t)b;
+    ++p.baseline_starting_indexes[b + 1];
+  }
+  std::partial_sum(p.baseline_starting_indexes, p.baseline_starting_indexes + B + 1, p.baseline_starting_indexes);
+  std::vector<size_t> dest(R), cursor(p.baseline_starting_indexes, p.baseline_starting_indexes + B);
+  for (size_t r = 0; r < R; ++r) dest[r] = cursor[slot[r]]++;
+  auto permute = [&](auto *arr, size_t width) {
+    if (!arr) return;
+    const size_t esz = sizeof(*arr) * width;
+    unsigned char *bytes = reinterpret_cast<unsigned char *>(arr);
+    std::vector<unsigned char> tmp(bytes, bytes + R * esz);
+    for (size_t r = 0; r < R; ++r) std::memcpy(bytes + dest[r] * esz, tmp.data() + r * esz, esz);
+  };
+  permute(p.uvw_coords, 1);
+  permute(p.visibilities, per);
+  permute(p.visibility_weights, per);
+  permute(p.flags, per);
+  permute(p.flagged_rows, 1);
+  permute(p.spw_index_array, 1);
+  permute(p.antenna_1_ids, 1);
+  permute(p.antenna_2_ids, 1);
+  permute(p.field_array, 1);
+  if (p.should_invert_jones_terms) permute(p.timestamp_ids, 1);
+}
+
+// ---------------------------------------------------------------- gridding launch
+static FacetXform facet_xform(double ra0, double dec0, double ra, double dec, bool phase, bool uvx) {
+  // phase_transform_policies.h:110-134 and baseline_transform_policies.h:117-149, in FP64
+  FacetXform x = {0, 0, 0, 0, 0};
+  const double k = (double)kArcsecToRad;
+  double d_ra = (ra - ra0) * k, n_dec = dec * k, o_dec = dec0 * k;
+  double c_d_ra = cos(d_ra), s_d_ra = sin(d_ra), c_n = cos(n_dec), s_n = sin(n_dec), c_o = cos(o_dec),
+         s_o = sin(o_dec);
+  if (uvx) {
+    double li0 = c_n * s_d_ra, mi0 = s_n * c_o - c_n * s_o * c_d_ra, ni0 = s_n * s_o + c_n * c_o * c_d_ra;
+    x.u_term = li0 / ni0;
+    x.v_term = mi0 / ni0;
+  }
+  if (phase) {
+    x.dl = -c_n * s_d_ra;
+    x.dm = -(s_n * c_o - c_n * s_o * c_d_ra);
+    x.dn = 1.0 - sqrt(1.0 - x.dl * x.dl - x.dm * x.dm);
+  }
+  return x;
+}
+
+struct LaunchShape {
+  int J, NT, V;
+  size_t smem;
+};
+
+template <int NC, bool WPROJ>
+static LaunchShape choose_shape(int W) {
+  LaunchShape s;
+  const int Js[] = {1, 2, 4, 8, 16};
+  s.J = 0;
+  for (int j : Js) {
+    if (W * ((W + j - 1) / j) <= 512) {
+      s.J = j;
+      break;
+    }
+  }
+  if (!s.J) {
+    s.J = 16;
+  }
+  int owners = W * ((W + s.J - 1) / s.J);
+  s.NT = std::max(32, ((owners + 31) / 32) * 32);
+  const size_t budget = 96 * 1024;
+  size_t per = sizeof(VisRec<NC>) + sizeof(typename TapT<WPROJ>::type) * 2 * (size_t)W;
+  int V = (int)std::min<size_t>(s.NT, (budget - 64) / per);
+  if (V < 1) V = 1;
+  s.V = V;
+  s.smem = grid_smem_bytes<NC, WPROJ>(V, W);
+  return s;
+}
+
+template <int NC, bool WPROJ, int J>
+static bool launch_j(const GridArgs &a, const LaunchShape &s, long long blocks, cudaStream_t st, bool comp) {
+  void (*kern)(const GridArgs);
+  if (comp)
+    kern = romein_grid_kernel<NC, WPROJ, J, true>;
+  else
+    kern = romein_grid_kernel<NC, WPROJ, J, false>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem) != cudaSuccess) {
+    bz_record_error(BZ_ERR_CUDA, "cudaFuncSetAttribute failed");
+    return false;
+  }
+  kern<<<(unsigned)blocks, s.NT, s.smem, st>>>(a);
+  g_ctx.launches++;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    bz_record_error(BZ_ERR_CUDA, "gridder launch failed: %s", cudaGetErrorString(e));
+    return false;
+  }
+  return true;
+}
+
+template <int NC, bool WPROJ>
+static bool launch_nc(GridArgs a, long long blocks, cudaStream_t st, bool comp) {
+  LaunchShape s = choose_shape<NC, WPROJ>(a.W);
+  if (a.W * ((a.W + s.J - 1) / s.J) > 512) {
+    bz_record_error(BZ_ERR_UNSUPPORTED, "full support %d is larger than this build supports", a.W);
+    return false;
+  }
+  a.V = s.V;
+  switch (s.J) {
+    case 1: return launch_j<NC, WPROJ, 1>(a, s, blocks, st, comp);
+    case 2: return launch_j<NC, WPROJ, 2>(a, s, blocks, st, comp);
+    case 4: return launch_j<NC, WPROJ, 4>(a, s, blocks, st, comp);
+    case 8: return launch_j<NC, WPROJ, 8>(a, s, blocks, st, comp);
+    default: return launch_j<NC, WPROJ, 16>(a, s, blocks, st, comp);
+  }
+}
+
+static bool launch_gridder(const GridArgs &a, int nc, bool wproj, long long blocks, cudaStream_t st, bool comp) {
+  if (blocks <= 0) return true;
+  if (blocks > 0x7fffffffLL) {
+    bz_record_error(BZ_ERR_UNSUPPORTED, "too many gridding work items in one chunk");
+    return false;
+  }
+  if (nc == 1) return wproj ? launch_nc<1, true>(a, blocks, st, comp) : launch_nc<1, false>(a, blocks, st, comp);
+  if (nc == 2) return wproj ? launch_nc<2, true>(a, blocks, st, comp) : launch_nc<2, false>(a, blocks, st, comp);
+  return wproj ? launch_nc<4, true>(a, blocks, st, comp) : launch_nc<4, false>(a, blocks, st, comp);
+}
+
+// Device mirrors for chunk_max_row_count rows (wrapper.cu:146-164), allocated once.
+static bool ensure_row_buffers() {
+  Context &c = g_ctx;
+  if (c.vis.ptr) return true;
+  const size_t R = std::max<size_t>(1, c.max_rows);
+  const size_t RC = R * c.nchan * c.npol;
+  return c.vis.alloc(RC) && c.weights.alloc(RC) && c.flags.alloc(RC) && c.uvw.alloc(3 * R) &&
+         c.flagged_rows.alloc(R) && c.field.alloc(R) && c.spw.alloc(R) && c.ant1.alloc(R) && c.ant2.alloc(R) &&
+         c.time_ids.alloc(R) && c.starts.alloc(c.baselines + 2);
+}
+
+static bool upload_rows(const gridding_parameters &p, bool need_ants, bool need_time) {
+  Context &c = g_ctx;
+  const size_t R = p.row_count;
+  if (c.device_inputs) return true;
+  if (!ensure_row_buffers()) return false;
+  if (R > c.max_rows) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "row_count %zu exceeds chunk_max_row_count %zu", R, c.max_rows);
+    return false;
+  }
+  if (R == 0) return true;
+  const size_t RC = R * c.nchan * c.npol;
+  cudaStream_t s = c.stream;
+  BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.vis.ptr, p.visibilities, sizeof(vis_complex) * RC, cudaMemcpyHostToDevice, s), false);
+  BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.weights.ptr, p.visibility_weights, sizeof(vis_real) * RC, cudaMemcpyHostToDevice, s), false);
+  BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.flags.ptr, p.flags, RC, cudaMemcpyHostToDevice, s), false);
+  BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.uvw.ptr, p.uvw_coords, sizeof(vis_real) * 3 * R, cudaMemcpyHostToDevice, s), false);
+  BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.flagged_rows.ptr, p.flagged_rows, R, cudaMemcpyHostToDevice, s), false);
+  BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.field.ptr, p.field_array, sizeof(unsigned) * R, cudaMemcpyHostToDevice, s), false);
+  BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.spw.ptr, p.spw_index_array, sizeof(unsigned) * R, cudaMemcpyHostToDevice, s), false);
+  if (need_ants) {
+    BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.ant1.ptr, p.antenna_1_ids, sizeof(unsigned) * R, cudaMemcpyHostToDevice, s), false);
+    BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.ant2.ptr, p.antenna_2_ids, sizeof(unsigned) * R, cudaMemcpyHostToDevice, s), false);
+  }
+  if (need_time)
+    BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.time_ids.ptr, p.timestamp_ids, sizeof(size_t) * R, cudaMemcpyHostToDevice, s), false);
+  return true;
+}
+
+// Validates and uploads the caller's baseline starts; returns number of track slots.
+static bool setup_tracks(const gridding_parameters &p, int &nslots, int &seg, const size_t **starts_dev) {
+  Context &c = g_ctx;
+  const size_t R = p.row_count;
+  *starts_dev = nullptr;
+  if (c.device_inputs) {
+    if (p.baseline_starting_indexes) {
+      *starts_dev = p.baseline_starting_indexes;
+      nslots = (int)p.baseline_count;
+      seg = 0;
+      return true;
+    }
+    seg = 256;
+    nslots = (int)((R + seg - 1) / seg);
+    return true;
+  }
+  if (p.baseline_starting_indexes) {
+    const size_t B = p.baseline_count;
+    const size_t *s = p.baseline_starting_indexes;
+    bool ok = s[0] == 0 && s[B] == R;
+    for (size_t b = 0; ok && b < B; ++b) ok = s[b] <= s[b + 1];
+    if (ok && B + 1 <= c.starts.n) {
+      BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.starts.ptr, s, sizeof(size_t) * (B + 1), cudaMemcpyHostToDevice, c.stream), false);
+      *starts_dev = c.starts.ptr;
+      nslots = (int)B;
+      seg = 0;
+      return true;
+    }
+    // starts that do not describe this chunk: fall back to fixed segments
+  }
+  seg = 256;
+  nslots = (int)((R + seg - 1) / seg);
+  return true;
+}
+
+static void copy_back_grids(gridding_parameters &p, bool sampling) {
+  Context &c = g_ctx;
+  const size_t nxy = c.nx * c.ny;
+  if (!sampling) {
+    const size_t n = c.F * c.cube * c.C * nxy;
+    resolve_compensated_kernel<<<1024, 256, 0, c.stream>>>(c.grid.ptr, c.grid_lo.ptr, c.scratch.ptr, (long long)n);
+    c.launches++;
+    if (p.output_buffer)
+      BZ_CUDA_TRY(cudaMemcpyAsync(p.output_buffer, c.scratch.ptr, sizeof(vis_complex) * n, cudaMemcpyDeviceToHost, c.stream));
+    std::vector<double> tmp(c.F * c.cube * c.C);
+    BZ_CUDA_TRY(cudaMemcpyAsync(tmp.data(), c.norm.ptr, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost, c.stream));
+    BZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    const size_t bins = c.W * c.W;
+    std::fill(c.host_norm.begin(), c.host_norm.end(), 0.0);
+    for (size_t i = 0; i < tmp.size(); ++i) c.host_norm[i * bins] = tmp[i];
+  } else {
+    const size_t n = c.F * c.sf_count * nxy;
+    resolve_compensated_kernel<<<1024, 256, 0, c.stream>>>(c.sf.ptr, c.sf_lo.ptr, c.scratch.ptr, (long long)n);
+    c.launches++;
+    if (p.sampling_function_buffer)
+      BZ_CUDA_TRY(cudaMemcpyAsync(p.sampling_function_buffer, c.scratch.ptr, sizeof(vis_complex) * n,
+                                  cudaMemcpyDeviceToHost, c.stream));
+    BZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
+  }
+}
+
+static void grid_common(gridding_parameters *pp, int nc, int mode, bool faceting, const char *name) {
+  gridding_parameters &p = *pp;
+  if (!check_ready(name)) return;
+  Context &c = g_ctx;
+  const bool sampling = mode == CORR_SAMPLING;
+  if (sampling && !c.want_sf) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: library initialised without should_grid_sampling_function", name);
+    return;
+  }
+  if (!sampling && (size_t)nc != c.C) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s grids %d correlations but the library was initialised for %zu", name, nc, c.C);
+    return;
+  }
+  if (nc == 4 && !sampling && c.npol != 4) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s needs 4 polarisation terms per visibility", name);
+    return;
+  }
+  if (!sampling && (p.polarization_index >= c.npol || (nc == 2 && p.second_polarization_index >= c.npol))) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: polarization index out of range", name);
+    return;
+  }
+  timer_start();
+  const bool jones = mode == CORR_QUAD_JONES;
+  if (!upload_rows(p, jones, jones)) return;
+  if (jones) {
+    const size_t nj = p.no_timestamps_read * p.antenna_count * c.F * c.nspw * c.nchan;
+    if (!p.jones_terms || nj == 0) {
+      bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: jones_terms missing", name);
+      return;
+    }
+    if (c.jones_inv.n < 4 * nj && !c.jones_inv.alloc(4 * nj)) return;
+    const vis_complex *jsrc = p.jones_terms;
+    if (!c.device_inputs) {
+      if (c.jones_raw.n < 4 * nj && !c.jones_raw.alloc(4 * nj)) return;
+      BZ_CUDA_TRY(cudaMemcpyAsync(c.jones_raw.ptr, p.jones_terms, sizeof(vis_complex) * 4 * nj, cudaMemcpyHostToDevice, c.stream));
+      jsrc = c.jones_raw.ptr;
+    }
+    invert_jones_kernel<<<(unsigned)((nj + 255) / 256), 256, 0, c.stream>>>(jsrc, c.jones_inv.ptr, (long long)nj,
+                                                                             c.dev_error.ptr);
+    c.launches++;
+  }
+  int nslots = 0, seg = 0;
+  const size_t *starts = nullptr;
+  if (!setup_tracks(p, nslots, seg, &starts)) return;
+  // per-facet transforms (FP64, host)
+  std::vector<FacetXform> fx(c.F);
+  const double ra0 = (double)p.phase_centre_ra, dec0 = (double)p.phase_centre_dec;
+  const bool phase = faceting && !sampling;
+  for (size_t f = 0; f < c.F; ++f) {
+    double ra = ra0, dec = dec0;
+    if (phase && p.facet_centres) {
+      ra = (double)p.facet_centres[2 * f];
+      dec = (double)p.facet_centres[2 * f + 1];
+    }
+    // the sampling-function policy reports the phase centre as facet centre
+    // (phase_transform_policies.h:77-82), so its uv transform is the identity
+    fx[f] = facet_xform(ra0, dec0, ra, dec, phase, faceting);
+  }
+  BZ_CUDA_TRY(cudaMemcpyAsync(c.facets.ptr, fx.data(), sizeof(FacetXform) * c.F, cudaMemcpyHostToDevice, c.stream));
+
+  GridArgs a;
+  std::memset(&a, 0, sizeof a);
+  if (c.device_inputs) {
+    a.vis = p.visibilities; a.weights = p.visibility_weights; a.flags = (const uint8_t *)p.flags;
+    a.uvw = (const vis_real *)p.uvw_coords; a.flagged_rows = (const uint8_t *)p.flagged_rows;
+    a.field = p.field_array; a.spw = p.spw_index_array; a.ant1 = p.antenna_1_ids; a.ant2 = p.antenna_2_ids;
+    a.time_ids = p.timestamp_ids;
+  } else {
+    a.vis = c.vis.ptr; a.weights = c.weights.ptr; a.flags = c.flags.ptr; a.uvw = c.uvw.ptr;
+    a.flagged_rows = c.flagged_rows.ptr; a.field = c.field.ptr; a.spw = c.spw.ptr;
+    a.ant1 = c.ant1.ptr; a.ant2 = c.ant2.ptr; a.time_ids = c.time_ids.ptr;
+  }
+  a.jones_inv = jones ? c.jones_inv.ptr : nullptr;
+  a.starts = starts;
+  a.wavelengths = c.wavelengths.ptr; a.enabled = c.enabled.ptr;
+  a.cgi = sampling ? c.sf_cgi.ptr : c.cgi.ptr;
+  a.conv = c.conv.ptr;
+  a.facets = c.facets.ptr;
+  a.grid = sampling ? c.sf.ptr : c.grid.ptr;
+  a.grid_lo = nullptr;
+#if defined(BULLSEYE_SINGLE)
+  if (c.compensated) a.grid_lo = sampling ? c.sf_lo.ptr : c.grid_lo.ptr;
+#endif
+  a.norm = sampling ? nullptr : c.norm.ptr;
+  a.error = c.dev_error.ptr;
+  a.nrows = (long long)p.row_count;
+  a.nchan = (int)c.nchan; a.npol = (int)c.npol;
+  a.pol0 = (int)p.polarization_index; a.pol1 = (int)p.second_polarization_index;
+  a.nspw = (int)c.nspw; a.nant = (int)p.antenna_count; a.ntimes = (int)p.no_timestamps_read;
+  a.facet_base = 0; a.nfacets_total = (int)c.F;
+  a.groups = (int)(sampling ? c.sf_count : c.cube);
+  a.nx = (int)c.nx; a.ny = (int)c.ny; a.W = (int)c.W; a.os = (int)c.os; a.K = (int)c.K; a.P = (int)c.P;
+  a.mode = mode; a.phase = phase ? 1 : 0; a.uvx = faceting ? 1 : 0;
+  a.nslots = nslots; a.seg = seg;
+  a.imaging_field = p.imaging_field;
+  // u_scale = nx * cell * ARCSEC_TO_RAD, v_scale = -(ny * cell * ARCSEC_TO_RAD) (templated_gridder.h:23-24)
+  a.u_scale = (double)c.nx * (double)p.cell_size_x * (double)kArcsecToRad;
+  a.v_scale = -((double)c.ny * (double)p.cell_size_y * (double)kArcsecToRad);
+  a.gcx = (double)(c.nx / 2 - p.conv_support);
+  a.gcy = (double)(c.ny / 2 - p.conv_support);
+  a.wmax = (double)(float)p.wmax_est;  // the reference divides by (float)wmax_est
+  const int nc_launch = sampling ? 1 : nc;
+  const long long blocks = (long long)c.F * nslots * (long long)c.nchan;
+  settle_kernel_timing();
+  cudaEventRecord(c.ev_k0, c.stream);
+  if (p.row_count > 0 && !launch_gridder(a, nc_launch, p.wplanes > 1, blocks, c.stream, a.grid_lo != nullptr)) return;
+  cudaEventRecord(c.ev_k1, c.stream);
+  c.kernel_timing_pending = true;
+  c.kernel_timing_kind = sampling ? 1 : 0;
+  c.kernel_count[c.kernel_timing_kind]++;
+  if (p.is_final_data_chunk) copy_back_grids(p, sampling);
+  timer_stop();
+}
+
+extern "C" void grid_single_pol(gridding_parameters *p) { grid_common(p, 1, CORR_SINGLE, false, "grid_single_pol"); }
+extern "C" void facet_single_pol(gridding_parameters *p) { grid_common(p, 1, CORR_SINGLE, true, "facet_single_pol"); }
+extern "C" void grid_duel_pol(gridding_parameters *p) { grid_common(p, 2, CORR_DUAL, false, "grid_duel_pol"); }
+extern "C" void facet_duel_pol(gridding_parameters *p) { grid_common(p, 2, CORR_DUAL, true, "facet_duel_pol"); }
+extern "C" void grid_4_cor(gridding_parameters *p) { grid_common(p, 4, CORR_QUAD, false, "grid_4_cor"); }
+extern "C" void facet_4_cor(gridding_parameters *p) { grid_common(p, 4, CORR_QUAD, true, "facet_4_cor"); }
+extern "C" void facet_4_cor_corrections(gridding_parameters *p) {
+  grid_common(p, 4, CORR_QUAD_JONES, true, "facet_4_cor_corrections");
+}
+extern "C" void grid_sampling_function(gridding_parameters *p) {
+  grid_common(p, 1, CORR_SAMPLING, false, "grid_sampling_function");
+}
+extern "C" void facet_sampling_function(gridding_parameters *p) {
+  grid_common(p, 1, CORR_SAMPLING, true, "facet_sampling_function");
+}
+
+// ---------------------------------------------------------------- host post-processing
+template <typename Fn>
+static void parallel_for(size_t n, Fn fn) {
+  unsigned nt = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+  if (n < 4096 || nt == 1) {
+    fn(0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  size_t step = (n + nt - 1) / nt;
+  for (unsigned t = 0; t < nt; ++t) {
+    size_t lo = t * step, hi = std::min(n, lo + step);
+    if (lo >= hi) break;
+    th.emplace_back([=] { fn(lo, hi); });
+  }
+  for (auto &x : th) x.join();
+}
+
+// wrapper.cu:275-291 (identical to the CPU library, wrapper.cpp:116-135): per cell,
+// divide by 1e-7 + sum of the sampling-function real parts whose channel maps to the cube slice
+// (channel_grid_indicies compared with the sampling-function channel index, as the reference).
+extern "C" void weight_uniformly(gridding_parameters *pp) {
+  gridding_parameters &p = *pp;
+  if (!check_ready("weight_uniformly")) return;
+  gridding_barrier();
+  if (!p.sampling_function_buffer || !p.output_buffer) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "weight_uniformly: sampling function and output buffers are required");
+    return;
+  }
+  const size_t F = std::max<size_t>(1, p.num_facet_centres), G = p.cube_channel_dim_size, nx = p.nx, ny = p.ny,
+               S = p.sampling_function_channel_count, C = p.number_of_polarization_terms_being_gridded;
+  const vis_real eps = (vis_real)0.0000001f;
+  parallel_for(F * G * ny, [&](size_t lo, size_t hi) {
+    for (size_t idx = lo; idx < hi; ++idx) {
+      size_t y = idx % ny, fg = idx / ny, g = fg % G, f = fg / G;
+      for (size_t x = 0; x < nx; ++x) {
+        vis_real count = eps;
+        for (size_t s = 0; s < S; ++s)
+          count += (int)(p.channel_grid_indicies[s] == g) *
+                   p.sampling_function_buffer[((f * S + s) * ny + y) * nx + x].re;
+        count = 1 / count;
+        for (size_t corr = 0; corr < C; ++corr) {
+          vis_complex &v = p.output_buffer[(((f * G + g) * C + corr) * ny + y) * nx + x];
+          v.re *= count;
+          v.im *= count;
+        }
+      }
+    }
+  });
+}
+
+// wrapper.cu:315-339: sum the normalisation bins, divide each (facet, cube, corr) slice.
+// complex<float> /= double divides by the value rounded to float (as the reference).
+extern "C" void normalize(gridding_parameters *pp) {
+  gridding_parameters &p = *pp;
+  if (!check_ready("normalize")) return;
+  gridding_barrier();
+  if (!p.output_buffer || !p.normalization_terms) return;
+  const size_t F = std::max<size_t>(1, p.num_facet_centres), G = p.cube_channel_dim_size, C = p.number_of_polarization_terms_being_gridded,
+               nxy = p.nx * p.ny, bins = (2 * p.conv_support + 1) * (2 * p.conv_support + 1);
+  std::vector<vis_real> div(F * G * C);
+  for (size_t s = 0; s < F * G * C; ++s) {
+    double v = 0;
+    for (size_t b = 0; b < bins; ++b) v += p.normalization_terms[s * bins + b];
+    div[s] = (vis_real)v;
+  }
+  parallel_for(F * G * C * p.ny, [&](size_t lo, size_t hi) {
+    for (size_t idx = lo; idx < hi; ++idx) {
+      size_t s = idx / p.ny, y = idx % p.ny;
+      vis_real d = div[s];
+      vis_complex *row = p.output_buffer + s * nxy + y * p.nx;
+      for (size_t x = 0; x < p.nx; ++x) {
+        row[x].re /= d;
+        row[x].im /= d;
+      }
+    }
+  });
+}
+
+// ---------------------------------------------------------------- finalize (cuFFT)
+static void finalize_buffer(vis_complex *host, size_t per_facet_slices, size_t nslices, const char *name) {
+  Context &c = g_ctx;
+  const size_t nxy = c.nx * c.ny, F = c.F;
+  if (!host || nslices == 0) return;
+  const size_t total = F * nslices * nxy;
+  DevBuf<vis_complex> work, shifted;
+  DevBuf<float> packed;
+  if (!work.alloc(total) || !shifted.alloc(total) || !packed.alloc(total)) return;
+  cudaStream_t s = c.stream;
+  cudaEventRecord(c.ev_i0, s);
+  // upload the first nslices slices of every facet block
+  for (size_t f = 0; f < F; ++f)
+    BZ_CUDA_TRY(cudaMemcpyAsync(shifted.ptr + f * nslices * nxy, host + f * per_facet_slices * nxy,
+                                sizeof(vis_complex) * nslices * nxy, cudaMemcpyHostToDevice, s));
+  ifftshift_gather_kernel<<<2048, 256, 0, s>>>(shifted.ptr, work.ptr, (int)c.nx, (int)c.ny, (long long)(F * nslices));
+  c.launches += 2;  // the gather and the packing kernel (cuFFT's own launches are not counted)
+  cufftHandle plan;
+  int dims[2] = {(int)c.ny, (int)c.nx};
+#if defined(BULLSEYE_SINGLE)
+  cufftType type = CUFFT_C2C;
+#else
+  cufftType type = CUFFT_Z2Z;
+#endif
+  if (cufftPlanMany(&plan, 2, dims, nullptr, 1, (int)nxy, nullptr, 1, (int)nxy, type, (int)(F * nslices)) != CUFFT_SUCCESS) {
+    bz_record_error(BZ_ERR_CUFFT, "%s: cufftPlanMany failed", name);
+    return;
+  }
+  cufftSetStream(plan, s);
+#if defined(BULLSEYE_SINGLE)
+  cufftResult r = cufftExecC2C(plan, (cufftComplex *)work.ptr, (cufftComplex *)work.ptr, CUFFT_INVERSE);
+#else
+  cufftResult r = cufftExecZ2Z(plan, (cufftDoubleComplex *)work.ptr, (cufftDoubleComplex *)work.ptr, CUFFT_INVERSE);
+#endif
+  if (r != CUFFT_SUCCESS) {
+    cufftDestroy(plan);
+    bz_record_error(BZ_ERR_CUFFT, "%s: cufftExec failed", name);
+    return;
+  }
+  const double *cx = c.have_corr ? c.corr_x.ptr : nullptr, *cy = c.have_corr ? c.corr_y.ptr : nullptr;
+  fftshift_pack_kernel<<<2048, 256, 0, s>>>(work.ptr, shifted.ptr, packed.ptr, (int)c.nx, (int)c.ny,
+                                            (long long)(F * nslices), cx, cy);
+  // transformed complex slices back into their facet blocks, then the packed float32 images at
+  // float index (per_facet_slices * nxy) * f, in that order (fft_and_repacking_routines.cpp:85-117)
+  for (size_t f = 0; f < F; ++f)
+    BZ_CUDA_TRY(cudaMemcpyAsync(host + f * per_facet_slices * nxy, shifted.ptr + f * nslices * nxy,
+                                sizeof(vis_complex) * nslices * nxy, cudaMemcpyDeviceToHost, s));
+  float *hf = reinterpret_cast<float *>(host);
+  for (size_t f = 0; f < F; ++f)
+    BZ_CUDA_TRY(cudaMemcpyAsync(hf + f * per_facet_slices * nxy, packed.ptr + f * nslices * nxy, sizeof(float) * nslices * nxy,
+                                cudaMemcpyDeviceToHost, s));
+  cudaEventRecord(c.ev_i1, s);
+  BZ_CUDA_TRY(cudaStreamSynchronize(s));
+  float ms = 0;
+  if (cudaEventElapsedTime(&ms, c.ev_i0, c.ev_i1) == cudaSuccess) c.inv_seconds += ms * 1e-3;
+  cufftDestroy(plan);
+  work.release();
+  shifted.release();
+  packed.release();
+}
+
+extern "C" void finalize(gridding_parameters *pp) {
+  if (!check_ready("finalize")) return;
+  gridding_barrier();
+  finalize_buffer(pp->output_buffer, pp->cube_channel_dim_size * pp->number_of_polarization_terms_being_gridded,
+                  pp->cube_channel_dim_size, "finalize");
+}
+
+extern "C" void finalize_psf(gridding_parameters *pp) {
+  if (!check_ready("finalize_psf")) return;
+  gridding_barrier();
+  if (!g_ctx.want_sf) return;
+  finalize_buffer(pp->sampling_function_buffer, pp->sampling_function_channel_count,
+                  pp->sampling_function_channel_count, "finalize_psf");
+}
+
+// Gridding correction (detaper) for finalize: image[y][x] /= corr_x[x] * corr_y[y].  Passing
+// null pointers switches it off (the default, which reproduces the reference's finalize).
+extern "C" void bullseye_set_gridding_correction(const double *corr_x, size_t nx, const double *corr_y, size_t ny) {
+  Context &c = g_ctx;
+  if (!check_ready("bullseye_set_gridding_correction")) return;
+  if (!corr_x || !corr_y) {
+    c.have_corr = false;
+    return;
+  }
+  if (nx != c.nx || ny != c.ny) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "gridding correction sizes must equal nx, ny");
+    return;
+  }
+  if (!c.corr_x.alloc(nx) || !c.corr_y.alloc(ny)) return;
+  BZ_CUDA_TRY(cudaMemcpy(c.corr_x.ptr, corr_x, sizeof(double) * nx, cudaMemcpyHostToDevice));
+  BZ_CUDA_TRY(cudaMemcpy(c.corr_y.ptr, corr_y, sizeof(double) * ny, cudaMemcpyHostToDevice));
+  c.have_corr = true;
+}
+

@@ -1,0 +1,114 @@
+// Small device kernels around the gridder: Jones inversion, compensated-grid resolution,
+// and the finalize (shift / real-part packing / gridding correction) passes.
+#pragma once
+#include "common.h"
+
+namespace bz {
+
+// Invert every 2x2 Jones matrix (jones_2x2.h:86-126).  Singular matrices (determinant exactly
+// zero) are replaced by zeros and flagged; the reference throws instead.
+__global__ void invert_jones_kernel(const vis_complex *__restrict__ in, vis_complex *__restrict__ out,
+                                    long long n, int *error) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  typedef vis_real T;
+  vis_complex a = in[4 * i], b = in[4 * i + 1], c = in[4 * i + 2], d = in[4 * i + 3];
+  T dr = (a.re * d.re - a.im * d.im) - (b.re * c.re - b.im * c.im);
+  T di = (a.re * d.im + a.im * d.re) - (b.re * c.im + b.im * c.re);
+  vis_complex z = {0, 0};
+  if (dr == (T)0 && di == (T)0) {
+    atomicOr(error, 4);
+    out[4 * i] = z; out[4 * i + 1] = z; out[4 * i + 2] = z; out[4 * i + 3] = z;
+    return;
+  }
+  // 1 / det with scaling (Smith's method) to avoid overflow
+  T ir, ii;
+  if (fabs((double)dr) >= fabs((double)di)) {
+    T r = di / dr, den = dr + di * r;
+    ir = (T)1 / den;
+    ii = -r / den;
+  } else {
+    T r = dr / di, den = dr * r + di;
+    ir = r / den;
+    ii = (T)-1 / den;
+  }
+  auto mul = [](vis_complex x, T yr, T yi) {
+    vis_complex o;
+    o.re = x.re * yr - x.im * yi;
+    o.im = x.re * yi + x.im * yr;
+    return o;
+  };
+  out[4 * i] = mul(d, ir, ii);
+  out[4 * i + 1] = mul(b, -ir, -ii);
+  out[4 * i + 2] = mul(c, -ir, -ii);
+  out[4 * i + 3] = mul(a, ir, ii);
+}
+
+// out = hi + lo (compensated grid resolution), element-wise over complex values.
+__global__ void resolve_compensated_kernel(const vis_complex *__restrict__ hi, const vis_complex *__restrict__ lo,
+                                           vis_complex *__restrict__ out, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    vis_complex h = hi[i];
+    if (lo) {
+      vis_complex l = lo[i];
+      h.re += l.re;
+      h.im += l.im;
+    }
+    out[i] = h;
+  }
+}
+
+// Gather with the inverse shift of numpy's ifftshift: dst[y][x] = src[(y+ny/2)%ny][(x+nx/2)%nx]
+// for each of `slices` planes.  Equivalent to bullseye/mo/cpu_gpu_common/fft_shift_utils.cpp:75-111.
+__global__ void ifftshift_gather_kernel(const vis_complex *__restrict__ src, vis_complex *__restrict__ dst, int nx,
+                                        int ny, long long slices) {
+  long long nxy = (long long)nx * ny;
+  long long total = nxy * slices;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long s = i / nxy, r = i - s * nxy;
+    int y = (int)(r / nx), x = (int)(r - (long long)y * nx);
+    int sy = (y + ny / 2) % ny, sx = (x + nx / 2) % nx;
+    dst[i] = src[s * nxy + (long long)sy * nx + sx];
+  }
+}
+
+// After the transform: fftshift (dst[y][x] = src[(y-ny/2)%ny][(x-nx/2)%nx]) into `shifted`,
+// and the float32 real parts into `packed`, optionally divided by the separable gridding
+// correction corr_x[x] * corr_y[y].
+__global__ void fftshift_pack_kernel(const vis_complex *__restrict__ src, vis_complex *__restrict__ shifted,
+                                     float *__restrict__ packed, int nx, int ny, long long slices,
+                                     const double *__restrict__ corr_x, const double *__restrict__ corr_y) {
+  long long nxy = (long long)nx * ny;
+  long long total = nxy * slices;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long s = i / nxy, r = i - s * nxy;
+    int y = (int)(r / nx), x = (int)(r - (long long)y * nx);
+    int sy = (y + ny - ny / 2) % ny, sx = (x + nx - nx / 2) % nx;
+    vis_complex v = src[s * nxy + (long long)sy * nx + sx];
+    if (shifted) shifted[i] = v;
+    double re = (double)v.re;
+    if (corr_x) re = re / (corr_x[x] * corr_y[y]);
+    packed[i] = (float)re;
+  }
+}
+
+// FP32 FMA throughput probe: kFmaProbeChains independent dependency chains per thread.
+constexpr int kFmaProbeChains = 16;
+__global__ void fma_probe_kernel(float *out, int iters) {
+  float acc[kFmaProbeChains];
+#pragma unroll
+  for (int k = 0; k < kFmaProbeChains; ++k) acc[k] = (float)(threadIdx.x + k) * 1e-3f;
+  const float m = 0.999999f, a = 1e-7f;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < kFmaProbeChains; ++k) acc[k] = fmaf(acc[k], m, a);
+  }
+  float s = 0;
+#pragma unroll
+  for (int k = 0; k < kFmaProbeChains; ++k) s += acc[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+}  // namespace bz

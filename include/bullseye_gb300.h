@@ -1,0 +1,105 @@
+/* C-ABI of the GB300 imaging libraries libgpu_imaging32.so / libgpu_imaging64.so.
+ *
+ * Drop-in for the reference's GPU imaging libraries: the same 19 entry points, the same
+ * argument (a gridding_parameters struct passed by reference, i.e. by pointer in C) and the same
+ * call sequencing (bullseye/bin/bullseye_pipeliner.py:260-424).  Each declaration below cites the
+ * reference interface it replaces.  Precision is chosen by which library is loaded (32: float
+ * data, 64: double data; normalisation terms are double in both), exactly as the reference's
+ * BULLSEYE_SINGLE / BULLSEYE_DOUBLE builds (bullseye/mo/cpu_gpu_common/base_types.h:41-59).
+ *
+ * The struct layout is bullseye/mo/cpu_gpu_common/gridding_parameters.h:44-109 (392 bytes in
+ * the 32-bit library, 408 in the 64-bit one); bullseye_gb300/csrc/common.h defines it with
+ * static_asserts on size and offsets.  It is opaque here.
+ *
+ * Errors never terminate the process: every entry point records the first error (sticky) and
+ * later calls return without work until it is cleared; bullseye_last_error() reports it.
+ */
+#ifndef BULLSEYE_GB300_H
+#define BULLSEYE_GB300_H
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gridding_parameters gridding_parameters;
+
+/* ---- reference entry points (bullseye/mo/cpu_gpu_common/wrapper.h:41-61) ---- */
+
+/* Seconds of device time spent in gridding calls (wrapper.cu:73-75, gpu_algorithm/timer.h). */
+double get_gridding_walltime(void);
+/* Seconds of device time spent in finalize / finalize_psf (wrapper.cu:76-78). */
+double get_inversion_walltime(void);
+/* Wait for queued gridding work and copy-backs (wrapper.cu:79-81). */
+void gridding_barrier(void);
+/* Allocate device state, upload tables and the caller's grids, publish the library-owned
+ * normalisation terms [facets][cube][corr][W*W] through params->normalization_terms
+ * (wrapper.cu:82-232).  No device reset, no device selection: the current device is used. */
+void initLibrary(gridding_parameters *params);
+/* Free all device state (wrapper.cu:233-274; no cudaDeviceReset). */
+void releaseLibrary(void);
+/* Uniform weighting of the host grids by the sampling function (wrapper.cu:275-291). */
+void weight_uniformly(gridding_parameters *params);
+/* Divide each host grid slice by its normalisation sum (wrapper.cu:315-339). */
+void normalize(gridding_parameters *params);
+/* Baseline-major stable repacking of the caller's row arrays, filling
+ * baseline_starting_indexes[baseline_count + 1] (wrapper.cu:367-454).  Host-only. */
+void repack_input_data(gridding_parameters *params);
+/* Inverse FFT of the first cube slices of every facet with the reference's shifts, float32
+ * real parts packed at float index (cube * corr * nx * ny) * facet
+ * (wrapper.cu:340-352, fft_and_repacking_routines.cpp:83-118). */
+void finalize(gridding_parameters *params);
+/* Same for the sampling-function grids (wrapper.cu:353-362, fft_and_repacking_routines.cpp:120-161). */
+void finalize_psf(gridding_parameters *params);
+/* Grid one correlation (polarization_index), no faceting (wrapper.cu:456-545). */
+void grid_single_pol(gridding_parameters *params);
+/* One correlation, faceted: phase rotation + planar uv transform per facet (wrapper.cu:546-639). */
+void facet_single_pol(gridding_parameters *params);
+/* Two correlations (polarization_index, second_polarization_index) (wrapper.cu:640-735). */
+void grid_duel_pol(gridding_parameters *params);
+/* Two correlations, faceted (wrapper.cu:736-831). */
+void facet_duel_pol(gridding_parameters *params);
+/* Four correlations, no faceting (wrapper.cu:832-909). */
+void grid_4_cor(gridding_parameters *params);
+/* Four correlations, faceted (wrapper.cu:910-987). */
+void facet_4_cor(gridding_parameters *params);
+/* Four correlations, faceted, with J_p^-1 V J_q^-H Jones correction (wrapper.cu:988-1150; the
+ * correction follows the CPU library, correlation_gridding_policies.h:503-542). */
+void facet_4_cor_corrections(gridding_parameters *params);
+/* Sampling function (V = 1, unit weight, row flags only), no faceting (wrapper.cu:1151-1217). */
+void grid_sampling_function(gridding_parameters *params);
+/* Sampling function, faceted (wrapper.cu:1218-1284). */
+void facet_sampling_function(gridding_parameters *params);
+
+/* ---- extensions (no counterpart in the reference) ---- */
+
+/* First recorded error: returns its code (0 = none) and copies the message into buf. */
+int bullseye_last_error(char *buf, size_t n);
+/* Clear the sticky error so the library accepts calls again. */
+void bullseye_clear_error(void);
+/* 32 or 64: the data precision of the loaded library. */
+int bullseye_precision_bits(void);
+/* 32-bit library: compensated (hi/lo TwoSum) grid accumulation on (1, default) or off (0). */
+void bullseye_set_compensated(int on);
+/* When on, the row arrays, jones_terms and baseline_starting_indexes in gridding_parameters are
+ * device pointers in baseline-major order and gridding calls copy nothing from the host. */
+void bullseye_set_device_inputs(int on);
+/* Gridding correction for finalize: image[y][x] /= corr_x[x] * corr_y[y]; nulls switch it off. */
+void bullseye_set_gridding_correction(const double *corr_x, size_t nx, const double *corr_y, size_t ny);
+/* The library's CUDA stream (cudaStream_t), valid between initLibrary and releaseLibrary. */
+void *bullseye_get_stream(void);
+/* Kernels launched by the library since initLibrary or the last counter reset. */
+long long bullseye_kernel_launches(void);
+/* Accumulated gridder kernel time in ms for kind 0 (visibilities) or 1 (sampling function). */
+double bullseye_gridder_kernel_ms(int kind, long long *count);
+/* Reset the launch and kernel-time counters. */
+void bullseye_reset_counters(void);
+/* Zero the device-resident grids and normalisation sums. */
+void bullseye_zero_grids(void);
+/* Measured FP32 FMA throughput of the current GPU in TFLOP/s (roofline denominator). */
+double bullseye_fp32_fma_tflops(int iters);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,85 @@
+"""CPU tests of the C-ABI boundary: struct layout, exported symbols, host-only entry points."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from bullseye_gb300.abi import EXPECTED_OFFSETS, EXPECTED_SIZEOF, REFERENCE_EXPORTS, gridding_parameters_type
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.mark.parametrize("precision", ["single", "double"])
+def test_struct_layout_matches_reference(precision):
+    cls = gridding_parameters_type(precision)
+    assert ctypes.sizeof(cls) == EXPECTED_SIZEOF[precision]
+    for field, off in EXPECTED_OFFSETS[precision].items():
+        assert getattr(cls, field).offset == off, field
+
+
+def declared_symbols():
+    text = open(os.path.join(REPO, "include", "bullseye_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\([^;{]*\)\s*;", text)))
+
+
+def test_header_declares_every_reference_export():
+    syms = declared_symbols()
+    for name in REFERENCE_EXPORTS:
+        assert name in syms, name
+
+
+@pytest.mark.parametrize("precision", ["single", "double"])
+def test_library_loads_and_exports_header_symbols(precision, built_libraries):
+    from bullseye_gb300.build import library_path
+    lib = ctypes.CDLL(library_path(precision))
+    for name in declared_symbols():
+        assert hasattr(lib, name), name
+    lib.bullseye_precision_bits.restype = ctypes.c_int
+    assert lib.bullseye_precision_bits() == (32 if precision == "single" else 64)
+
+
+def test_repack_input_data_is_a_stable_baseline_sort(built_libraries):
+    """repack_input_data (host-only) against a numpy stable sort by baseline slot."""
+    from bullseye_gb300 import synth
+    from bullseye_gb300.imaging import baseline_index
+    from bullseye_gb300.library import load_library
+    lib = load_library("GPU", "double")
+    p = synth.small_problem("double", n_ant=6, n_times=7, n_chan=3)
+    rng = np.random.default_rng(0)
+    perm = rng.permutation(p.rows)  # scramble the rows first
+    arrays = dict(vis=p.vis[perm].copy(), uvw=p.uvw[perm].copy(), wt=p.weights[perm].copy(),
+                  fl=p.flags[perm].copy(), fr=p.flagged_rows[perm].copy(), spw=p.spw_ids[perm].copy(),
+                  a1=p.antenna1[perm].copy(), a2=p.antenna2[perm].copy(), field=p.field_ids[perm].copy(),
+                  t=p.timestamp_ids[perm].copy())
+    starts = np.zeros(p.baseline_count + 1, np.uintp)
+    st = gridding_parameters_type("double")()
+    P = ctypes.c_void_p
+    st.visibilities = arrays["vis"].ctypes.data_as(P)
+    st.uvw_coords = arrays["uvw"].ctypes.data_as(P)
+    st.visibility_weights = arrays["wt"].ctypes.data_as(P)
+    st.flags = arrays["fl"].ctypes.data_as(P)
+    st.flagged_rows = arrays["fr"].ctypes.data_as(P)
+    st.spw_index_array = arrays["spw"].ctypes.data_as(P)
+    st.antenna_1_ids = arrays["a1"].ctypes.data_as(P)
+    st.antenna_2_ids = arrays["a2"].ctypes.data_as(P)
+    st.field_array = arrays["field"].ctypes.data_as(P)
+    st.timestamp_ids = arrays["t"].ctypes.data_as(P)
+    st.should_invert_jones_terms = True
+    st.baseline_starting_indexes = starts.ctypes.data_as(P)
+    st.row_count = p.rows
+    st.baseline_count = p.baseline_count
+    st.antenna_count = p.n_antennas
+    st.channel_count = p.channels
+    st.number_of_polarization_terms = p.n_pol
+    lib.repack_input_data(ctypes.byref(st))
+    b = baseline_index(p.antenna1[perm], p.antenna2[perm], p.n_antennas)
+    order = np.argsort(b, kind="stable")
+    np.testing.assert_array_equal(arrays["vis"], p.vis[perm][order])
+    np.testing.assert_array_equal(arrays["uvw"], p.uvw[perm][order])
+    np.testing.assert_array_equal(arrays["fl"], p.flags[perm][order])
+    np.testing.assert_array_equal(arrays["t"], p.timestamp_ids[perm][order])
+    counts = np.bincount(b, minlength=p.baseline_count)
+    np.testing.assert_array_equal(starts, np.concatenate([[0], np.cumsum(counts)]))
