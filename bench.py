@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-comp", action="store_true", help="plain (uncompensated) FP32 grid flushes")
     return ap.parse_args()
 
 
@@ -356,6 +357,7 @@ def main():
     st = gridding_parameters_type("single")()
     tab.fill(st, geo, R)
     lib.bullseye_set_device_inputs(1)
+    lib.bullseye_set_compensated(0 if args.no_comp else 1)
     lib.initLibrary(ctypes.byref(st))
     check(lib)
     set_rows(st, d, lambda t: ctypes.c_void_p(t.data_ptr()))

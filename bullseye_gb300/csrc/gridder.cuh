@@ -117,13 +117,14 @@ struct TapT<true> {
   typedef cplx type;
 };
 
+// One staged visibility, prepared by the prologue (16-byte aligned header for vector loads).
 template <int NC>
-struct VisRec {
-  cplx vis[NC];
-  acc_real cw[NC];
-  int u0, v0, ru, rv;
-  int g, valid;
-  int fu, fv, plane;
+struct __align__(16) VisRec {
+  int u0, v0, ru, rv;      // footprint corner and its residues mod W
+  int g, valid, fu, fv;    // grid group, validity, tap offsets
+  int plane, pad0, pad1, pad2;
+  cplx vis[NC];            // weighted, corrected, rotated visibility
+  acc_real cw[NC];         // weight x flag per correlation (normalisation)
 };
 
 __device__ __forceinline__ void load_tap(const void *conv, long long idx, acc_real &t) {
@@ -177,32 +178,43 @@ __device__ __forceinline__ cplx phase_factor(double x) {
   return r;
 }
 
-// Flush one owned cell's register accumulator into the grid.
+// Flush one owned cell's register accumulator into the grid.  Compensated mode adds with
+// atomics that return the previous value, then recovers each addition's rounding error exactly
+// (TwoSum: s = a + b, e = (a - (s - (s - a))) + (b - (s - a))) and adds it to the lo grid; the
+// final grid is hi + lo.  The NC atomics of a cell are issued before any result is consumed.
 template <int NC, bool COMP>
 __device__ __forceinline__ void flush_cell(const GridArgs &a, long long slice0, long long nxy, int x, int y,
                                            cplx (&acc)[NC]) {
-  long long cell = (long long)y * a.nx + x;
+  const long long cell = (long long)y * a.nx + x;
+#if defined(BULLSEYE_SINGLE)
+  if (COMP) {
+    float2 old[NC];
+#pragma unroll
+    for (int k = 0; k < NC; ++k)
+      old[k] = atomicAdd(reinterpret_cast<float2 *>(a.grid + (slice0 + k) * nxy + cell), make_float2(acc[k].re, acc[k].im));
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+      float s0 = old[k].x + acc[k].re, b0 = s0 - old[k].x;
+      float e0 = (old[k].x - (s0 - b0)) + (acc[k].re - b0);
+      float s1 = old[k].y + acc[k].im, b1 = s1 - old[k].y;
+      float e1 = (old[k].y - (s1 - b1)) + (acc[k].im - b1);
+      if (e0 != 0.0f || e1 != 0.0f)
+        atomicAdd(reinterpret_cast<float2 *>(a.grid_lo + (slice0 + k) * nxy + cell), make_float2(e0, e1));
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < NC; ++k)
+      atomicAdd(reinterpret_cast<float2 *>(a.grid + (slice0 + k) * nxy + cell), make_float2(acc[k].re, acc[k].im));
+  }
+#else
 #pragma unroll
   for (int k = 0; k < NC; ++k) {
-    long long idx = (slice0 + k) * nxy + cell;
-#if defined(BULLSEYE_SINGLE)
-    float2 *dst = reinterpret_cast<float2 *>(a.grid + idx);
-    float2 val = make_float2(acc[k].re, acc[k].im);
-    if (COMP) {
-      float2 old = atomicAdd(dst, val);
-      float s0 = old.x + val.x, b0 = s0 - old.x;
-      float e0 = (old.x - (s0 - b0)) + (val.x - b0);
-      float s1 = old.y + val.y, b1 = s1 - old.y;
-      float e1 = (old.y - (s1 - b1)) + (val.y - b1);
-      if (e0 != 0.0f || e1 != 0.0f)
-        atomicAdd(reinterpret_cast<float2 *>(a.grid_lo + idx), make_float2(e0, e1));
-    } else {
-      atomicAdd(dst, val);
-    }
-#else
-    atomicAdd(&a.grid[idx].re, acc[k].re);
-    atomicAdd(&a.grid[idx].im, acc[k].im);
+    atomicAdd(&a.grid[(slice0 + k) * nxy + cell].re, acc[k].re);
+    atomicAdd(&a.grid[(slice0 + k) * nxy + cell].im, acc[k].im);
+  }
 #endif
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
     acc[k].re = 0;
     acc[k].im = 0;
   }
@@ -341,17 +353,58 @@ __device__ __forceinline__ void prologue(const GridArgs &a, int f_local, int cha
 template <int NC, bool WPROJ>
 __host__ __device__ inline size_t grid_smem_bytes(int V, int W) {
   size_t recs = sizeof(VisRec<NC>) * (size_t)V;
+  size_t norm = (sizeof(double) * NC + 2 * sizeof(int)) * (size_t)V;  // per-lane normalisation state
   size_t taps = sizeof(typename TapT<WPROJ>::type) * (size_t)V * W * 2;
-  return recs + taps + 64;
+  return recs + norm + taps + 64;
 }
 
-template <int NC, bool WPROJ, int J, bool COMP>
+// premultiplied visibility times the column tap
+__device__ __forceinline__ cplx premul(cplx v, acc_real t) {
+  cplx r;
+  r.re = v.re * t;
+  r.im = v.im * t;
+  return r;
+}
+__device__ __forceinline__ cplx premul(cplx v, cplx t) { return cmul(v, t); }
+__device__ __forceinline__ void mac(cplx &acc, cplx a, acc_real t) {
+  acc.re = fma(a.re, t, acc.re);
+  acc.im = fma(a.im, t, acc.im);
+}
+__device__ __forceinline__ void mac(cplx &acc, cplx a, cplx t) {
+  acc.re = fma(a.re, t.re, acc.re);
+  acc.re = fma(-a.im, t.im, acc.re);
+  acc.im = fma(a.re, t.im, acc.im);
+  acc.im = fma(a.im, t.re, acc.im);
+}
+
+// Thread -> owned (column, strip) map.  WIDE pads the columns to a multiple of 32 so that every
+// warp covers one strip: the row taps it reads are then warp-uniform (shared-memory broadcast).
+template <bool WIDE>
+__device__ __forceinline__ void owner_map(int tid, int W, int J, int &du, int &strip, bool &owner) {
+  const int nstrips = (W + J - 1) / J;
+  if (WIDE) {
+    const int wpr = (W + 31) >> 5;  // warps per strip
+    const int warp = tid >> 5, lane = tid & 31;
+    du = (warp % wpr) * 32 + lane;
+    strip = warp / wpr;
+    owner = du < W && strip < nstrips;
+  } else {
+    du = tid % W;
+    strip = tid / W;
+    owner = strip < nstrips;
+  }
+}
+
+template <int NC, bool WPROJ, int J, bool COMP, bool WIDE>
 __global__ void __launch_bounds__(512, 1) romein_grid_kernel(const GridArgs a) {
   typedef typename TapT<WPROJ>::type tap_t;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   VisRec<NC> *recs = reinterpret_cast<VisRec<NC> *>(smem_raw);
-  tap_t *tu = reinterpret_cast<tap_t *>(smem_raw + sizeof(VisRec<NC>) * a.V);
-  tap_t *tv = tu + (size_t)a.V * a.W;
+  double *s_nacc = reinterpret_cast<double *>(smem_raw + sizeof(VisRec<NC>) * a.V);  // [V][NC]
+  int *s_ng = reinterpret_cast<int *>(s_nacc + (size_t)a.V * NC);                    // [V]
+  int *s_mixed = s_ng + a.V;                                                          // [V]
+  tap_t *tu = reinterpret_cast<tap_t *>(smem_raw + ((sizeof(VisRec<NC>) + sizeof(double) * NC + 2 * sizeof(int)) * a.V + 15) / 16 * 16);
+  tap_t *tv = tu + a.V * a.W;
   __shared__ int s_same_g;
   __shared__ double s_norm[NC];
 
@@ -374,29 +427,35 @@ __global__ void __launch_bounds__(512, 1) romein_grid_kernel(const GridArgs a) {
   if (r0 >= r1) return;
 
   const int tid = threadIdx.x;
-  const int nstrips = (W + J - 1) / J;
-  const bool owner = tid < W * nstrips;
-  const int du = tid % W;
-  const int strip = tid / W;
+  int du, strip;
+  bool owner;
+  owner_map<WIDE>(tid, W, J, du, strip, owner);
+  unsigned rows_mask = 0;
+#pragma unroll
+  for (int j = 0; j < J; ++j)
+    if (strip * J + j < W) rows_mask |= 1u << j;
+  if (!owner) rows_mask = 0;
+  const long long fslice = (long long)(a.facet_base + f_local) * a.groups;
+  const bool want_norm = a.norm != nullptr;
+  if (want_norm && tid < a.V) {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) s_nacc[tid * NC + k] = 0.0;
+    s_ng[tid] = -1;
+    s_mixed[tid] = 0;
+  }
 
+  // Register state: accumulators of the J owned cells and the footprint they belong to.  The
+  // owned cells are (pu0 + ou, pv0 + ovj[j]) for the last footprint corner (pu0, pv0).
   cplx acc[J][NC];
-  int cy[J];
+  int ovj[J];
 #pragma unroll
   for (int j = 0; j < J; ++j) {
-    cy[j] = -1;
+    ovj[j] = 0;
 #pragma unroll
     for (int k = 0; k < NC; ++k) { acc[j][k].re = 0; acc[j][k].im = 0; }
   }
   unsigned dirty = 0;
-  int cx = -1, cg = -1;
-
-  // normalisation accumulators of this thread's staged visibilities
-  double nacc[NC];
-#pragma unroll
-  for (int k = 0; k < NC; ++k) nacc[k] = 0;
-  int ng = -1;
-  bool ng_mixed = false;
-  const bool want_norm = a.norm != nullptr;
+  int cg = -1, pu0 = -1, pv0 = -1, ou = 0;
 
   for (long long base = r0; base < r1; base += a.V) {
     const int nv = (int)min((long long)a.V, r1 - base);
@@ -409,134 +468,147 @@ __global__ void __launch_bounds__(512, 1) romein_grid_kernel(const GridArgs a) {
     // gather the 2W taps of every staged visibility
     const int per = 2 * W;
     for (int idx = tid; idx < nv * per; idx += blockDim.x) {
-      int vi = idx / per, j = idx - vi * per;
+      const int vi = idx / per, j = idx - vi * per;
       const VisRec<NC> &r = recs[vi];
       if (!r.valid) continue;
-      bool isv = j >= W;
-      int jj = isv ? j - W : j;
-      long long ti = (long long)r.plane * a.K + (isv ? r.fv : r.fu) + (long long)jj * a.os;
+      const bool isv = j >= W;
+      const int jj = isv ? j - W : j;
+      const long long ti = (long long)r.plane * a.K + (isv ? r.fv : r.fu) + (long long)jj * a.os;
       tap_t t;
       load_tap(a.conv, ti, t);
-      (isv ? tv : tu)[(size_t)vi * W + jj] = t;
+      (isv ? tv : tu)[vi * W + jj] = t;
     }
     __syncthreads();
-    // normalisation: Re(sum_u k_u * sum_v k_v) * weight x flag, per staged visibility
-    if (want_norm && tid < nv && recs[tid].valid) {
-      const VisRec<NC> &r = recs[tid];
-      double nt;
-      if (WPROJ) {
+    // normalisation, four lanes per staged visibility: Re(sum_u k_u * sum_v k_v) x weight x flag
+    // (loop bounds are warp-uniform so the shuffles always see full warps); lane 4i owns the
+    // running sums of staged slot i in shared memory
+    if (want_norm) {
+      for (int b4 = tid & ~31; b4 < 4 * nv; b4 += blockDim.x) {
+        const int q = b4 + (tid & 31);
+        const int vi = q >> 2, part = q & 3;
+        const bool act = vi < nv;
         double sur = 0, sui = 0, svr = 0, svi = 0;
-        const cplx *pu = reinterpret_cast<const cplx *>(tu) + (size_t)tid * W;
-        const cplx *pv = reinterpret_cast<const cplx *>(tv) + (size_t)tid * W;
-        for (int j = 0; j < W; ++j) { sur += pu[j].re; sui += pu[j].im; svr += pv[j].re; svi += pv[j].im; }
-        nt = sur * svr - sui * svi;
-      } else {
-        double su = 0, sv = 0;
-        const acc_real *pu = reinterpret_cast<const acc_real *>(tu) + (size_t)tid * W;
-        const acc_real *pv = reinterpret_cast<const acc_real *>(tv) + (size_t)tid * W;
-        for (int j = 0; j < W; ++j) { su += pu[j]; sv += pv[j]; }
-        nt = su * sv;
-      }
-      if (ng != r.g) {
-        if (ng >= 0) {
-          ng_mixed = true;
-#pragma unroll
-          for (int k = 0; k < NC; ++k)
-            if (nacc[k] != 0.0) atomicAdd(&a.norm[((long long)(a.facet_base + f_local) * a.groups + ng) * NC + k], nacc[k]);
+        if (act) {
+          if (WPROJ) {
+            const cplx *pu = reinterpret_cast<const cplx *>(tu) + vi * W;
+            const cplx *pv = reinterpret_cast<const cplx *>(tv) + vi * W;
+            for (int j = part; j < W; j += 4) { sur += pu[j].re; sui += pu[j].im; svr += pv[j].re; svi += pv[j].im; }
+          } else {
+            const acc_real *pu = reinterpret_cast<const acc_real *>(tu) + vi * W;
+            const acc_real *pv = reinterpret_cast<const acc_real *>(tv) + vi * W;
+            for (int j = part; j < W; j += 4) { sur += pu[j]; svr += pv[j]; }
+          }
         }
 #pragma unroll
-        for (int k = 0; k < NC; ++k) nacc[k] = 0;
-        ng = r.g;
-      }
+        for (int off = 1; off < 4; off <<= 1) {
+          sur += __shfl_xor_sync(0xffffffffu, sur, off);
+          sui += __shfl_xor_sync(0xffffffffu, sui, off);
+          svr += __shfl_xor_sync(0xffffffffu, svr, off);
+          svi += __shfl_xor_sync(0xffffffffu, svi, off);
+        }
+        if (act && part == 0 && recs[vi].valid) {
+          const VisRec<NC> &r = recs[vi];
+          const double nt = sur * svr - sui * svi;
+          double *na = s_nacc + vi * NC;
+          if (s_ng[vi] != r.g) {
+            if (s_ng[vi] >= 0) {
+              s_mixed[vi] = 1;
 #pragma unroll
-      for (int k = 0; k < NC; ++k) nacc[k] += (double)r.cw[k] * nt;
+              for (int k = 0; k < NC; ++k)
+                if (na[k] != 0.0) atomicAdd(&a.norm[(fslice + s_ng[vi]) * NC + k], na[k]);
+            }
+#pragma unroll
+            for (int k = 0; k < NC; ++k) na[k] = 0;
+            s_ng[vi] = r.g;
+          }
+#pragma unroll
+          for (int k = 0; k < NC; ++k) na[k] += (double)r.cw[k] * nt;
+        }
+      }
     }
     // grid the staged chunk
-    if (owner) {
+    if (rows_mask) {
       for (int vi = 0; vi < nv; ++vi) {
-        const VisRec<NC> &r = recs[vi];
-        if (!r.valid) continue;
-        int ou = du - r.ru;
-        ou += (ou < 0) ? W : 0;
-        const int x = r.u0 + ou;
-        if (x != cx || r.g != cg) {
-          if (dirty) {
-            long long slice0 = ((long long)(a.facet_base + f_local) * a.groups + cg) * NC;
+        const int4 h0 = *reinterpret_cast<const int4 *>(&recs[vi].u0);
+        const int4 h1 = *reinterpret_cast<const int4 *>(&recs[vi].g);
+        if (!h1.y) continue;
+        if (h0.x != pu0 || h0.y != pv0 || h1.x != cg) {
+          // footprint moved: recompute the owned cells, flush those that changed
+          int o = du - h0.z;
+          o += (o < 0) ? W : 0;
+          if (h0.x + o != pu0 + ou || h1.x != cg) {
+            if (dirty) {
 #pragma unroll
-            for (int j = 0; j < J; ++j)
-              if (dirty & (1u << j)) flush_cell<NC, COMP>(a, slice0, nxy, cx, cy[j], acc[j]);
-            dirty = 0;
+              for (int j = 0; j < J; ++j)
+                if (dirty & (1u << j)) flush_cell<NC, COMP>(a, (fslice + cg) * NC, nxy, pu0 + ou, pv0 + ovj[j], acc[j]);
+              dirty = 0;
+            }
+            cg = h1.x;
           }
-          cx = x;
-          cg = r.g;
 #pragma unroll
-          for (int j = 0; j < J; ++j) cy[j] = -1;
+          for (int j = 0; j < J; ++j) {
+            int ov = strip * J + j - h0.w;
+            ov += (ov < 0) ? W : 0;
+            if ((dirty & (1u << j)) && h0.y + ov != pv0 + ovj[j]) {
+              flush_cell<NC, COMP>(a, (fslice + cg) * NC, nxy, pu0 + ou, pv0 + ovj[j], acc[j]);
+              dirty &= ~(1u << j);
+            }
+            ovj[j] = ov;
+          }
+          ou = o;
+          pu0 = h0.x;
+          pv0 = h0.y;
         }
-        const tap_t tuv = tu[(size_t)vi * W + ou];
-        cplx vv[NC];
+        const tap_t tuv = tu[vi * W + ou];
+        cplx pre[NC];
 #pragma unroll
-        for (int k = 0; k < NC; ++k) vv[k] = r.vis[k];
+        for (int k = 0; k < NC; ++k) pre[k] = premul(recs[vi].vis[k], tuv);
+        const tap_t *tvrow = tv + vi * W;
 #pragma unroll
         for (int j = 0; j < J; ++j) {
-          const int dvj = strip * J + j;
-          if (dvj < W) {
-            int ov = dvj - r.rv;
-            ov += (ov < 0) ? W : 0;
-            const int y = r.v0 + ov;
-            if (y != cy[j]) {
-              if (dirty & (1u << j)) {
-                long long slice0 = ((long long)(a.facet_base + f_local) * a.groups + cg) * NC;
-                flush_cell<NC, COMP>(a, slice0, nxy, cx, cy[j], acc[j]);
-                dirty &= ~(1u << j);
-              }
-              cy[j] = y;
-            }
-            const tap_t tvv = tv[(size_t)vi * W + ov];
+          if (rows_mask & (1u << j)) {
+            const tap_t t = tvrow[ovj[j]];
 #pragma unroll
-            for (int k = 0; k < NC; ++k) {
-              cplx m = tap_mul(tuv, tvv, vv[k]);
-              acc[j][k].re += m.re;
-              acc[j][k].im += m.im;
-            }
-            dirty |= (1u << j);
+            for (int k = 0; k < NC; ++k) mac(acc[j][k], pre[k], t);
           }
         }
+        dirty = rows_mask;
       }
     }
     __syncthreads();
   }
   // final flush of owned cells
-  if (owner && dirty) {
-    long long slice0 = ((long long)(a.facet_base + f_local) * a.groups + cg) * NC;
+  if (dirty) {
 #pragma unroll
     for (int j = 0; j < J; ++j)
-      if (dirty & (1u << j)) flush_cell<NC, COMP>(a, slice0, nxy, cx, cy[j], acc[j]);
+      if (dirty & (1u << j)) flush_cell<NC, COMP>(a, (fslice + cg) * NC, nxy, pu0 + ou, pv0 + ovj[j], acc[j]);
   }
-  // normalisation: one reduction per CTA when every staged visibility shared a grid group
+  // normalisation: one reduction per CTA when every staged slot saw a single grid group
   if (want_norm) {
     if (tid == 0) s_same_g = -1;
     if (tid < NC) s_norm[tid] = 0.0;
     __syncthreads();
-    if (ng >= 0) atomicMax(&s_same_g, ng);
+    const int my_g = tid < a.V ? s_ng[tid] : -1;
+    if (my_g >= 0) atomicMax(&s_same_g, my_g);
     __syncthreads();
     const int gmax = s_same_g;
-    __syncthreads();
-    bool uniform_here = !ng_mixed && (ng < 0 || ng == gmax);
-    int all_uniform = __syncthreads_and(uniform_here ? 1 : 0);
-    if (all_uniform) {
-      if (ng >= 0) {
+    const bool uniform_here = tid >= a.V || (!s_mixed[tid] && (my_g < 0 || my_g == gmax));
+    const int all_uniform = __syncthreads_and(uniform_here ? 1 : 0);
+    if (tid < a.V && my_g >= 0) {
+      const double *na = s_nacc + tid * NC;
+      if (all_uniform) {
 #pragma unroll
         for (int k = 0; k < NC; ++k)
-          if (nacc[k] != 0.0) atomicAdd(&s_norm[k], nacc[k]);
-      }
-      __syncthreads();
-      if (tid < NC && gmax >= 0 && s_norm[tid] != 0.0)
-        atomicAdd(&a.norm[((long long)(a.facet_base + f_local) * a.groups + gmax) * NC + tid], s_norm[tid]);
-    } else if (ng >= 0) {
+          if (na[k] != 0.0) atomicAdd(&s_norm[k], na[k]);
+      } else {
 #pragma unroll
-      for (int k = 0; k < NC; ++k)
-        if (nacc[k] != 0.0) atomicAdd(&a.norm[((long long)(a.facet_base + f_local) * a.groups + ng) * NC + k], nacc[k]);
+        for (int k = 0; k < NC; ++k)
+          if (na[k] != 0.0) atomicAdd(&a.norm[(fslice + my_g) * NC + k], na[k]);
+      }
     }
+    __syncthreads();
+    if (all_uniform && tid < NC && gmax >= 0 && s_norm[tid] != 0.0)
+      atomicAdd(&a.norm[(fslice + gmax) * NC + tid], s_norm[tid]);
   }
 }
 

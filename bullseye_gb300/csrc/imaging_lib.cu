@@ -133,7 +133,11 @@ struct Context {
   DevBuf<vis_complex> jones_raw, jones_inv;
   DevBuf<FacetXform> facets;
   // grids
-  DevBuf<vis_complex> grid, grid_lo, sf, sf_lo, scratch;
+  // sf holds the caller's initial sampling grids [facets][sf][ny][nx]; every facet receives the
+  // same sampling-function contribution (the phase policy of the sampling function reports the
+  // phase centre as facet centre, phase_transform_policies.h:77-82, so the uv transform is the
+  // identity), which is gridded once into sf_acc/sf_lo [sf][ny][nx] and added to every facet.
+  DevBuf<vis_complex> grid, grid_lo, sf, sf_acc, sf_lo, scratch;
   DevBuf<double> norm;
   DevBuf<int> dev_error;
   std::vector<double> host_norm;  // published through params.normalization_terms
@@ -254,7 +258,8 @@ extern "C" void bullseye_zero_grids() {
   BZ_CUDA_TRY(cudaMemsetAsync(c.grid.ptr, 0, sizeof(vis_complex) * c.F * c.cube * c.C * nxy, c.stream));
   if (c.grid_lo.ptr) BZ_CUDA_TRY(cudaMemsetAsync(c.grid_lo.ptr, 0, sizeof(vis_complex) * c.F * c.cube * c.C * nxy, c.stream));
   if (c.sf.ptr) BZ_CUDA_TRY(cudaMemsetAsync(c.sf.ptr, 0, sizeof(vis_complex) * c.F * c.sf_count * nxy, c.stream));
-  if (c.sf_lo.ptr) BZ_CUDA_TRY(cudaMemsetAsync(c.sf_lo.ptr, 0, sizeof(vis_complex) * c.F * c.sf_count * nxy, c.stream));
+  if (c.sf_acc.ptr) BZ_CUDA_TRY(cudaMemsetAsync(c.sf_acc.ptr, 0, sizeof(vis_complex) * c.sf_count * nxy, c.stream));
+  if (c.sf_lo.ptr) BZ_CUDA_TRY(cudaMemsetAsync(c.sf_lo.ptr, 0, sizeof(vis_complex) * c.sf_count * nxy, c.stream));
   BZ_CUDA_TRY(cudaMemsetAsync(c.norm.ptr, 0, sizeof(double) * c.F * c.cube * c.C, c.stream));
 }
 
@@ -385,9 +390,12 @@ extern "C" void initLibrary(gridding_parameters *pp) {
       BZ_CUDA_TRY(cudaMemcpy(c.sf.ptr, p.sampling_function_buffer, sizeof(vis_complex) * ns, cudaMemcpyHostToDevice));
     else
       BZ_CUDA_TRY(cudaMemset(c.sf.ptr, 0, sizeof(vis_complex) * ns));
+    const size_t na = c.sf_count * nxy;
+    if (!c.sf_acc.alloc(na)) return;
+    BZ_CUDA_TRY(cudaMemset(c.sf_acc.ptr, 0, sizeof(vis_complex) * na));
 #if defined(BULLSEYE_SINGLE)
-    if (!c.sf_lo.alloc(ns)) return;
-    BZ_CUDA_TRY(cudaMemset(c.sf_lo.ptr, 0, sizeof(vis_complex) * ns));
+    if (!c.sf_lo.alloc(na)) return;
+    BZ_CUDA_TRY(cudaMemset(c.sf_lo.ptr, 0, sizeof(vis_complex) * na));
 #endif
   }
   // library-owned normalisation terms in the GPU library's layout
@@ -406,7 +414,7 @@ extern "C" void releaseLibrary() {
   c.cgi.release(); c.sf_cgi.release(); c.vis.release(); c.weights.release(); c.uvw.release();
   c.flags.release(); c.flagged_rows.release(); c.field.release(); c.spw.release(); c.ant1.release();
   c.ant2.release(); c.time_ids.release(); c.starts.release(); c.jones_raw.release(); c.jones_inv.release();
-  c.facets.release(); c.grid.release(); c.grid_lo.release(); c.sf.release(); c.sf_lo.release();
+  c.facets.release(); c.grid.release(); c.grid_lo.release(); c.sf.release(); c.sf_acc.release(); c.sf_lo.release();
   c.scratch.release(); c.norm.release(); c.dev_error.release(); c.corr_x.release(); c.corr_y.release();
   if (c.ev_g0) cudaEventDestroy(c.ev_g0);
   if (c.ev_g1) cudaEventDestroy(c.ev_g1);
@@ -495,41 +503,59 @@ static FacetXform facet_xform(double ra0, double dec0, double ra, double dec, bo
 
 struct LaunchShape {
   int J, NT, V;
+  bool wide;
   size_t smem;
 };
 
+// Ownership layout for full support W: J rows per thread; WIDE pads columns to a multiple of 32
+// (chosen when that wastes at most 1/8 of the columns) so each warp holds one strip.
 template <int NC, bool WPROJ>
 static LaunchShape choose_shape(int W) {
   LaunchShape s;
-  const int Js[] = {1, 2, 4, 8, 16};
   s.J = 0;
-  for (int j : Js) {
-    if (W * ((W + j - 1) / j) <= 512) {
-      s.J = j;
-      break;
+  s.wide = false;
+  const int cols = ((W + 31) / 32) * 32;
+  if ((cols - W) * 8 <= W) {
+    for (int j : {2, 8}) {
+      if (cols * ((W + j - 1) / j) <= 512) {
+        s.J = j;
+        s.wide = true;
+        break;
+      }
     }
   }
   if (!s.J) {
-    s.J = 16;
+    for (int j : {1, 2, 4, 8, 16}) {
+      if (W * ((W + j - 1) / j) <= 512) {
+        s.J = j;
+        break;
+      }
+    }
   }
-  int owners = W * ((W + s.J - 1) / s.J);
+  if (!s.J) s.J = 16;
+  const int owners = s.wide ? cols * ((W + s.J - 1) / s.J) : W * ((W + s.J - 1) / s.J);
   s.NT = std::max(32, ((owners + 31) / 32) * 32);
-  const size_t budget = 96 * 1024;
-  size_t per = sizeof(VisRec<NC>) + sizeof(typename TapT<WPROJ>::type) * 2 * (size_t)W;
+  const size_t budget = 160 * 1024;
+  const size_t per = sizeof(VisRec<NC>) + sizeof(double) * NC + 2 * sizeof(int) +
+                     sizeof(typename TapT<WPROJ>::type) * 2 * (size_t)W;
   int V = (int)std::min<size_t>(s.NT, (budget - 64) / per);
-  if (V < 1) V = 1;
-  s.V = V;
-  s.smem = grid_smem_bytes<NC, WPROJ>(V, W);
+  s.V = std::max(1, V);
+  s.smem = grid_smem_bytes<NC, WPROJ>(s.V, W);
   return s;
 }
 
-template <int NC, bool WPROJ, int J>
+template <int NC, bool WPROJ, int J, bool WIDE>
 static bool launch_j(const GridArgs &a, const LaunchShape &s, long long blocks, cudaStream_t st, bool comp) {
   void (*kern)(const GridArgs);
+#if defined(BULLSEYE_SINGLE)
   if (comp)
-    kern = romein_grid_kernel<NC, WPROJ, J, true>;
+    kern = romein_grid_kernel<NC, WPROJ, J, true, WIDE>;
   else
-    kern = romein_grid_kernel<NC, WPROJ, J, false>;
+    kern = romein_grid_kernel<NC, WPROJ, J, false, WIDE>;
+#else
+  (void)comp;  // FP64 accumulation needs no compensation
+  kern = romein_grid_kernel<NC, WPROJ, J, false, WIDE>;
+#endif
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem) != cudaSuccess) {
     bz_record_error(BZ_ERR_CUDA, "cudaFuncSetAttribute failed");
     return false;
@@ -547,17 +573,21 @@ static bool launch_j(const GridArgs &a, const LaunchShape &s, long long blocks, 
 template <int NC, bool WPROJ>
 static bool launch_nc(GridArgs a, long long blocks, cudaStream_t st, bool comp) {
   LaunchShape s = choose_shape<NC, WPROJ>(a.W);
-  if (a.W * ((a.W + s.J - 1) / s.J) > 512) {
+  if (s.NT > 512) {
     bz_record_error(BZ_ERR_UNSUPPORTED, "full support %d is larger than this build supports", a.W);
     return false;
   }
   a.V = s.V;
+  if (s.wide) {
+    if (s.J == 2) return launch_j<NC, WPROJ, 2, true>(a, s, blocks, st, comp);
+    return launch_j<NC, WPROJ, 8, true>(a, s, blocks, st, comp);
+  }
   switch (s.J) {
-    case 1: return launch_j<NC, WPROJ, 1>(a, s, blocks, st, comp);
-    case 2: return launch_j<NC, WPROJ, 2>(a, s, blocks, st, comp);
-    case 4: return launch_j<NC, WPROJ, 4>(a, s, blocks, st, comp);
-    case 8: return launch_j<NC, WPROJ, 8>(a, s, blocks, st, comp);
-    default: return launch_j<NC, WPROJ, 16>(a, s, blocks, st, comp);
+    case 1: return launch_j<NC, WPROJ, 1, false>(a, s, blocks, st, comp);
+    case 2: return launch_j<NC, WPROJ, 2, false>(a, s, blocks, st, comp);
+    case 4: return launch_j<NC, WPROJ, 4, false>(a, s, blocks, st, comp);
+    case 8: return launch_j<NC, WPROJ, 8, false>(a, s, blocks, st, comp);
+    default: return launch_j<NC, WPROJ, 16, false>(a, s, blocks, st, comp);
   }
 }
 
@@ -663,7 +693,8 @@ static void copy_back_grids(gridding_parameters &p, bool sampling) {
     for (size_t i = 0; i < tmp.size(); ++i) c.host_norm[i * bins] = tmp[i];
   } else {
     const size_t n = c.F * c.sf_count * nxy;
-    resolve_compensated_kernel<<<1024, 256, 0, c.stream>>>(c.sf.ptr, c.sf_lo.ptr, c.scratch.ptr, (long long)n);
+    broadcast_add_kernel<<<1024, 256, 0, c.stream>>>(c.sf.ptr, c.sf_acc.ptr, c.sf_lo.ptr, c.scratch.ptr,
+                                                    (long long)(c.sf_count * nxy), (long long)c.F);
     c.launches++;
     if (p.sampling_function_buffer)
       BZ_CUDA_TRY(cudaMemcpyAsync(p.sampling_function_buffer, c.scratch.ptr, sizeof(vis_complex) * n,
@@ -750,7 +781,7 @@ static void grid_common(gridding_parameters *pp, int nc, int mode, bool faceting
   a.cgi = sampling ? c.sf_cgi.ptr : c.cgi.ptr;
   a.conv = c.conv.ptr;
   a.facets = c.facets.ptr;
-  a.grid = sampling ? c.sf.ptr : c.grid.ptr;
+  a.grid = sampling ? c.sf_acc.ptr : c.grid.ptr;
   a.grid_lo = nullptr;
 #if defined(BULLSEYE_SINGLE)
   if (c.compensated) a.grid_lo = sampling ? c.sf_lo.ptr : c.grid_lo.ptr;
@@ -774,7 +805,8 @@ static void grid_common(gridding_parameters *pp, int nc, int mode, bool faceting
   a.gcy = (double)(c.ny / 2 - p.conv_support);
   a.wmax = (double)(float)p.wmax_est;  // the reference divides by (float)wmax_est
   const int nc_launch = sampling ? 1 : nc;
-  const long long blocks = (long long)c.F * nslots * (long long)c.nchan;
+  // the sampling function is identical for every facet: grid it once (facet 0)
+  const long long blocks = (long long)(sampling ? 1 : c.F) * nslots * (long long)c.nchan;
   settle_kernel_timing();
   cudaEventRecord(c.ev_k0, c.stream);
   if (p.row_count > 0 && !launch_gridder(a, nc_launch, p.wplanes > 1, blocks, c.stream, a.grid_lo != nullptr)) return;

@@ -58,6 +58,26 @@ __global__ void resolve_compensated_kernel(const vis_complex *__restrict__ hi, c
   }
 }
 
+// out[f][i] = init[f][i] + hi[i] + lo[i] for f < nf, i < per: a facet-invariant accumulated
+// contribution added to every facet's initial grid.
+__global__ void broadcast_add_kernel(const vis_complex *__restrict__ init, const vis_complex *__restrict__ hi,
+                                     const vis_complex *__restrict__ lo, vis_complex *__restrict__ out, long long per,
+                                     long long nf) {
+  const long long total = per * nf;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const long long r = i % per;
+    vis_complex h = hi[r];
+    if (lo) {
+      h.re += lo[r].re;
+      h.im += lo[r].im;
+    }
+    vis_complex o = init[i];
+    o.re += h.re;
+    o.im += h.im;
+    out[i] = o;
+  }
+}
+
 // Gather with the inverse shift of numpy's ifftshift: dst[y][x] = src[(y+ny/2)%ny][(x+nx/2)%nx]
 // for each of `slices` planes.  Equivalent to bullseye/mo/cpu_gpu_common/fft_shift_utils.cpp:75-111.
 __global__ void ifftshift_gather_kernel(const vis_complex *__restrict__ src, vis_complex *__restrict__ dst, int nx,
