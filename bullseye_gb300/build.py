@@ -43,7 +43,7 @@ def _cmd(precision: str, out: str, verbose_ptxas: bool = False):
     macro = "-DBULLSEYE_SINGLE" if precision == "single" else "-DBULLSEYE_DOUBLE"
     cmd = [os.path.join(ch, "bin", "nvcc"), *ARCH, "-O3", "-lineinfo", "-std=c++17", macro,
            "-Xcompiler", "-fPIC", "-shared", "--expt-relaxed-constexpr",
-           os.path.join(CSRC, "imaging_lib.cu"), "-o", out,
+           os.path.join(CSRC, "imaging_lib.cu"), os.path.join(CSRC, "noalloc.cu"), "-o", out,
            "-L" + os.path.join(ch, "lib64"), "-lcufft",
            "-Xlinker", "-rpath," + os.path.join(ch, "lib64")]
     if verbose_ptxas:

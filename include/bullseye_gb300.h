@@ -99,6 +99,24 @@ void bullseye_zero_grids(void);
 /* Measured FP32 FMA throughput of the current GPU in TFLOP/s (roofline denominator). */
 double bullseye_fp32_fma_tflops(int iters);
 
+/* Allocation-free facet_4_cor_corrections, for callers that cannot allocate device memory while
+ * they grid (a fixed device arena with no further cudaMalloc/cudaFree, or code where a device
+ * allocation would synchronise or is not permitted).  No counterpart in the reference.
+ * Every pointer in *params is a DEVICE pointer: row arrays in baseline-major order (with
+ * baseline_starting_indexes, or null for fixed row segments), jones_terms (inverted IN PLACE, as
+ * the reference CPU library does), conv, reference_wavelengths, enabled_channels,
+ * channel_grid_indicies, facet_centres, output_buffer (grids, accumulated into) and
+ * normalization_terms (float64 [facets][cube][4], accumulated into); sizes and scalars are read
+ * from the struct.  Work is queued on `stream` (a cudaStream_t); nothing is allocated and the
+ * call does not synchronise.  Scratch is one fixed file-scope device array of the library
+ * (40 MiB + 64 KiB, held by every GPU that loads the library until exit): in the 32-bit library,
+ * grids beyond 5,242,880 complex cells (facets x cube x 4 x ny x nx) are rejected with
+ * BZ_ERR_UNSUPPORTED (5)
+ * and a message in bullseye_last_error().  Calls whose work overlaps on one GPU race on the shared
+ * scratch.  The first call on each device resolves the scratch address and should come before any
+ * stream capture on that device.  Returns 0 when queued. */
+int bullseye_facet_4_cor_corrections_noalloc(const gridding_parameters *params, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
