@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-comp", action="store_true", help="plain (uncompensated) FP32 grid flushes")
+    ap.add_argument("--chans", type=int, default=0, help="override the channel count (profiling cases)")
+    ap.add_argument("--facets", type=int, default=0, help="override the facet count (profiling cases)")
     return ap.parse_args()
 
 
@@ -314,6 +316,11 @@ def cpu_baseline(geo, conv1d, target_s):
 # ----------------------------------------------------------------------------- main
 def main():
     args = parse()
+    global N_CHAN, N_FACETS
+    if args.chans:
+        N_CHAN = args.chans
+    if args.facets:
+        N_FACETS = args.facets
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     n_times = max(8, int(N_TIMES * args.time_frac))

@@ -220,9 +220,73 @@ __device__ __forceinline__ void flush_cell(const GridArgs &a, long long slice0, 
   }
 }
 
+// Compensated flushes go through a per-warp queue in shared memory: a lane that must flush a
+// cell appends (cell, values) and carries on; when a queue holds kDrainAt records the warp drains
+// it with one record per lane, so the atomics' round trips overlap instead of serialising in the
+// lane that owns the cells.
+constexpr int kFlushQueueCap = 64;
+constexpr int kDrainAt = 32;
+
+template <int NC>
+struct FlushRec {
+  long long cell;        // slice0 * nxy + y * nx + x of correlation 0
+  float2 v[NC];
+};
+
+template <int NC>
+__device__ __forceinline__ void compensated_add(const GridArgs &a, long long idx, float2 val, float2 old) {
+  float s0 = old.x + val.x, b0 = s0 - old.x;
+  float e0 = (old.x - (s0 - b0)) + (val.x - b0);
+  float s1 = old.y + val.y, b1 = s1 - old.y;
+  float e1 = (old.y - (s1 - b1)) + (val.y - b1);
+  if (e0 != 0.0f || e1 != 0.0f) atomicAdd(reinterpret_cast<float2 *>(a.grid_lo + idx), make_float2(e0, e1));
+}
+
+// Drain the calling warp's queue (warp-uniform call).
+template <int NC>
+__device__ __forceinline__ void drain_queue(const GridArgs &a, long long nxy, FlushRec<NC> *q, int *qn) {
+#if defined(BULLSEYE_SINGLE)
+  __syncwarp();
+  const int n = min(*qn, kFlushQueueCap);
+  const int lane = threadIdx.x & 31;
+  for (int i = lane; i < n; i += 32) {
+    const FlushRec<NC> r = q[i];
+    float2 old[NC];
+#pragma unroll
+    for (int k = 0; k < NC; ++k) old[k] = atomicAdd(reinterpret_cast<float2 *>(a.grid + r.cell + k * nxy), r.v[k]);
+#pragma unroll
+    for (int k = 0; k < NC; ++k) compensated_add<NC>(a, r.cell + k * nxy, r.v[k], old[k]);
+  }
+  __syncwarp();
+  if (lane == 0) *qn = 0;
+  __syncwarp();
+#endif
+}
+
+// Queue one owned cell's accumulator (falls back to a direct flush when the queue is full).
+template <int NC>
+__device__ __forceinline__ void queue_cell(const GridArgs &a, long long slice0, long long nxy, int x, int y,
+                                           cplx (&acc)[NC], FlushRec<NC> *q, int *qn) {
+#if defined(BULLSEYE_SINGLE)
+  const int slot = atomicAdd(qn, 1);
+  if (slot < kFlushQueueCap) {
+    FlushRec<NC> r;
+    r.cell = slice0 * nxy + (long long)y * a.nx + x;
+#pragma unroll
+    for (int k = 0; k < NC; ++k) r.v[k] = make_float2(acc[k].re, acc[k].im);
+    q[slot] = r;
+#pragma unroll
+    for (int k = 0; k < NC; ++k) { acc[k].re = 0; acc[k].im = 0; }
+  } else {
+    flush_cell<NC, true>(a, slice0, nxy, x, y, acc);
+  }
+#endif
+}
+
 template <int NC, bool WPROJ>
 __device__ __forceinline__ void prologue(const GridArgs &a, int f_local, int chan, long long row, bool in_range,
-                                         VisRec<NC> &rec) {
+                                         VisRec<NC> &rec, unsigned &cached_spw, double &cached_inv,
+                                         const double plane_scale) {
   rec.valid = 0;
   if (!in_range) return;
   const int c = chan;
@@ -240,7 +304,11 @@ __device__ __forceinline__ void prologue(const GridArgs &a, int f_local, int cha
   }
   const int fglob = a.facet_base + f_local;
   const FacetXform fx = a.facets[f_local];
-  double inv_lambda = 1.0 / (double)a.wavelengths[sc];
+  if (spw != cached_spw) {  // 1/lambda is constant along a track unless the spw changes
+    cached_spw = spw;
+    cached_inv = 1.0 / (double)a.wavelengths[sc];
+  }
+  const double inv_lambda = cached_inv;
   double u = (double)a.uvw[3 * row] * inv_lambda;
   double v = (double)a.uvw[3 * row + 1] * inv_lambda;
   double w = (double)a.uvw[3 * row + 2] * inv_lambda;
@@ -329,7 +397,7 @@ __device__ __forceinline__ void prologue(const GridArgs &a, int f_local, int cha
   double dv_d = WPROJ ? rint(v + a.gcy) : floor(v + a.gcy);
   long long plane = 0;
   if (WPROJ) {
-    double pl = rint(fabs(w) / a.wmax * (double)(a.P - 1));
+    double pl = rint(fabs(w) * plane_scale);
     plane = (pl >= 0.0 && pl < (double)a.P) ? (long long)pl : -1;  // NaN and out of range -> dropped
   }
   if (!(du_d >= 0.0 && dv_d >= 0.0 && du_d + (a.W + 2) < (double)a.nx && dv_d + (a.W + 2) < (double)a.ny &&
@@ -350,12 +418,26 @@ __device__ __forceinline__ void prologue(const GridArgs &a, int f_local, int cha
 }
 
 // Shared-memory bytes for a launch with V staged visibilities.
+// Per-warp flush queues (compensated single precision only), for up to 16 warps.
+template <int NC>
+__host__ __device__ inline size_t flush_queue_bytes() {
+#if defined(BULLSEYE_SINGLE)
+  return 16 * (sizeof(FlushRec<NC>) * kFlushQueueCap + 16);
+#else
+  return 0;
+#endif
+}
+
+// Row taps are stored W + kTvPad long per visibility: the first kTvPad taps are repeated after the
+// last, so the J consecutive row classes of a thread read consecutive addresses without a wrap.
+constexpr int kTvPad = 15;
+
 template <int NC, bool WPROJ>
 __host__ __device__ inline size_t grid_smem_bytes(int V, int W) {
   size_t recs = sizeof(VisRec<NC>) * (size_t)V;
   size_t norm = (sizeof(double) * NC + 2 * sizeof(int)) * (size_t)V;  // per-lane normalisation state
-  size_t taps = sizeof(typename TapT<WPROJ>::type) * (size_t)V * W * 2;
-  return recs + norm + taps + 64;
+  size_t taps = sizeof(typename TapT<WPROJ>::type) * (size_t)V * (2 * W + kTvPad);
+  return recs + norm + taps + flush_queue_bytes<NC>() + 64;
 }
 
 // premultiplied visibility times the column tap
@@ -404,7 +486,15 @@ __global__ void __launch_bounds__(512, 1) romein_grid_kernel(const GridArgs a) {
   int *s_ng = reinterpret_cast<int *>(s_nacc + (size_t)a.V * NC);                    // [V]
   int *s_mixed = s_ng + a.V;                                                          // [V]
   tap_t *tu = reinterpret_cast<tap_t *>(smem_raw + ((sizeof(VisRec<NC>) + sizeof(double) * NC + 2 * sizeof(int)) * a.V + 15) / 16 * 16);
+  const int TVS = a.W + kTvPad;  // row-tap stride per staged visibility
   tap_t *tv = tu + a.V * a.W;
+  // per-warp flush queues follow the taps
+  unsigned char *qbase = reinterpret_cast<unsigned char *>(tv + a.V * TVS);
+  qbase = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(qbase) + 15) & ~(uintptr_t)15);
+  const int warp_id = threadIdx.x >> 5;
+  FlushRec<NC> *fq = reinterpret_cast<FlushRec<NC> *>(qbase) + warp_id * kFlushQueueCap;
+  int *fqn = reinterpret_cast<int *>(qbase + 16 * sizeof(FlushRec<NC>) * kFlushQueueCap) + warp_id * 4;
+  if (COMP && (threadIdx.x & 31) == 0) *fqn = 0;
   __shared__ int s_same_g;
   __shared__ double s_norm[NC];
 
@@ -444,39 +534,44 @@ __global__ void __launch_bounds__(512, 1) romein_grid_kernel(const GridArgs a) {
     s_mixed[tid] = 0;
   }
 
-  // Register state: accumulators of the J owned cells and the footprint they belong to.  The
-  // owned cells are (pu0 + ou, pv0 + ovj[j]) for the last footprint corner (pu0, pv0).
+  // Register state: accumulators of the J owned cells and the footprint they belong to.  For
+  // the last footprint corner (pu0, pv0) the owned cells are (pu0 + ou, pv0 + wrap(ov0 + j)),
+  // wrap(i) = i - W when i >= W.
   cplx acc[J][NC];
-  int ovj[J];
 #pragma unroll
   for (int j = 0; j < J; ++j) {
-    ovj[j] = 0;
 #pragma unroll
     for (int k = 0; k < NC; ++k) { acc[j][k].re = 0; acc[j][k].im = 0; }
   }
   unsigned dirty = 0;
-  int cg = -1, pu0 = -1, pv0 = -1, ou = 0;
+  int cg = -1, pu0 = -1, pv0 = -1, ou = 0, ov0 = 0;
+  unsigned cached_spw = 0xffffffffu;
+  double cached_inv = 0.0;
+  const double plane_scale = WPROJ ? (double)(a.P - 1) / a.wmax : 0.0;
 
   for (long long base = r0; base < r1; base += a.V) {
     const int nv = (int)min((long long)a.V, r1 - base);
     if (tid < a.V) {
       VisRec<NC> rec;
-      prologue<NC, WPROJ>(a, f_local, chan, base + tid, tid < nv, rec);
+      prologue<NC, WPROJ>(a, f_local, chan, base + tid, tid < nv, rec, cached_spw, cached_inv, plane_scale);
       recs[tid] = rec;
     }
     __syncthreads();
-    // gather the 2W taps of every staged visibility
-    const int per = 2 * W;
+    // gather the taps of every staged visibility: W column taps, W + kTvPad row taps
+    const int per = 2 * W + kTvPad;
     for (int idx = tid; idx < nv * per; idx += blockDim.x) {
       const int vi = idx / per, j = idx - vi * per;
       const VisRec<NC> &r = recs[vi];
       if (!r.valid) continue;
       const bool isv = j >= W;
-      const int jj = isv ? j - W : j;
+      int jj = isv ? j - W : j;
+      tap_t *dst = isv ? tv + vi * TVS + jj : tu + vi * W + jj;
+      if (jj >= W) jj -= W;  // repeated leading row taps
+      if (jj >= W) jj = W - 1;
       const long long ti = (long long)r.plane * a.K + (isv ? r.fv : r.fu) + (long long)jj * a.os;
       tap_t t;
       load_tap(a.conv, ti, t);
-      (isv ? tv : tu)[vi * W + jj] = t;
+      *dst = t;
     }
     __syncthreads();
     // normalisation, four lanes per staged visibility: Re(sum_u k_u * sum_v k_v) x weight x flag
@@ -487,15 +582,16 @@ __global__ void __launch_bounds__(512, 1) romein_grid_kernel(const GridArgs a) {
         const int q = b4 + (tid & 31);
         const int vi = q >> 2, part = q & 3;
         const bool act = vi < nv;
-        double sur = 0, sui = 0, svr = 0, svi = 0;
+        // tap sums in the library's working precision (FP64 units are scarce on this GPU)
+        acc_real sur = 0, sui = 0, svr = 0, svi = 0;
         if (act) {
           if (WPROJ) {
             const cplx *pu = reinterpret_cast<const cplx *>(tu) + vi * W;
-            const cplx *pv = reinterpret_cast<const cplx *>(tv) + vi * W;
+            const cplx *pv = reinterpret_cast<const cplx *>(tv) + vi * TVS;
             for (int j = part; j < W; j += 4) { sur += pu[j].re; sui += pu[j].im; svr += pv[j].re; svi += pv[j].im; }
           } else {
             const acc_real *pu = reinterpret_cast<const acc_real *>(tu) + vi * W;
-            const acc_real *pv = reinterpret_cast<const acc_real *>(tv) + vi * W;
+            const acc_real *pv = reinterpret_cast<const acc_real *>(tv) + vi * TVS;
             for (int j = part; j < W; j += 4) { sur += pu[j]; svr += pv[j]; }
           }
         }
@@ -508,7 +604,7 @@ __global__ void __launch_bounds__(512, 1) romein_grid_kernel(const GridArgs a) {
         }
         if (act && part == 0 && recs[vi].valid) {
           const VisRec<NC> &r = recs[vi];
-          const double nt = sur * svr - sui * svi;
+          const double nt = (double)sur * (double)svr - (double)sui * (double)svi;
           double *na = s_nacc + vi * NC;
           if (s_ng[vi] != r.g) {
             if (s_ng[vi] >= 0) {
@@ -526,8 +622,9 @@ __global__ void __launch_bounds__(512, 1) romein_grid_kernel(const GridArgs a) {
         }
       }
     }
-    // grid the staged chunk
-    if (rows_mask) {
+    // grid the staged chunk (every lane of a warp with any owned cell takes part, so the
+    // queue drains below are warp-uniform)
+    if (__any_sync(0xffffffffu, rows_mask != 0)) {
       for (int vi = 0; vi < nv; ++vi) {
         const int4 h0 = *reinterpret_cast<const int4 *>(&recs[vi].u0);
         const int4 h1 = *reinterpret_cast<const int4 *>(&recs[vi].g);
@@ -536,52 +633,72 @@ __global__ void __launch_bounds__(512, 1) romein_grid_kernel(const GridArgs a) {
           // footprint moved: recompute the owned cells, flush those that changed
           int o = du - h0.z;
           o += (o < 0) ? W : 0;
+          int nov0 = strip * J - h0.w;
+          nov0 += (nov0 < 0) ? W : 0;
           if (h0.x + o != pu0 + ou || h1.x != cg) {
             if (dirty) {
 #pragma unroll
               for (int j = 0; j < J; ++j)
-                if (dirty & (1u << j)) flush_cell<NC, COMP>(a, (fslice + cg) * NC, nxy, pu0 + ou, pv0 + ovj[j], acc[j]);
+                if (dirty & (1u << j)) {
+                  const int oy = ov0 + j >= W ? ov0 + j - W : ov0 + j;
+                  if (COMP)
+                    queue_cell<NC>(a, (fslice + cg) * NC, nxy, pu0 + ou, pv0 + oy, acc[j], fq, fqn);
+                  else
+                    flush_cell<NC, false>(a, (fslice + cg) * NC, nxy, pu0 + ou, pv0 + oy, acc[j]);
+                }
               dirty = 0;
             }
             cg = h1.x;
           }
+          if (dirty) {
 #pragma unroll
-          for (int j = 0; j < J; ++j) {
-            int ov = strip * J + j - h0.w;
-            ov += (ov < 0) ? W : 0;
-            if ((dirty & (1u << j)) && h0.y + ov != pv0 + ovj[j]) {
-              flush_cell<NC, COMP>(a, (fslice + cg) * NC, nxy, pu0 + ou, pv0 + ovj[j], acc[j]);
-              dirty &= ~(1u << j);
+            for (int j = 0; j < J; ++j) {
+              const int oy = ov0 + j >= W ? ov0 + j - W : ov0 + j;
+              const int ny = nov0 + j >= W ? nov0 + j - W : nov0 + j;
+              if ((dirty & (1u << j)) && h0.y + ny != pv0 + oy) {
+                if (COMP)
+                  queue_cell<NC>(a, (fslice + cg) * NC, nxy, pu0 + ou, pv0 + oy, acc[j], fq, fqn);
+                else
+                  flush_cell<NC, false>(a, (fslice + cg) * NC, nxy, pu0 + ou, pv0 + oy, acc[j]);
+                dirty &= ~(1u << j);
+              }
             }
-            ovj[j] = ov;
           }
-          ou = o;
+          // columns beyond W (padding lanes) read in-bounds taps and are never flushed
+          ou = o < W ? o : W - 1;
+          ov0 = nov0;
           pu0 = h0.x;
           pv0 = h0.y;
+        }
+        if (COMP) {
+          __syncwarp();
+          if (*fqn >= kDrainAt) drain_queue<NC>(a, nxy, fq, fqn);
         }
         const tap_t tuv = tu[vi * W + ou];
         cplx pre[NC];
 #pragma unroll
         for (int k = 0; k < NC; ++k) pre[k] = premul(recs[vi].vis[k], tuv);
-        const tap_t *tvrow = tv + vi * W;
+        // J consecutive row taps from one base (rows past W are in-bounds padding, never flushed)
+        const tap_t *tvrow = tv + vi * TVS + ov0;
 #pragma unroll
         for (int j = 0; j < J; ++j) {
-          if (rows_mask & (1u << j)) {
-            const tap_t t = tvrow[ovj[j]];
+          const tap_t t = tvrow[j];
 #pragma unroll
-            for (int k = 0; k < NC; ++k) mac(acc[j][k], pre[k], t);
-          }
+          for (int k = 0; k < NC; ++k) mac(acc[j][k], pre[k], t);
         }
         dirty = rows_mask;
       }
+      if (COMP) drain_queue<NC>(a, nxy, fq, fqn);
     }
     __syncthreads();
   }
   // final flush of owned cells
   if (dirty) {
 #pragma unroll
-    for (int j = 0; j < J; ++j)
-      if (dirty & (1u << j)) flush_cell<NC, COMP>(a, (fslice + cg) * NC, nxy, pu0 + ou, pv0 + ovj[j], acc[j]);
+    for (int j = 0; j < J; ++j) {
+      const int oy = ov0 + j >= W ? ov0 + j - W : ov0 + j;
+      if (dirty & (1u << j)) flush_cell<NC, COMP>(a, (fslice + cg) * NC, nxy, pu0 + ou, pv0 + oy, acc[j]);
+    }
   }
   // normalisation: one reduction per CTA when every staged slot saw a single grid group
   if (want_norm) {
