@@ -59,6 +59,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-comp", action="store_true", help="plain (uncompensated) FP32 grid flushes")
     ap.add_argument("--chans", type=int, default=0, help="override the channel count (profiling cases)")
+    ap.add_argument("--form", default="batched", choices=["batched", "plain"],
+                    help="batched: bullseye_grid_batched; plain: the per-call drop-in ABI path")
+    ap.add_argument("--no-other", action="store_true", help="skip timing the other form")
     ap.add_argument("--facets", type=int, default=0, help="override the facet count (profiling cases)")
     return ap.parse_args()
 
@@ -96,6 +99,36 @@ def kernel_stack(wmax):
     fov = NX * CELL * np.pi / (180 * 3600)
     stack, supports = wproj_kernels(S_HALF, OS, WPLANES, wmax, fov, min_support=MIN_SUPPORT)
     return stack.astype(np.complex64), supports
+
+
+def support_class_widths(conv, W, os_):
+    """Per w plane, the support-class width the batched gridder uses (same rule as the library:
+    the plane's possibly-nonzero support window rounded up to 16, 24, ..., 56 or W)."""
+    widths = [w for w in (16, 24, 32, 40, 48, 56) if w < W] + [W]
+    out = []
+    for row in conv:
+        nz = np.nonzero(np.abs(row) > 0)[0]
+        if nz.size == 0:
+            out.append(widths[0])
+            continue
+        slo = max(0, int(np.ceil((nz[0] - 2 * os_ + 1) / os_)))
+        shi = min(W - 1, nz[-1] // os_)
+        width = max(1, shi - slo + 1)
+        out.append(next((w for w in widths if w >= width), W))
+    return np.asarray(out)
+
+
+def effective_taps(geo, conv):
+    """Sum over (row, channel) of W_class^2: the taps the batched gridder processes per facet."""
+    W = 2 * S_HALF + 1
+    wc = support_class_widths(conv, W, OS)
+    w = np.abs(geo["uvw"][:, 2])
+    total = 0.0
+    for lam in geo["lam"]:
+        pl = np.rint(w / lam * ((WPLANES - 1) / geo["wmax"])).astype(np.int64)
+        pl = np.clip(pl, 0, WPLANES - 1)
+        total += float(np.sum(wc[pl].astype(np.float64) ** 2))
+    return total
 
 
 def device_inputs(geo, torch):
@@ -371,9 +404,32 @@ def main():
     st.is_final_data_chunk = False
     stream = torch.cuda.ExternalStream(lib.bullseye_get_stream())
 
-    def step():
+    def step_plain():
         lib.facet_4_cor_corrections(ctypes.byref(st))
         lib.facet_sampling_function(ctypes.byref(st))
+
+    def step_batched():
+        rc = lib.bullseye_grid_batched(ctypes.byref(st), 0, 1)
+        if rc:
+            check(lib)
+
+    step = step_plain if args.form == "plain" else step_batched
+
+    # the other form, timed the same way, reported beside the headline form
+    other = step_batched if args.form == "plain" else step_plain
+    other_ms = None
+    if not args.no_other:
+        other()
+        torch.cuda.synchronize()
+        check(lib)
+        o0 = torch.cuda.Event(enable_timing=True)
+        o1 = torch.cuda.Event(enable_timing=True)
+        o0.record(stream)
+        other()
+        o1.record(stream)
+        torch.cuda.synchronize()
+        other_ms = o0.elapsed_time(o1)
+        lib.bullseye_zero_grids()
 
     for _ in range(args.warmup):
         step()
@@ -409,10 +465,23 @@ def main():
     value = pairs_per_step * world / (ms_per_step * 1e-3) / 1e6
     fp32_peak = lib.bullseye_fp32_fma_tflops(4096)
     W = 2 * S_HALF + 1
-    flops_per_pair = 8 * 4 * W * W + 6 * 4 + 128
-    launch_ms = vis_kernel_ms / n_vis_launch
-    achieved = pairs_per_step * flops_per_pair / (launch_ms * 1e-3) / 1e12
     bytes_per_pair = 8 * 4 + 4 * 4 + 4 + 12 + 64
+    if args.form == "plain":
+        # dominant kernel: the visibility gridder launch (CUDA events around it in the library)
+        flops_per_pair = 8 * 4 * W * W + 6 * 4 + 128
+        launch_ms = vis_kernel_ms / n_vis_launch
+        step_flops = pairs_per_step * flops_per_pair
+        kernel_name = "romein_grid_kernel<4,wproj,J=8,wide> (visibilities, padded W=63)"
+    else:
+        # batched: the per-class persistent gridder launches make up the step; algorithmic flops
+        # are those of the support windows actually gridded (complex tap x 4 correlations, plus
+        # the facet-invariant sampling function once), over the whole step time
+        taps = effective_taps(geo, conv)
+        step_flops = taps * N_FACETS * 8 * 4 + taps * 8 + pairs_per_step * (6 * 4 + 128)
+        flops_per_pair = step_flops / pairs_per_step
+        launch_ms = ms_per_step
+        kernel_name = "romein_segment_kernel per support class (whole batched step)"
+    achieved = step_flops / (launch_ms * 1e-3) / 1e12
     hbm_gbs = pairs_per_step * bytes_per_pair / (launch_ms * 1e-3) / 1e9
     peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(REPO, "MEASURED_PEAKS.json")) else {}
@@ -439,8 +508,11 @@ def main():
             lib.initLibrary(ctypes.byref(s2))
             set_rows(s2, hnp, lambda a: a.ctypes.data_as(P))
             s2.is_final_data_chunk = True
-            lib.facet_4_cor_corrections(ctypes.byref(s2))
-            lib.facet_sampling_function(ctypes.byref(s2))
+            if args.form == "plain":
+                lib.facet_4_cor_corrections(ctypes.byref(s2))
+                lib.facet_sampling_function(ctypes.byref(s2))
+            else:
+                lib.bullseye_grid_batched(ctypes.byref(s2), 0, 1)
             lib.gridding_barrier()
             lib.weight_uniformly(ctypes.byref(s2))
             lib.normalize(ctypes.byref(s2))
@@ -463,8 +535,9 @@ def main():
         d2h = tab.grid.nbytes + tab.sf.nbytes + N_FACETS * NX * NX * (8 + 4)
         e2e = {"value": pairs_per_step / dt / 1e6, "unit": "Mvis/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "s_per_step": dt,
-               "calls": "initLibrary, facet_4_cor_corrections, facet_sampling_function, weight_uniformly, normalize, "
-                        "finalize, releaseLibrary (host pinned buffers)"}
+               "calls": ("initLibrary, " + ("facet_4_cor_corrections, facet_sampling_function"
+                                             if args.form == "plain" else "bullseye_grid_batched(call 0, sampling)") +
+                         ", weight_uniformly, normalize, finalize, releaseLibrary (host pinned buffers)")}
 
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
@@ -477,11 +550,16 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "rows": R, "channels": N_CHAN, "facets": N_FACETS,
                        "vis_facet_pairs_per_step": pairs_per_step, "l2": "inputs 4.2 GB per step > 129 MB L2",
-                       "form": "plain drop-in (per-call launches, compensated FP32)"},
+                       "form": ("batched: bullseye_grid_batched (support-aware, persistent per-class launches, "
+                                "CUDA graph, compensated FP32)" if args.form == "batched" else
+                                "plain: per-call drop-in ABI path (padded support, compensated FP32)")},
+            "other_form": None if other_ms is None else {
+                "form": "plain" if args.form == "batched" else "batched", "ms_per_step": other_ms,
+                "value": pairs_per_step * world / (other_ms * 1e-3) / 1e6, "unit": "Mvis/s"},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                          "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
                          "peak_source": "measured FP32 FMA probe on this GPU (MEASURED_PEAKS.json has no FP32 rate)",
-                         "kernel": "romein_grid_kernel<4,wproj,J=8> (visibilities)", "launch_ms": launch_ms,
+                         "kernel": kernel_name, "launch_ms": launch_ms,
                          "flops_per_pair": flops_per_pair, "hbm_gbs": hbm_gbs,
                          "hbm_frac_of_measured": hbm_gbs / peaks["hbm_gbs"] if peaks.get("hbm_gbs") else None,
                          "sampling_kernel_ms": sf_kernel_ms / max(1, cnt.value)},

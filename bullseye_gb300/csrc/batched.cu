@@ -1,0 +1,541 @@
+// Batched, support-aware gridding: one call grids every facet (and the sampling function) of a
+// chunk with a schedule built on the device and replayed as a CUDA graph.
+//
+// Support awareness.  The reference's ABI carries one padded kernel support W for every w plane
+// (bullseye/mo/cpu_gpu_common/gridding_parameters.h:66-67), so each visibility is spread over
+// W x W cells even when its plane's kernel is much narrower; the taps outside a plane's window
+// are exactly zero.  The window of every plane is read from the kernel table once, rounded up to
+// a support class (a few widths), and each visibility is gridded over its class's window only:
+// the same sums, computed over nonzero (or possibly nonzero) taps.
+//
+// Schedule (all on the device, so it can be captured and replayed):
+//   classify     class of every (channel, row) from its w plane (FP64, as the gridder);
+//   seg_count    per track (baseline, channel): number of runs of one class;
+//   scan         track offsets;
+//   seg_write    the runs {row_begin, row_end, channel, class};
+//   bucket       runs ordered by class;
+//   per class    one persistent Romein launch (romein_segment_kernel) over (run, facet) items,
+//                with the thread layout chosen for that class width by the autotuner; then the
+//                same for the sampling function (facet-invariant, gridded once).
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include "context.h"
+
+using namespace bz;
+
+namespace {
+
+constexpr int kMaxClasses = 8;
+
+__global__ void classify_kernel(const vis_real *__restrict__ uvw, const unsigned *__restrict__ spw,
+                                const vis_real *__restrict__ wavelengths, int nchan, int nspw, long long R,
+                                double wmax, int P, const int *__restrict__ plane_class, unsigned char *__restrict__ cls) {
+  const double plane_scale = P > 1 ? (double)(P - 1) / wmax : 0.0;  // as the gridder's prologue
+  const long long total = (long long)nchan * R;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(i / R);
+    const long long r = i - (long long)c * R;
+    int k = plane_class[0];
+    if (P > 1) {
+      const unsigned s = spw[r];
+      if (s < (unsigned)nspw) {
+        const double inv = 1.0 / (double)wavelengths[(long long)s * nchan + c];
+        const double w = (double)uvw[3 * r + 2] * inv;
+        const double pl = rint(fabs(w) * plane_scale);
+        if (pl >= 0.0 && pl < (double)P) k = plane_class[(int)pl];
+      }
+    }
+    cls[i] = (unsigned char)k;
+  }
+}
+
+__device__ __forceinline__ void track_rows(int t, int nchan, int nslots, int seg_len, long long R, const size_t *starts,
+                                           int &c, long long &r0, long long &r1) {
+  const int b = t / nchan;
+  c = t - b * nchan;
+  if (starts) {
+    r0 = (long long)starts[b];
+    r1 = (long long)starts[b + 1];
+  } else {
+    r0 = (long long)b * seg_len;
+    r1 = r0 + seg_len;
+  }
+  if (r1 > R) r1 = R;
+  if (r0 > r1) r0 = r1;
+}
+
+__global__ void seg_count_kernel(const size_t *starts, int nslots, int seg_len, long long R, int nchan,
+                                 const unsigned char *__restrict__ cls, int *__restrict__ nseg) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nslots * nchan) return;
+  int c;
+  long long r0, r1;
+  track_rows(t, nchan, nslots, seg_len, R, starts, c, r0, r1);
+  const unsigned char *k = cls + (long long)c * R;
+  int n = 0;
+  int prev = -1;
+  for (long long r = r0; r < r1; ++r) {
+    if (k[r] != prev) {
+      ++n;
+      prev = k[r];
+    }
+  }
+  nseg[t] = n;
+}
+
+// Exclusive scan of n ints by one block; total -> *total.
+__global__ void scan_kernel(const int *__restrict__ in, int *__restrict__ out, int n, int *total) {
+  __shared__ int part[1024];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int per = (n + nt - 1) / nt;
+  const int lo = tid * per, hi = min(n, lo + per);
+  int s = 0;
+  for (int i = lo; i < hi; ++i) s += in[i];
+  part[tid] = s;
+  __syncthreads();
+  for (int off = 1; off < nt; off <<= 1) {
+    int v = tid >= off ? part[tid - off] : 0;
+    __syncthreads();
+    part[tid] += v;
+    __syncthreads();
+  }
+  int run = tid ? part[tid - 1] : 0;
+  for (int i = lo; i < hi; ++i) {
+    out[i] = run;
+    run += in[i];
+  }
+  if (tid == nt - 1) *total = part[nt - 1];
+}
+
+__global__ void seg_write_kernel(const size_t *starts, int nslots, int seg_len, long long R, int nchan,
+                                 const unsigned char *__restrict__ cls, const int *__restrict__ off,
+                                 int4 *__restrict__ segs, int *__restrict__ class_count) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nslots * nchan) return;
+  int c;
+  long long r0, r1;
+  track_rows(t, nchan, nslots, seg_len, R, starts, c, r0, r1);
+  const unsigned char *k = cls + (long long)c * R;
+  int o = off[t];
+  long long begin = r0;
+  for (long long r = r0; r < r1; ++r) {
+    if (r + 1 == r1 || k[r + 1] != k[r]) {
+      segs[o++] = make_int4((int)begin, (int)(r + 1), c, (int)k[r]);
+      atomicAdd(&class_count[k[r]], 1);
+      begin = r + 1;
+    }
+  }
+}
+
+__global__ void class_offsets_kernel(const int *class_count, int *class_off, int *class_cursor, int ncls) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int s = 0;
+  for (int k = 0; k < ncls; ++k) {
+    class_off[k] = s;
+    class_cursor[k] = 0;
+    s += class_count[k];
+  }
+}
+
+__global__ void bucket_kernel(const int4 *__restrict__ segs, const int *total, int4 *__restrict__ sorted,
+                              int *class_cursor, const int *class_off) {
+  const int n = *total;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int4 s = segs[i];
+    const int pos = class_off[s.w] + atomicAdd(&class_cursor[s.w], 1);
+    sorted[pos] = s;
+  }
+}
+
+// ---------------------------------------------------------------- launch variants
+struct Variant {
+  int J;
+  bool wide;
+  int NT, V, grid;
+  size_t smem;
+};
+
+template <int NC, bool WPROJ, bool COMP>
+using SegKernel = void (*)(const GridArgs, const int);
+
+template <int NC, bool WPROJ, bool COMP>
+SegKernel<NC, WPROJ, COMP> seg_kernel(int J, bool wide) {
+  if (wide) return J == 4 ? romein_segment_kernel<NC, WPROJ, 4, COMP, true> : romein_segment_kernel<NC, WPROJ, 8, COMP, true>;
+  return J == 4 ? romein_segment_kernel<NC, WPROJ, 4, COMP, false> : romein_segment_kernel<NC, WPROJ, 8, COMP, false>;
+}
+
+template <int NC, bool WPROJ>
+bool make_variant(int W, int J, bool wide, Variant &v) {
+  const int cols = ((W + 31) / 32) * 32;
+  if (wide && (cols - W) * 8 > W) return false;
+  const int owners = wide ? cols * ((W + J - 1) / J) : W * ((W + J - 1) / J);
+  v.J = J;
+  v.wide = wide;
+  v.NT = std::max(32, ((owners + 31) / 32) * 32);
+  if (v.NT > 512) return false;
+  const size_t budget = 160 * 1024;
+  const size_t per = sizeof(VisRec<NC>) + sizeof(double) * NC + 2 * sizeof(int) +
+                     sizeof(typename TapT<WPROJ>::type) * (2 * (size_t)W + kTvPad);
+  v.V = std::max(1, (int)std::min<size_t>(v.NT, (budget - 64) / per));
+  v.smem = grid_smem_bytes<NC, WPROJ>(v.V, W);
+  return true;
+}
+
+struct ClassInfo {
+  int width;
+  Variant vis, sf;  // chosen layouts for the visibility (NC = c.C) and sampling (NC = 1) launches
+};
+
+struct BatchedState {
+  bool planned = false;
+  int ncls = 0;
+  ClassInfo cls[kMaxClasses];
+  DevBuf<int> plane_class, plane_lo;
+  DevBuf<unsigned char> row_class;
+  DevBuf<int> nseg, seg_off, seg_total, class_count, class_off, class_cursor, work_next, sample_count;
+  DevBuf<int4> segs, sorted;
+  size_t rows_cap = 0, tracks_cap = 0, segs_cap = 0;
+  // tuning decisions, by (class width, NC, WPROJ, COMP)
+  std::map<std::tuple<int, int, int, int>, std::pair<int, int>> tuned;
+  // captured graph
+  cudaGraphExec_t exec = nullptr;
+  std::vector<unsigned char> key;
+};
+BatchedState g_bs;
+
+// Support windows of every w plane, rounded up to a class width.
+bool plan_classes() {
+  Context &c = g_ctx;
+  BatchedState &b = g_bs;
+  const int W = (int)c.W, os = (int)c.os, K = (int)c.K, P = (int)c.P;
+  const bool wproj = c.P > 1;
+  std::vector<int> widths;
+  for (int w : {16, 24, 32, 40, 48, 56})
+    if (w < W) widths.push_back(w);
+  widths.push_back(W);
+  std::vector<int> pcls(P), plo(P);
+  std::vector<int> used(widths.size(), 0);
+  for (int p = 0; p < P; ++p) {
+    int nzlo = -1, nzhi = -1;
+    for (int i = 0; i < K; ++i) {
+      bool nz;
+      if (wproj) nz = c.conv_host[2 * ((size_t)p * K + i)] != 0 || c.conv_host[2 * ((size_t)p * K + i) + 1] != 0;
+      else nz = c.conv_host[i] != 0;
+      if (nz) {
+        if (nzlo < 0) nzlo = i;
+        nzhi = i;
+      }
+    }
+    int slo = 0, shi = 0;
+    if (nzlo >= 0) {
+      // a tap of support index s reads offset f + s*os with f in [0, 2 os): keep every s that can
+      // reach a nonzero sample
+      slo = std::max(0, (int)std::ceil((double)(nzlo - 2 * os + 1) / os));
+      shi = std::min(W - 1, nzhi / os);
+    }
+    const int width = std::max(1, shi - slo + 1);
+    int k = (int)widths.size() - 1;
+    for (int j = 0; j < (int)widths.size(); ++j)
+      if (widths[j] >= width) { k = j; break; }
+    pcls[p] = k;
+    plo[p] = std::min(slo, W - widths[k]);
+    used[k] = 1;
+  }
+  b.ncls = (int)widths.size();
+  if (b.ncls > kMaxClasses) return false;
+  for (int k = 0; k < b.ncls; ++k) b.cls[k].width = widths[k];
+  if (!b.plane_class.alloc(P) || !b.plane_lo.alloc(P)) return false;
+  BZ_CUDA_TRY_RET(cudaMemcpy(b.plane_class.ptr, pcls.data(), sizeof(int) * P, cudaMemcpyHostToDevice), false);
+  BZ_CUDA_TRY_RET(cudaMemcpy(b.plane_lo.ptr, plo.data(), sizeof(int) * P, cudaMemcpyHostToDevice), false);
+  if (!b.class_count.alloc(kMaxClasses) || !b.class_off.alloc(kMaxClasses) || !b.class_cursor.alloc(kMaxClasses) ||
+      !b.work_next.alloc(2 * kMaxClasses) || !b.seg_total.alloc(1) || !b.sample_count.alloc(kMaxClasses))
+    return false;
+  b.planned = true;
+  return true;
+}
+
+// Grows the schedule buffers; a reallocation invalidates the captured graph (it holds the
+// buffer addresses).
+bool ensure_capacity(size_t rows, size_t tracks) {
+  Context &c = g_ctx;
+  BatchedState &b = g_bs;
+  const void *before[3] = {b.row_class.ptr, b.nseg.ptr, b.segs.ptr};
+  if (rows * c.nchan > b.rows_cap) {
+    if (!b.row_class.alloc(rows * c.nchan)) return false;
+    b.rows_cap = rows * c.nchan;
+  }
+  if (tracks > b.tracks_cap) {
+    if (!b.nseg.alloc(tracks) || !b.seg_off.alloc(tracks)) return false;
+    b.tracks_cap = tracks;
+  }
+  // runs: at most one per (track, class change); bound by rows x channels
+  const size_t maxseg = std::max<size_t>(rows * c.nchan, 1);
+  if (maxseg > b.segs_cap) {
+    if (!b.segs.alloc(maxseg) || !b.sorted.alloc(maxseg)) return false;
+    b.segs_cap = maxseg;
+  }
+  if (before[0] != b.row_class.ptr || before[1] != b.nseg.ptr || before[2] != b.segs.ptr) {
+    if (b.exec) cudaGraphExecDestroy(b.exec);
+    b.exec = nullptr;
+  }
+  return true;
+}
+
+template <int NC, bool WPROJ, bool COMP>
+bool launch_class(const GridArgs &base, int k, const Variant &v, int nfacets, const int *count, int *next,
+                  cudaStream_t st) {
+  GridArgs a = base;
+  a.W = g_bs.cls[k].width;
+  a.V = v.V;
+  a.plane_lo = g_bs.plane_lo.ptr;
+  a.segments = g_bs.sorted.ptr;
+  a.segment_base = g_bs.class_off.ptr + k;
+  a.work_count = count;
+  a.work_next = next;
+  auto kern = seg_kernel<NC, WPROJ, COMP>(v.J, v.wide);
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem) != cudaSuccess) {
+    bz_record_error(BZ_ERR_CUDA, "batched: cudaFuncSetAttribute failed");
+    return false;
+  }
+  BZ_CUDA_TRY_RET(cudaMemsetAsync(next, 0, sizeof(int), st), false);
+  kern<<<v.grid, v.NT, v.smem, st>>>(a, nfacets);
+  g_ctx.launches++;
+  BZ_CUDA_TRY_RET(cudaGetLastError(), false);
+  return true;
+}
+
+template <int NC, bool WPROJ, bool COMP>
+bool finish_variant(Variant &v) {
+  auto kern = seg_kernel<NC, WPROJ, COMP>(v.J, v.wide);
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem) != cudaSuccess) return false;
+  int per_sm = 0, dev = 0, sms = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, v.NT, v.smem) != cudaSuccess || per_sm < 1) return false;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  v.grid = per_sm * sms;
+  return true;
+}
+
+// Autotuner: time every valid layout of a class on a sample of its own work items, gridding into
+// scratch grids, and keep the fastest.  Decisions are cached by (width, NC, WPROJ, COMP).
+template <int NC, bool WPROJ, bool COMP>
+bool tune_class(const GridArgs &base, int k, int nfacets, Variant &out, int host_count) {
+  BatchedState &b = g_bs;
+  Context &c = g_ctx;
+  const int W = b.cls[k].width;
+  auto key = std::make_tuple(W, NC, (int)WPROJ, (int)COMP);
+  auto it = b.tuned.find(key);
+  std::vector<Variant> cands;
+  for (int J : {8, 4})
+    for (bool wide : {true, false}) {
+      Variant v;
+      if (make_variant<NC, WPROJ>(W, J, wide, v) && finish_variant<NC, WPROJ, COMP>(v)) cands.push_back(v);
+    }
+  if (cands.empty()) {
+    bz_record_error(BZ_ERR_UNSUPPORTED, "batched: no layout for support class %d", W);
+    return false;
+  }
+  if (it != b.tuned.end()) {
+    for (auto &v : cands)
+      if (v.J == it->second.first && (int)v.wide == it->second.second) { out = v; return true; }
+  }
+  if (cands.size() == 1 || host_count == 0) {
+    out = cands[0];
+    b.tuned[key] = {out.J, (int)out.wide};
+    return true;
+  }
+  // sample: up to 512 segments of the class, into the scratch grid (no effect on results)
+  const int sample = std::min(host_count, 512);
+  BZ_CUDA_TRY_RET(cudaMemcpy(b.sample_count.ptr + k, &sample, sizeof(int), cudaMemcpyHostToDevice), false);
+  GridArgs a = base;
+  a.grid = c.scratch.ptr;
+  a.grid_lo = COMP ? c.scratch.ptr : nullptr;
+  a.norm = nullptr;
+  float best = 1e30f;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  for (auto &v : cands) {
+    if (!launch_class<NC, WPROJ, COMP>(a, k, v, nfacets, b.sample_count.ptr + k, b.work_next.ptr + k, c.stream)) break;
+    cudaEventRecord(e0, c.stream);
+    launch_class<NC, WPROJ, COMP>(a, k, v, nfacets, b.sample_count.ptr + k, b.work_next.ptr + k, c.stream);
+    cudaEventRecord(e1, c.stream);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) {
+      best = ms;
+      out = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  BZ_CUDA_TRY_RET(cudaMemsetAsync(c.scratch.ptr, 0, sizeof(vis_complex) * c.scratch.n, c.stream), false);
+  b.tuned[key] = {out.J, (int)out.wide};
+  return bz_error_code() == BZ_OK;
+}
+
+template <int NC, bool WPROJ, bool COMP>
+bool tune_all(const GridArgs &base, int nfacets, bool sampling, const std::vector<int> &counts) {
+  for (int k = 0; k < g_bs.ncls; ++k) {
+    Variant &v = sampling ? g_bs.cls[k].sf : g_bs.cls[k].vis;
+    if (!tune_class<NC, WPROJ, COMP>(base, k, nfacets, v, counts[k])) return false;
+  }
+  return true;
+}
+
+template <int NC, bool WPROJ, bool COMP>
+bool launch_all(const GridArgs &base, int nfacets, bool sampling, cudaStream_t st) {
+  for (int k = 0; k < g_bs.ncls; ++k) {
+    const Variant &v = sampling ? g_bs.cls[k].sf : g_bs.cls[k].vis;
+    if (!launch_class<NC, WPROJ, COMP>(base, k, v, nfacets, g_bs.class_count.ptr + k,
+                                       g_bs.work_next.ptr + (sampling ? kMaxClasses : 0) + k, st))
+      return false;
+  }
+  return true;
+}
+
+template <bool WPROJ, bool COMP>
+bool dispatch(const GridArgs &va, const GridArgs *sa, int nfacets, bool tune, const std::vector<int> &counts,
+              cudaStream_t st) {
+  if (tune) {
+    if (!tune_all<4, WPROJ, COMP>(va, nfacets, false, counts)) return false;
+    if (sa && !tune_all<1, WPROJ, COMP>(*sa, 1, true, counts)) return false;
+    return true;
+  }
+  if (!launch_all<4, WPROJ, COMP>(va, nfacets, false, st)) return false;
+  if (sa && !launch_all<1, WPROJ, COMP>(*sa, 1, true, st)) return false;
+  return true;
+}
+
+bool run_dispatch(const GridArgs &va, const GridArgs *sa, bool wproj, bool comp, bool tune, const std::vector<int> &counts,
+                  cudaStream_t st) {
+  const int F = (int)g_ctx.F;
+#if defined(BULLSEYE_SINGLE)
+  if (comp) return wproj ? dispatch<true, true>(va, sa, F, tune, counts, st) : dispatch<false, true>(va, sa, F, tune, counts, st);
+#else
+  (void)comp;
+#endif
+  return wproj ? dispatch<true, false>(va, sa, F, tune, counts, st) : dispatch<false, false>(va, sa, F, tune, counts, st);
+}
+
+// The schedule-building kernels (everything before the per-class launches).
+bool enqueue_schedule(const GridArgs &va, cudaStream_t st) {
+  Context &c = g_ctx;
+  BatchedState &b = g_bs;
+  const long long R = va.nrows;
+  const int tracks = va.nslots * va.nchan;
+  BZ_CUDA_TRY_RET(cudaMemsetAsync(b.class_count.ptr, 0, sizeof(int) * kMaxClasses, st), false);
+  classify_kernel<<<1024, 256, 0, st>>>(va.uvw, va.spw, c.wavelengths.ptr, va.nchan, va.nspw, R, va.wmax, va.P,
+                                        b.plane_class.ptr, b.row_class.ptr);
+  seg_count_kernel<<<(tracks + 127) / 128, 128, 0, st>>>(va.starts, va.nslots, va.seg, R, va.nchan, b.row_class.ptr,
+                                                         b.nseg.ptr);
+  scan_kernel<<<1, 1024, 0, st>>>(b.nseg.ptr, b.seg_off.ptr, tracks, b.seg_total.ptr);
+  seg_write_kernel<<<(tracks + 127) / 128, 128, 0, st>>>(va.starts, va.nslots, va.seg, R, va.nchan, b.row_class.ptr,
+                                                         b.seg_off.ptr, b.segs.ptr, b.class_count.ptr);
+  class_offsets_kernel<<<1, 1, 0, st>>>(b.class_count.ptr, b.class_off.ptr, b.class_cursor.ptr, b.ncls);
+  bucket_kernel<<<1024, 256, 0, st>>>(b.segs.ptr, b.seg_total.ptr, b.sorted.ptr, b.class_cursor.ptr, b.class_off.ptr);
+  c.launches += 6;
+  BZ_CUDA_TRY_RET(cudaGetLastError(), false);
+  return true;
+}
+
+}  // namespace
+
+void bz_release_batched() {
+  BatchedState &b = g_bs;
+  if (b.exec) cudaGraphExecDestroy(b.exec);
+  b.exec = nullptr;
+  b.key.clear();
+  b.plane_class.release(); b.plane_lo.release(); b.row_class.release(); b.nseg.release(); b.seg_off.release();
+  b.seg_total.release(); b.class_count.release(); b.class_off.release(); b.class_cursor.release();
+  b.work_next.release(); b.sample_count.release(); b.segs.release(); b.sorted.release();
+  b.rows_cap = b.tracks_cap = b.segs_cap = 0;
+  b.planned = false;
+  b.ncls = 0;
+}
+
+// See include/bullseye_gb300.h.
+extern "C" int bullseye_grid_batched(gridding_parameters *pp, int call, int with_sampling) {
+  if (!bz_check_ready("bullseye_grid_batched")) return bz_error_code() ? bz_error_code() : BZ_ERR_NOT_INITIALISED;
+  gridding_parameters &p = *pp;
+  Context &c = g_ctx;
+  BatchedState &b = g_bs;
+  int mode;
+  bool faceting;
+  switch (call) {
+    case 0: mode = CORR_QUAD_JONES; faceting = true; break;   // facet_4_cor_corrections
+    case 1: mode = CORR_QUAD; faceting = true; break;         // facet_4_cor
+    case 2: mode = CORR_QUAD; faceting = false; break;        // grid_4_cor
+    default:
+      bz_record_error(BZ_ERR_INVALID_ARGUMENT, "bullseye_grid_batched: unknown call %d", call);
+      return BZ_ERR_INVALID_ARGUMENT;
+  }
+  if (c.C != 4) {
+    bz_record_error(BZ_ERR_UNSUPPORTED, "bullseye_grid_batched grids 4 correlations");
+    return BZ_ERR_UNSUPPORTED;
+  }
+  const bool sf = with_sampling && c.want_sf;
+  bz_timer_start();
+  GridArgs va, sa;
+  int nslots = 0, nslots_sf = 0;
+  if (!bz_prepare_grid_args(p, 4, mode, faceting, va, nslots, "bullseye_grid_batched")) return bz_error_code();
+  if (sf && !bz_prepare_grid_args(p, 1, CORR_SAMPLING, faceting, sa, nslots_sf, "bullseye_grid_batched")) return bz_error_code();
+  if (p.row_count == 0) {
+    bz_timer_stop();
+    return BZ_OK;
+  }
+  if (!b.planned && !plan_classes()) return bz_error_code() ? bz_error_code() : BZ_ERR_CUDA;
+  if (!ensure_capacity(p.row_count, (size_t)nslots * c.nchan)) return bz_error_code();
+  const bool wproj = p.wplanes > 1;
+  const bool comp = va.grid_lo != nullptr;
+
+  // graph key: everything the captured launches read by value
+  std::vector<unsigned char> key(sizeof(GridArgs) * 2 + 8);
+  std::memcpy(key.data(), &va, sizeof(GridArgs));
+  if (sf) std::memcpy(key.data() + sizeof(GridArgs), &sa, sizeof(GridArgs));
+  key[sizeof(GridArgs) * 2] = (unsigned char)sf;
+  key[sizeof(GridArgs) * 2 + 1] = (unsigned char)comp;
+
+  if (!b.exec || key != b.key) {
+    // first run of this configuration: build the schedule eagerly, tune each class, then capture
+    if (!enqueue_schedule(va, c.stream)) return bz_error_code();
+    std::vector<int> counts(kMaxClasses, 0);
+    BZ_CUDA_TRY_RET(cudaMemcpyAsync(counts.data(), b.class_count.ptr, sizeof(int) * kMaxClasses, cudaMemcpyDeviceToHost,
+                                    c.stream), BZ_ERR_CUDA);
+    BZ_CUDA_TRY_RET(cudaStreamSynchronize(c.stream), BZ_ERR_CUDA);
+    if (!run_dispatch(va, sf ? &sa : nullptr, wproj, comp, true, counts, c.stream)) return bz_error_code();
+    if (b.exec) cudaGraphExecDestroy(b.exec);
+    b.exec = nullptr;
+    cudaGraph_t graph;
+    BZ_CUDA_TRY_RET(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal), BZ_ERR_CUDA);
+    const long long launches0 = c.launches;
+    bool ok = enqueue_schedule(va, c.stream) && run_dispatch(va, sf ? &sa : nullptr, wproj, comp, false, counts, c.stream);
+    cudaError_t ce = cudaStreamEndCapture(c.stream, &graph);
+    if (!ok || ce != cudaSuccess) {
+      bz_record_error(BZ_ERR_CUDA, "bullseye_grid_batched: graph capture failed (%s)", cudaGetErrorString(ce));
+      return BZ_ERR_CUDA;
+    }
+    c.launches = launches0;  // counted again when the graph is launched
+    ce = cudaGraphInstantiate(&b.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) {
+      bz_record_error(BZ_ERR_CUDA, "bullseye_grid_batched: graph instantiation failed (%s)", cudaGetErrorString(ce));
+      return BZ_ERR_CUDA;
+    }
+    b.key = key;
+  }
+  BZ_CUDA_TRY_RET(cudaGraphLaunch(b.exec, c.stream), BZ_ERR_CUDA);
+  c.launches += 6 + (long long)b.ncls * (sf ? 2 : 1);
+  if (p.is_final_data_chunk) {
+    bz_copy_back_grids(p, false);
+    if (sf) bz_copy_back_grids(p, true);
+  }
+  bz_timer_stop();
+  return bz_error_code();
+}

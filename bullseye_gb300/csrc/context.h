@@ -1,0 +1,97 @@
+// Library context of the GB300 imaging library (shared by its translation units).
+#pragma once
+#include <cstring>
+#include <vector>
+
+#include "common.h"
+#include "gridder.cuh"
+
+using bz::FacetXform;
+using bz::GridArgs;
+
+// ------------------------------------------------------------------ device buffer helper
+template <typename T>
+struct DevBuf {
+  T *ptr = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  bool alloc(size_t count) {
+    release();
+    if (count == 0) count = 1;
+    if (cudaMalloc((void **)&ptr, sizeof(T) * count) != cudaSuccess) {
+      ptr = nullptr;
+      bz_record_error(BZ_ERR_CUDA, "cudaMalloc of %zu bytes failed", sizeof(T) * count);
+      return false;
+    }
+    n = count;
+    return true;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    n = 0;
+  }
+};
+
+// ------------------------------------------------------------------ library context
+struct Context {
+  bool initialized = false;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev_g0 = nullptr, ev_g1 = nullptr, ev_i0 = nullptr, ev_i1 = nullptr;
+  bool grid_timing_pending = false, inv_timing_pending = false;
+  double grid_seconds = 0.0, inv_seconds = 0.0;
+  bool compensated = true;  // FP32: compensated (hi/lo) grid accumulation
+  bool device_inputs = false;  // row arrays, Jones terms and baseline starts are device pointers
+  long long launches = 0;      // kernels launched by this library since initLibrary
+  cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;  // around the last gridder launch
+  bool kernel_timing_pending = false;
+  int kernel_timing_kind = 0;  // 0 visibilities, 1 sampling function
+  double kernel_ms[2] = {0.0, 0.0};  // accumulated gridder kernel time (ms) per kind
+  long long kernel_count[2] = {0, 0};
+
+  // sizes fixed at init
+  size_t F = 1, cube = 1, C = 1, nx = 0, ny = 0, sf_count = 0, W = 1, os = 1, K = 1, P = 1;
+  size_t nchan = 1, nspw = 1, npol = 1, max_rows = 0, baselines = 0;
+  bool want_sf = false;
+
+  // device tables
+  DevBuf<vis_real> conv, wavelengths, facet_centres;
+  std::vector<vis_real> conv_host;  // host copy of the kernel table (support windows)
+  DevBuf<uint8_t> enabled;
+  DevBuf<size_t> cgi, sf_cgi;
+  // device row buffers (chunk_max_row_count rows)
+  DevBuf<vis_complex> vis;
+  DevBuf<vis_real> weights, uvw;
+  DevBuf<uint8_t> flags, flagged_rows;
+  DevBuf<unsigned> field, spw, ant1, ant2;
+  DevBuf<size_t> time_ids, starts;
+  DevBuf<vis_complex> jones_raw, jones_inv;
+  DevBuf<FacetXform> facets, facets_sf;
+  // grids
+  // sf holds the caller's initial sampling grids [facets][sf][ny][nx]; every facet receives the
+  // same sampling-function contribution (the phase policy of the sampling function reports the
+  // phase centre as facet centre, phase_transform_policies.h:77-82, so the uv transform is the
+  // identity), which is gridded once into sf_acc/sf_lo [sf][ny][nx] and added to every facet.
+  DevBuf<vis_complex> grid, grid_lo, sf, sf_acc, sf_lo, scratch;
+  DevBuf<double> norm;
+  DevBuf<int> dev_error;
+  std::vector<double> host_norm;  // published through params.normalization_terms
+  // gridding correction (detaper) factors for finalize, optional
+  DevBuf<double> corr_x, corr_y;
+  bool have_corr = false;
+};
+
+
+extern Context g_ctx;
+
+// helpers defined in imaging_lib.cu
+bool bz_check_ready(const char *fn);
+void bz_copy_back_grids(gridding_parameters &p, bool sampling);
+void bz_timer_start();
+void bz_timer_stop();
+bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool faceting, GridArgs &a,
+                          int &nslots, const char *name);

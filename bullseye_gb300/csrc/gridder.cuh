@@ -95,10 +95,16 @@ struct GridArgs {
   int nfacets_total;             // ABI num_facet_centres (Jones indexing)
   int groups;                    // cube channels (or sampling-function channels)
   int nx, ny, W, os, K, P;
+  int W_full;                    // the ABI's full support (visibility acceptance test); 0 means W
   int mode;                      // CorrMode
   int phase, uvx;                // faceting phase rotation / planar uv transform
   int nslots, seg;               // track slots (baselines or fixed segments), segment length
   int V;                         // visibilities staged per chunk
+  const int *plane_lo;           // per w plane: first tap of its nonzero window (support-aware), or null
+  const int4 *segments;          // persistent mode: {row_begin, row_end, channel, -} per segment, or null
+  const int *work_count;         // persistent mode: number of segments of this launch (device)
+  const int *segment_base;       // persistent mode: index of this launch's first segment (device)
+  int *work_next;                // persistent mode: work-item counter (device, zeroed before launch)
   unsigned imaging_field;
   double u_scale, v_scale, gcx, gcy, wmax;
 };
@@ -400,12 +406,22 @@ __device__ __forceinline__ void prologue(const GridArgs &a, int f_local, int cha
     double pl = rint(fabs(w) * plane_scale);
     plane = (pl >= 0.0 && pl < (double)a.P) ? (long long)pl : -1;  // NaN and out of range -> dropped
   }
-  if (!(du_d >= 0.0 && dv_d >= 0.0 && du_d + (a.W + 2) < (double)a.nx && dv_d + (a.W + 2) < (double)a.ny &&
+  const int Wf = a.W_full ? a.W_full : a.W;  // acceptance uses the full support, as the reference
+  if (!(du_d >= 0.0 && dv_d >= 0.0 && du_d + (Wf + 2) < (double)a.nx && dv_d + (Wf + 2) < (double)a.ny &&
         plane >= 0 && plane < a.P))
     return;
   int du = (int)du_d, dv = (int)dv_d;
   rec.fu = (int)((1.0 - u + ru_) * (double)a.os);
   rec.fv = (int)((1.0 - v + rv_) * (double)a.os);
+  if (a.plane_lo) {
+    // support-aware: grid only the plane's nonzero window of a.W taps (the taps outside it are
+    // exactly zero), shifting the footprint corner and the tap offsets by the window start
+    const int lo = a.plane_lo[plane];
+    du += lo;
+    dv += lo;
+    rec.fu += lo * a.os;
+    rec.fv += lo * a.os;
+  }
   rec.plane = (int)plane;
   rec.u0 = du;
   rec.v0 = dv;
@@ -478,7 +494,8 @@ __device__ __forceinline__ void owner_map(int tid, int W, int J, int &du, int &s
 }
 
 template <int NC, bool WPROJ, int J, bool COMP, bool WIDE>
-__global__ void __launch_bounds__(512, 1) romein_grid_kernel(const GridArgs a) {
+__device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local, const int chan, long long r0,
+                                           long long r1) {
   typedef typename TapT<WPROJ>::type tap_t;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   VisRec<NC> *recs = reinterpret_cast<VisRec<NC> *>(smem_raw);
@@ -500,19 +517,6 @@ __global__ void __launch_bounds__(512, 1) romein_grid_kernel(const GridArgs a) {
 
   const int W = a.W;
   const long long nxy = (long long)a.nx * a.ny;
-  long long track = blockIdx.x;
-  const int chan = (int)(track % a.nchan);
-  track /= a.nchan;
-  const int slot = (int)(track % a.nslots);
-  const int f_local = (int)(track / a.nslots);
-  long long r0, r1;
-  if (a.starts) {
-    r0 = (long long)a.starts[slot];
-    r1 = (long long)a.starts[slot + 1];
-  } else {
-    r0 = (long long)slot * a.seg;
-    r1 = min(a.nrows, r0 + a.seg);
-  }
   if (r1 > a.nrows) r1 = a.nrows;
   if (r0 >= r1) return;
 
@@ -726,6 +730,48 @@ __global__ void __launch_bounds__(512, 1) romein_grid_kernel(const GridArgs a) {
     __syncthreads();
     if (all_uniform && tid < NC && gmax >= 0 && s_norm[tid] != 0.0)
       atomicAdd(&a.norm[(fslice + gmax) * NC + tid], s_norm[tid]);
+  }
+}
+
+// One CTA per track: blockIdx -> (facet, baseline slot or row segment, channel).
+template <int NC, bool WPROJ, int J, bool COMP, bool WIDE>
+__global__ void __launch_bounds__(512, 1) romein_grid_kernel(const GridArgs a) {
+  long long track = blockIdx.x;
+  const int chan = (int)(track % a.nchan);
+  track /= a.nchan;
+  const int slot = (int)(track % a.nslots);
+  const int f_local = (int)(track / a.nslots);
+  long long r0, r1;
+  if (a.starts) {
+    r0 = (long long)a.starts[slot];
+    r1 = (long long)a.starts[slot + 1];
+  } else {
+    r0 = (long long)slot * a.seg;
+    r1 = min(a.nrows, r0 + a.seg);
+  }
+  grid_track<NC, WPROJ, J, COMP, WIDE>(a, f_local, chan, r0, r1);
+}
+
+// Persistent form: a fixed grid of CTAs takes (segment, facet) work items from a device counter
+// until the device-side item count is exhausted; every segment is a run of one track's rows
+// whose w planes share this launch's support class (a.W).  Items of one segment are adjacent, so
+// the facets of a segment are gridded while its rows are hot in L2.  The loop ends on the count,
+// never waits on other CTAs.
+template <int NC, bool WPROJ, int J, bool COMP, bool WIDE>
+__global__ void __launch_bounds__(512, 1) romein_segment_kernel(const GridArgs a, const int nfacets) {
+  __shared__ int s_item;
+  const int count = *a.work_count;
+  const long long total = (long long)count * nfacets;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_item = atomicAdd(a.work_next, 1);
+    __syncthreads();
+    const long long item = s_item;
+    if (item >= total) break;
+    const int seg = (int)(item / nfacets);
+    const int f_local = (int)(item - (long long)seg * nfacets);
+    const int4 sg = a.segments[*a.segment_base + seg];
+    grid_track<NC, WPROJ, J, COMP, WIDE>(a, f_local, sg.z, sg.x, sg.y);
   }
 }
 

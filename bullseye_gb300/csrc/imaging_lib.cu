@@ -71,81 +71,10 @@ static void bz_clear_error() {
   g_err_msg.clear();
 }
 
-// ------------------------------------------------------------------ device buffer helper
-template <typename T>
-struct DevBuf {
-  T *ptr = nullptr;
-  size_t n = 0;
-  DevBuf() = default;
-  DevBuf(const DevBuf &) = delete;
-  DevBuf &operator=(const DevBuf &) = delete;
-  ~DevBuf() { release(); }
-  bool alloc(size_t count) {
-    release();
-    if (count == 0) count = 1;
-    if (cudaMalloc((void **)&ptr, sizeof(T) * count) != cudaSuccess) {
-      ptr = nullptr;
-      bz_record_error(BZ_ERR_CUDA, "cudaMalloc of %zu bytes failed", sizeof(T) * count);
-      return false;
-    }
-    n = count;
-    return true;
-  }
-  void release() {
-    if (ptr) cudaFree(ptr);
-    ptr = nullptr;
-    n = 0;
-  }
-};
+#include "context.h"
 
-// ------------------------------------------------------------------ library context
-struct Context {
-  bool initialized = false;
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev_g0 = nullptr, ev_g1 = nullptr, ev_i0 = nullptr, ev_i1 = nullptr;
-  bool grid_timing_pending = false, inv_timing_pending = false;
-  double grid_seconds = 0.0, inv_seconds = 0.0;
-  bool compensated = true;  // FP32: compensated (hi/lo) grid accumulation
-  bool device_inputs = false;  // row arrays, Jones terms and baseline starts are device pointers
-  long long launches = 0;      // kernels launched by this library since initLibrary
-  cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;  // around the last gridder launch
-  bool kernel_timing_pending = false;
-  int kernel_timing_kind = 0;  // 0 visibilities, 1 sampling function
-  double kernel_ms[2] = {0.0, 0.0};  // accumulated gridder kernel time (ms) per kind
-  long long kernel_count[2] = {0, 0};
-
-  // sizes fixed at init
-  size_t F = 1, cube = 1, C = 1, nx = 0, ny = 0, sf_count = 0, W = 1, os = 1, K = 1, P = 1;
-  size_t nchan = 1, nspw = 1, npol = 1, max_rows = 0, baselines = 0;
-  bool want_sf = false;
-
-  // device tables
-  DevBuf<vis_real> conv, wavelengths, facet_centres;
-  DevBuf<uint8_t> enabled;
-  DevBuf<size_t> cgi, sf_cgi;
-  // device row buffers (chunk_max_row_count rows)
-  DevBuf<vis_complex> vis;
-  DevBuf<vis_real> weights, uvw;
-  DevBuf<uint8_t> flags, flagged_rows;
-  DevBuf<unsigned> field, spw, ant1, ant2;
-  DevBuf<size_t> time_ids, starts;
-  DevBuf<vis_complex> jones_raw, jones_inv;
-  DevBuf<FacetXform> facets;
-  // grids
-  // sf holds the caller's initial sampling grids [facets][sf][ny][nx]; every facet receives the
-  // same sampling-function contribution (the phase policy of the sampling function reports the
-  // phase centre as facet centre, phase_transform_policies.h:77-82, so the uv transform is the
-  // identity), which is gridded once into sf_acc/sf_lo [sf][ny][nx] and added to every facet.
-  DevBuf<vis_complex> grid, grid_lo, sf, sf_acc, sf_lo, scratch;
-  DevBuf<double> norm;
-  DevBuf<int> dev_error;
-  std::vector<double> host_norm;  // published through params.normalization_terms
-  // gridding correction (detaper) factors for finalize, optional
-  DevBuf<double> corr_x, corr_y;
-  bool have_corr = false;
-};
-static Context g_ctx;
+Context g_ctx;
+void bz_release_batched();
 
 static bool check_ready(const char *fn) {
   if (!g_ctx.initialized) {
@@ -361,6 +290,7 @@ extern "C" void initLibrary(gridding_parameters *pp) {
             c.dev_error.alloc(1) && c.norm.alloc(c.F * c.cube * c.C);
   if (!ok) return;
   BZ_CUDA_TRY(cudaMemcpy(c.conv.ptr, p.conv, sizeof(vis_real) * conv_elems, cudaMemcpyHostToDevice));
+  c.conv_host.assign(p.conv, p.conv + conv_elems);
   BZ_CUDA_TRY(cudaMemcpy(c.wavelengths.ptr, p.reference_wavelengths, sizeof(vis_real) * sc, cudaMemcpyHostToDevice));
   BZ_CUDA_TRY(cudaMemcpy(c.enabled.ptr, p.enabled_channels, sc, cudaMemcpyHostToDevice));
   BZ_CUDA_TRY(cudaMemcpy(c.cgi.ptr, p.channel_grid_indicies, sizeof(size_t) * sc, cudaMemcpyHostToDevice));
@@ -414,7 +344,7 @@ extern "C" void releaseLibrary() {
   c.cgi.release(); c.sf_cgi.release(); c.vis.release(); c.weights.release(); c.uvw.release();
   c.flags.release(); c.flagged_rows.release(); c.field.release(); c.spw.release(); c.ant1.release();
   c.ant2.release(); c.time_ids.release(); c.starts.release(); c.jones_raw.release(); c.jones_inv.release();
-  c.facets.release(); c.grid.release(); c.grid_lo.release(); c.sf.release(); c.sf_acc.release(); c.sf_lo.release();
+  c.facets.release(); c.facets_sf.release(); c.grid.release(); c.grid_lo.release(); c.sf.release(); c.sf_acc.release(); c.sf_lo.release();
   c.scratch.release(); c.norm.release(); c.dev_error.release(); c.corr_x.release(); c.corr_y.release();
   if (c.ev_g0) cudaEventDestroy(c.ev_g0);
   if (c.ev_g1) cudaEventDestroy(c.ev_g1);
@@ -427,6 +357,8 @@ extern "C" void releaseLibrary() {
   c.stream = nullptr;
   c.host_norm.clear();
   c.host_norm.shrink_to_fit();
+  c.conv_host.clear();
+  bz_release_batched();
   c.initialized = false;
 }
 
@@ -676,6 +608,8 @@ static bool setup_tracks(const gridding_parameters &p, int &nslots, int &seg, co
   return true;
 }
 
+bool bz_check_ready(const char *fn) { return check_ready(fn); }
+void bz_copy_back_grids(gridding_parameters &p, bool sampling);
 static void copy_back_grids(gridding_parameters &p, bool sampling) {
   Context &c = g_ctx;
   const size_t nxy = c.nx * c.ny;
@@ -703,50 +637,50 @@ static void copy_back_grids(gridding_parameters &p, bool sampling) {
   }
 }
 
-static void grid_common(gridding_parameters *pp, int nc, int mode, bool faceting, const char *name) {
-  gridding_parameters &p = *pp;
-  if (!check_ready(name)) return;
+// Validation, uploads, Jones inversion, track setup and the per-facet transforms of one gridding
+// call; fills the kernel arguments.  Shared by the per-call and the batched paths.
+bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool faceting, GridArgs &a, int &nslots,
+                          const char *name) {
   Context &c = g_ctx;
   const bool sampling = mode == CORR_SAMPLING;
   if (sampling && !c.want_sf) {
     bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: library initialised without should_grid_sampling_function", name);
-    return;
+    return false;
   }
   if (!sampling && (size_t)nc != c.C) {
     bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s grids %d correlations but the library was initialised for %zu", name, nc, c.C);
-    return;
+    return false;
   }
   if (nc == 4 && !sampling && c.npol != 4) {
     bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s needs 4 polarisation terms per visibility", name);
-    return;
+    return false;
   }
   if (!sampling && (p.polarization_index >= c.npol || (nc == 2 && p.second_polarization_index >= c.npol))) {
     bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: polarization index out of range", name);
-    return;
+    return false;
   }
-  timer_start();
   const bool jones = mode == CORR_QUAD_JONES;
-  if (!upload_rows(p, jones, jones)) return;
+  if (!upload_rows(p, jones, jones)) return false;
   if (jones) {
     const size_t nj = p.no_timestamps_read * p.antenna_count * c.F * c.nspw * c.nchan;
     if (!p.jones_terms || nj == 0) {
       bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: jones_terms missing", name);
-      return;
+      return false;
     }
-    if (c.jones_inv.n < 4 * nj && !c.jones_inv.alloc(4 * nj)) return;
+    if (c.jones_inv.n < 4 * nj && !c.jones_inv.alloc(4 * nj)) return false;
     const vis_complex *jsrc = p.jones_terms;
     if (!c.device_inputs) {
-      if (c.jones_raw.n < 4 * nj && !c.jones_raw.alloc(4 * nj)) return;
-      BZ_CUDA_TRY(cudaMemcpyAsync(c.jones_raw.ptr, p.jones_terms, sizeof(vis_complex) * 4 * nj, cudaMemcpyHostToDevice, c.stream));
+      if (c.jones_raw.n < 4 * nj && !c.jones_raw.alloc(4 * nj)) return false;
+      BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.jones_raw.ptr, p.jones_terms, sizeof(vis_complex) * 4 * nj, cudaMemcpyHostToDevice, c.stream), false);
       jsrc = c.jones_raw.ptr;
     }
     invert_jones_kernel<<<(unsigned)((nj + 255) / 256), 256, 0, c.stream>>>(jsrc, c.jones_inv.ptr, (long long)nj,
                                                                              c.dev_error.ptr);
     c.launches++;
   }
-  int nslots = 0, seg = 0;
+  int seg = 0;
   const size_t *starts = nullptr;
-  if (!setup_tracks(p, nslots, seg, &starts)) return;
+  if (!setup_tracks(p, nslots, seg, &starts)) return false;
   // per-facet transforms (FP64, host)
   std::vector<FacetXform> fx(c.F);
   const double ra0 = (double)p.phase_centre_ra, dec0 = (double)p.phase_centre_dec;
@@ -761,9 +695,10 @@ static void grid_common(gridding_parameters *pp, int nc, int mode, bool faceting
     // (phase_transform_policies.h:77-82), so its uv transform is the identity
     fx[f] = facet_xform(ra0, dec0, ra, dec, phase, faceting);
   }
-  BZ_CUDA_TRY(cudaMemcpyAsync(c.facets.ptr, fx.data(), sizeof(FacetXform) * c.F, cudaMemcpyHostToDevice, c.stream));
+  DevBuf<FacetXform> &table = sampling ? c.facets_sf : c.facets;
+  if (table.n < c.F && !table.alloc(c.F)) return false;
+  BZ_CUDA_TRY_RET(cudaMemcpyAsync(table.ptr, fx.data(), sizeof(FacetXform) * c.F, cudaMemcpyHostToDevice, c.stream), false);
 
-  GridArgs a;
   std::memset(&a, 0, sizeof a);
   if (c.device_inputs) {
     a.vis = p.visibilities; a.weights = p.visibility_weights; a.flags = (const uint8_t *)p.flags;
@@ -780,7 +715,7 @@ static void grid_common(gridding_parameters *pp, int nc, int mode, bool faceting
   a.wavelengths = c.wavelengths.ptr; a.enabled = c.enabled.ptr;
   a.cgi = sampling ? c.sf_cgi.ptr : c.cgi.ptr;
   a.conv = c.conv.ptr;
-  a.facets = c.facets.ptr;
+  a.facets = table.ptr;
   a.grid = sampling ? c.sf_acc.ptr : c.grid.ptr;
   a.grid_lo = nullptr;
 #if defined(BULLSEYE_SINGLE)
@@ -795,6 +730,7 @@ static void grid_common(gridding_parameters *pp, int nc, int mode, bool faceting
   a.facet_base = 0; a.nfacets_total = (int)c.F;
   a.groups = (int)(sampling ? c.sf_count : c.cube);
   a.nx = (int)c.nx; a.ny = (int)c.ny; a.W = (int)c.W; a.os = (int)c.os; a.K = (int)c.K; a.P = (int)c.P;
+  a.W_full = (int)c.W;
   a.mode = mode; a.phase = phase ? 1 : 0; a.uvx = faceting ? 1 : 0;
   a.nslots = nslots; a.seg = seg;
   a.imaging_field = p.imaging_field;
@@ -804,6 +740,18 @@ static void grid_common(gridding_parameters *pp, int nc, int mode, bool faceting
   a.gcx = (double)(c.nx / 2 - p.conv_support);
   a.gcy = (double)(c.ny / 2 - p.conv_support);
   a.wmax = (double)(float)p.wmax_est;  // the reference divides by (float)wmax_est
+  return true;
+}
+
+static void grid_common(gridding_parameters *pp, int nc, int mode, bool faceting, const char *name) {
+  gridding_parameters &p = *pp;
+  if (!check_ready(name)) return;
+  Context &c = g_ctx;
+  const bool sampling = mode == CORR_SAMPLING;
+  timer_start();
+  GridArgs a;
+  int nslots = 0;
+  if (!bz_prepare_grid_args(p, nc, mode, faceting, a, nslots, name)) return;
   const int nc_launch = sampling ? 1 : nc;
   // the sampling function is identical for every facet: grid it once (facet 0)
   const long long blocks = (long long)(sampling ? 1 : c.F) * nslots * (long long)c.nchan;
@@ -833,6 +781,10 @@ extern "C" void grid_sampling_function(gridding_parameters *p) {
 extern "C" void facet_sampling_function(gridding_parameters *p) {
   grid_common(p, 1, CORR_SAMPLING, true, "facet_sampling_function");
 }
+
+void bz_copy_back_grids(gridding_parameters &p, bool sampling) { copy_back_grids(p, sampling); }
+void bz_timer_start() { timer_start(); }
+void bz_timer_stop() { timer_stop(); }
 
 // ---------------------------------------------------------------- host post-processing
 template <typename Fn>

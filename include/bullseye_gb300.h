@@ -99,6 +99,16 @@ void bullseye_zero_grids(void);
 /* Measured FP32 FMA throughput of the current GPU in TFLOP/s (roofline denominator). */
 double bullseye_fp32_fma_tflops(int iters);
 
+/* Batched, support-aware gridding of every facet of the current chunk: `call` 0 grids like
+ * facet_4_cor_corrections, 1 like facet_4_cor, 2 like grid_4_cor; with_sampling != 0 also grids
+ * the sampling function (like facet_/grid_sampling_function).  Same results as those calls: each
+ * visibility is gridded over its w plane's nonzero support window (read from the kernel table)
+ * instead of the padded W x W, by persistent per-support-class launches over (track run, facet)
+ * work items; the schedule is built on the device and the whole call is replayed as a CUDA graph
+ * after its first use (layouts per support class are picked by timing on that first use).
+ * Returns 0 or the error code (also reported by bullseye_last_error). */
+int bullseye_grid_batched(gridding_parameters *params, int call, int with_sampling);
+
 /* Allocation-free facet_4_cor_corrections, for callers that cannot allocate device memory while
  * they grid (a fixed device arena with no further cudaMalloc/cudaFree, or code where a device
  * allocation would synchronise or is not permitted).  No counterpart in the reference.
