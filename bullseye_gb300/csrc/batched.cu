@@ -178,11 +178,8 @@ bool make_variant(int W, int J, bool wide, Variant &v) {
   v.wide = wide;
   v.NT = std::max(32, ((owners + 31) / 32) * 32);
   if (v.NT > 512) return false;
-  const size_t budget = 160 * 1024;
-  const size_t per = sizeof(VisRec<NC>) + sizeof(double) * NC + 2 * sizeof(int) +
-                     sizeof(typename TapT<WPROJ>::type) * (2 * (size_t)W + kTvPad);
-  v.V = std::max(1, (int)std::min<size_t>(v.NT, (budget - 64) / per));
-  v.smem = grid_smem_bytes<NC, WPROJ>(v.V, W);
+  v.V = grid_chunk_size<NC, WPROJ>(W, v.NT);
+  v.smem = grid_smem_bytes<NC, WPROJ>(v.V, W, v.NT);
   return true;
 }
 
@@ -295,6 +292,7 @@ bool launch_class(const GridArgs &base, int k, const Variant &v, int nfacets, co
   a.plane_lo = g_bs.plane_lo.ptr;
   a.segments = g_bs.sorted.ptr;
   a.segment_base = g_bs.class_off.ptr + k;
+  a.segment_capacity = (long long)g_bs.segs_cap;
   a.work_count = count;
   a.work_next = next;
   auto kern = seg_kernel<NC, WPROJ, COMP>(v.J, v.wide);

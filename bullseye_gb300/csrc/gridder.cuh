@@ -34,6 +34,8 @@
 //    (templated_gridder.h:97 and store_normalization_term), computed per visibility as
 //    Re(sum_j k_u[j] * sum_i k_v[i]).
 #pragma once
+#include <algorithm>
+
 #include "common.h"
 
 namespace bz {
@@ -104,6 +106,7 @@ struct GridArgs {
   const int4 *segments;          // persistent mode: {row_begin, row_end, channel, -} per segment, or null
   const int *work_count;         // persistent mode: number of segments of this launch (device)
   const int *segment_base;       // persistent mode: index of this launch's first segment (device)
+  long long segment_capacity;    // persistent mode: entries in segments
   int *work_next;                // persistent mode: work-item counter (device, zeroed before launch)
   unsigned imaging_field;
   double u_scale, v_scale, gcx, gcy, wmax;
@@ -434,12 +437,14 @@ __device__ __forceinline__ void prologue(const GridArgs &a, int f_local, int cha
 }
 
 // Shared-memory bytes for a launch with V staged visibilities.
-// Per-warp flush queues (compensated single precision only), for up to 16 warps.
+// Per-warp flush queues (compensated single precision only): nwarps record arrays, then one
+// 16-byte counter slot per warp.
 template <int NC>
-__host__ __device__ inline size_t flush_queue_bytes() {
+__host__ __device__ inline size_t flush_queue_bytes(int nwarps) {
 #if defined(BULLSEYE_SINGLE)
-  return 16 * (sizeof(FlushRec<NC>) * kFlushQueueCap + 16);
+  return (size_t)nwarps * (sizeof(FlushRec<NC>) * kFlushQueueCap + 16);
 #else
+  (void)nwarps;
   return 0;
 #endif
 }
@@ -449,11 +454,25 @@ __host__ __device__ inline size_t flush_queue_bytes() {
 constexpr int kTvPad = 15;
 
 template <int NC, bool WPROJ>
-__host__ __device__ inline size_t grid_smem_bytes(int V, int W) {
+__host__ __device__ inline size_t grid_smem_bytes(int V, int W, int nthreads) {
   size_t recs = sizeof(VisRec<NC>) * (size_t)V;
   size_t norm = (sizeof(double) * NC + 2 * sizeof(int)) * (size_t)V;  // per-lane normalisation state
   size_t taps = sizeof(typename TapT<WPROJ>::type) * (size_t)V * (2 * W + kTvPad);
-  return recs + norm + taps + flush_queue_bytes<NC>() + 64;
+  return recs + norm + taps + flush_queue_bytes<NC>((nthreads + 31) / 32) + 64;
+}
+
+// Staged-chunk size V for a CTA of nthreads: one visibility per thread at most, and shared memory
+// small enough that the CTAs the register file allows (128 registers per thread) fit on an SM.
+template <int NC, bool WPROJ>
+__host__ inline int grid_chunk_size(int W, int nthreads) {
+  const int ctas = std::max(1, std::min(8, 65536 / (nthreads * 128)));
+  const size_t smem_sm = 227 * 1024;
+  size_t budget = std::min<size_t>(200 * 1024, smem_sm / ctas - 1024);
+  const size_t fixed = flush_queue_bytes<NC>((nthreads + 31) / 32) + 64;
+  budget = budget > fixed ? budget - fixed : 0;
+  const size_t per = sizeof(VisRec<NC>) + sizeof(double) * NC + 2 * sizeof(int) +
+                     sizeof(typename TapT<WPROJ>::type) * (2 * (size_t)W + kTvPad);
+  return std::max(1, (int)std::min<size_t>(nthreads, budget / per));
 }
 
 // premultiplied visibility times the column tap
@@ -508,9 +527,9 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
   // per-warp flush queues follow the taps
   unsigned char *qbase = reinterpret_cast<unsigned char *>(tv + a.V * TVS);
   qbase = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(qbase) + 15) & ~(uintptr_t)15);
-  const int warp_id = threadIdx.x >> 5;
+  const int warp_id = threadIdx.x >> 5, nwarps = (blockDim.x + 31) >> 5;
   FlushRec<NC> *fq = reinterpret_cast<FlushRec<NC> *>(qbase) + warp_id * kFlushQueueCap;
-  int *fqn = reinterpret_cast<int *>(qbase + 16 * sizeof(FlushRec<NC>) * kFlushQueueCap) + warp_id * 4;
+  int *fqn = reinterpret_cast<int *>(qbase + nwarps * sizeof(FlushRec<NC>) * kFlushQueueCap) + warp_id * 4;
   if (COMP && (threadIdx.x & 31) == 0) *fqn = 0;
   __shared__ int s_same_g;
   __shared__ double s_norm[NC];
@@ -770,7 +789,16 @@ __global__ void __launch_bounds__(512, 1) romein_segment_kernel(const GridArgs a
     if (item >= total) break;
     const int seg = (int)(item / nfacets);
     const int f_local = (int)(item - (long long)seg * nfacets);
-    const int4 sg = a.segments[*a.segment_base + seg];
+    const long long si = (long long)*a.segment_base + seg;
+    if (si < 0 || si >= a.segment_capacity) {  // schedule out of range: record and stop
+      if (threadIdx.x == 0) atomicOr(a.error, DEV_ERR_GRID_INDEX);
+      break;
+    }
+    const int4 sg = a.segments[si];
+    if (sg.x < 0 || sg.x > sg.y || (long long)sg.y > a.nrows || sg.z < 0 || sg.z >= a.nchan) {
+      if (threadIdx.x == 0) atomicOr(a.error, DEV_ERR_GRID_INDEX);
+      continue;
+    }
     grid_track<NC, WPROJ, J, COMP, WIDE>(a, f_local, sg.z, sg.x, sg.y);
   }
 }

@@ -467,12 +467,8 @@ static LaunchShape choose_shape(int W) {
   if (!s.J) s.J = 16;
   const int owners = s.wide ? cols * ((W + s.J - 1) / s.J) : W * ((W + s.J - 1) / s.J);
   s.NT = std::max(32, ((owners + 31) / 32) * 32);
-  const size_t budget = 160 * 1024;
-  const size_t per = sizeof(VisRec<NC>) + sizeof(double) * NC + 2 * sizeof(int) +
-                     sizeof(typename TapT<WPROJ>::type) * (2 * (size_t)W + kTvPad);
-  int V = (int)std::min<size_t>(s.NT, (budget - 64) / per);
-  s.V = std::max(1, V);
-  s.smem = grid_smem_bytes<NC, WPROJ>(s.V, W);
+  s.V = grid_chunk_size<NC, WPROJ>(W, s.NT);
+  s.smem = grid_smem_bytes<NC, WPROJ>(s.V, W, s.NT);
   return s;
 }
 
