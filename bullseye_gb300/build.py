@@ -1,7 +1,7 @@
 """Build the GB300 imaging libraries in-tree with nvcc (sm_103a only).
 
 Produces ``bullseye_gb300/lib/libgpu_imaging32.so`` and ``libgpu_imaging64.so`` from
-``bullseye_gb300/csrc/imaging_lib.cu``, compiled once per precision (``-DBULLSEYE_SINGLE`` /
+the ``.cu`` files under ``bullseye_gb300/csrc``, compiled once per precision (``-DBULLSEYE_SINGLE`` /
 ``-DBULLSEYE_DOUBLE``), the two compiles running in parallel.  Nothing is installed outside the
 repository.  The build is incremental: a library is rebuilt when any source under ``csrc`` is
 newer than it.
@@ -44,7 +44,7 @@ def _cmd(precision: str, out: str, verbose_ptxas: bool = False):
     cmd = [os.path.join(ch, "bin", "nvcc"), *ARCH, "-O3", "-lineinfo", "-std=c++17", macro, "--threads", "4",
            "-Xcompiler", "-fPIC", "-shared", "--expt-relaxed-constexpr",
            os.path.join(CSRC, "imaging_lib.cu"), os.path.join(CSRC, "noalloc.cu"),
-           os.path.join(CSRC, "batched.cu"), "-o", out,
+           os.path.join(CSRC, "batched.cu"), os.path.join(CSRC, "adjoint.cu"), "-o", out,
            "-L" + os.path.join(ch, "lib64"), "-lcufft",
            "-Xlinker", "-rpath," + os.path.join(ch, "lib64")]
     if verbose_ptxas:

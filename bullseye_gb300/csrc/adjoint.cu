@@ -1,0 +1,366 @@
+// Adjoint of facet gridding (a degridder): gradients of a real loss with respect to the
+// visibilities and the per-antenna 2x2 Jones terms, given the gradient with respect to the grids.
+//
+// Forward (per facet f, visibility (row, channel), correlation c, footprint cell (x, y)):
+//   M   = J_p^-1 V J_q^-H                       (Jones correction, 2x2)
+//   V'  = s M,  s = weight x flag x e^{i phi_f} (phase rotation to the facet centre)
+//   y   = V' (w >= 0) or conj(V') (w < 0, gridded at (-u, -v))
+//   G  += y tap(x - u0, y - v0)
+// With the real-inner-product convention dL = Re <g_z, dz> (torch's complex gradient):
+//   g_y  = sum over the footprint of g_G conj(tap)         (a gather: no atomics)
+//   g_V' = g_y or conj(g_y)
+//   g_M  = conj(s) g_V'
+//   g_V  = P^H g_M Q                                      (P = J_p^-1, Q = J_q^-1)
+//   g_Jp = -P^H g_M M^H,   g_Jq = -Q^H g_M^H M            (d(J^-1) = -J^-1 dJ J^-1)
+// Cells and taps are selected exactly as the gridder does (FP64 uvw, phase and cell selection,
+// floor for 1-D AA kernels, round-half-even for w-projection, full support W).  The normalisation
+// sums depend only on weights and taps, so they carry no gradient.
+//
+// One warp per (row, channel) loops over the facets: the lanes split the W x W footprint, the
+// partial sums are reduced with shuffles, lane 0 forms the gradients.  The visibility gradient
+// (summed over facets) is written once; Jones gradients are accumulated with atomics because
+// every antenna appears on many baselines.
+#include <cstring>
+
+#include "common.h"
+#include "gridder.cuh"
+
+using namespace bz;
+
+namespace {
+
+struct AdjointArgs {
+  const vis_complex *vis;
+  const vis_real *weights;
+  const uint8_t *flags;
+  const vis_real *uvw;
+  const uint8_t *flagged_rows;
+  const unsigned *field;
+  const unsigned *spw;
+  const unsigned *ant1, *ant2;
+  const size_t *time_ids;
+  const vis_complex *jones;  // raw terms [T][A][F][S][Ch][4], or null (no correction)
+  const vis_real *wavelengths;
+  const uint8_t *enabled;
+  const size_t *cgi;
+  const void *conv;
+  const vis_real *facet_centres;  // [F][2] arcsec, or null (no faceting)
+  const vis_complex *grad_grid;   // [F][cube][4][ny][nx]
+  vis_complex *grad_vis;          // [R][Ch][4]
+  vis_complex *grad_jones;        // like jones, accumulated; or null
+  long long nrows;
+  int nchan, nspw, nant, ntimes, nfacets, cube, nx, ny, W, os, K, P, faceting;
+  unsigned imaging_field;
+  double u_scale, v_scale, gcx, gcy, wmax, ra0, dec0;
+};
+
+__device__ __forceinline__ cplx cconj(cplx a) {
+  a.im = -a.im;
+  return a;
+}
+__device__ __forceinline__ cplx cadd(cplx a, cplx b) {
+  a.re += b.re;
+  a.im += b.im;
+  return a;
+}
+// 2x2 products with optional hermitian transposes: O = op(A) op(B)
+__device__ __forceinline__ void mat2(const cplx *A, bool ha, const cplx *B, bool hb, cplx *O) {
+  cplx a[4], b[4];
+  if (ha) { a[0] = cconj(A[0]); a[1] = cconj(A[2]); a[2] = cconj(A[1]); a[3] = cconj(A[3]); }
+  else { a[0] = A[0]; a[1] = A[1]; a[2] = A[2]; a[3] = A[3]; }
+  if (hb) { b[0] = cconj(B[0]); b[1] = cconj(B[2]); b[2] = cconj(B[1]); b[3] = cconj(B[3]); }
+  else { b[0] = B[0]; b[1] = B[1]; b[2] = B[2]; b[3] = B[3]; }
+  jmul(a, b, O);
+}
+
+__device__ __forceinline__ bool inv2(cplx *m) {
+  cplx det;
+  det.re = (m[0].re * m[3].re - m[0].im * m[3].im) - (m[1].re * m[2].re - m[1].im * m[2].im);
+  det.im = (m[0].re * m[3].im + m[0].im * m[3].re) - (m[1].re * m[2].im + m[1].im * m[2].re);
+  if (det.re == (acc_real)0 && det.im == (acc_real)0) return false;
+  const acc_real n2 = det.re * det.re + det.im * det.im;
+  cplx inv;
+  inv.re = det.re / n2;
+  inv.im = -det.im / n2;
+  cplx neg;
+  neg.re = -inv.re;
+  neg.im = -inv.im;
+  const cplx a0 = m[0];
+  m[0] = cmul(m[3], inv);
+  m[3] = cmul(a0, inv);
+  m[1] = cmul(m[1], neg);
+  m[2] = cmul(m[2], neg);
+  return true;
+}
+
+template <bool WPROJ>
+__device__ __forceinline__ cplx tap_at(const void *conv, long long idx) {
+  cplx t;
+  if (WPROJ) {
+    const vis_complex c = ((const vis_complex *)conv)[idx];
+    t.re = (acc_real)c.re;
+    t.im = (acc_real)c.im;
+  } else {
+    t.re = (acc_real)((const vis_real *)conv)[idx];
+    t.im = 0;
+  }
+  return t;
+}
+
+__device__ __forceinline__ void atomic_add_c(vis_complex *dst, cplx v) {
+  atomicAdd(&dst->re, (vis_real)v.re);
+  atomicAdd(&dst->im, (vis_real)v.im);
+}
+
+template <bool WPROJ>
+__global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  FacetXform *fx = reinterpret_cast<FacetXform *>(smem_raw);
+  for (int f = threadIdx.x; f < a.nfacets; f += blockDim.x) {
+    double ra = a.ra0, dec = a.dec0;
+    if (a.faceting && a.facet_centres) {
+      ra = (double)a.facet_centres[2 * f];
+      dec = (double)a.facet_centres[2 * f + 1];
+    }
+    // same constants as the gridder (phase_transform_policies.h:110-134, baseline_transform_policies.h:117-149)
+    const double k = (double)kArcsecToRad;
+    double d_ra = (ra - a.ra0) * k, n_dec = dec * k, o_dec = a.dec0 * k;
+    double c_d_ra = cos(d_ra), s_d_ra = sin(d_ra), c_n = cos(n_dec), s_n = sin(n_dec), c_o = cos(o_dec), s_o = sin(o_dec);
+    FacetXform x = {0, 0, 0, 0, 0};
+    if (a.faceting) {
+      double li0 = c_n * s_d_ra, mi0 = s_n * c_o - c_n * s_o * c_d_ra, ni0 = s_n * s_o + c_n * c_o * c_d_ra;
+      x.u_term = li0 / ni0;
+      x.v_term = mi0 / ni0;
+      x.dl = -c_n * s_d_ra;
+      x.dm = -(s_n * c_o - c_n * s_o * c_d_ra);
+      x.dn = 1.0 - sqrt(1.0 - x.dl * x.dl - x.dm * x.dm);
+    }
+    fx[f] = x;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  const int W = a.W;
+  const long long nxy = (long long)a.nx * a.ny;
+  const double plane_scale = WPROJ ? (double)(a.P - 1) / a.wmax : 0.0;
+
+  for (long long item = warp; item < a.nrows * a.nchan; item += nwarps) {
+    const long long row = item / a.nchan;
+    const int c = (int)(item - row * a.nchan);
+    const unsigned spw = a.spw[row];
+    if (spw >= (unsigned)a.nspw) continue;
+    const long long sc = (long long)spw * a.nchan + c;
+    if (!a.enabled[sc]) continue;
+    const size_t g = a.cgi[sc];
+    if (g >= (size_t)a.cube) continue;
+    const double inv = 1.0 / (double)a.wavelengths[sc];
+    const double u_l = (double)a.uvw[3 * row] * inv, v_l = (double)a.uvw[3 * row + 1] * inv,
+                 w_l = (double)a.uvw[3 * row + 2] * inv;
+    const bool row_ok = !a.flagged_rows[row] && a.field[row] == a.imaging_field;
+    const long long base = (row * a.nchan + c) * 4;
+    acc_real cw[4];
+    cplx V[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const bool keep = row_ok && !a.flags[base + k];
+      cw[k] = keep ? (acc_real)a.weights[base + k] : (acc_real)0;
+      V[k].re = a.vis[base + k].re;
+      V[k].im = a.vis[base + k].im;
+    }
+    cplx gV[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { gV[k].re = 0; gV[k].im = 0; }
+
+    for (int f = 0; f < a.nfacets; ++f) {
+      // Jones inverses of this row and facet
+      cplx Pm[4], Qm[4];
+      long long i1 = 0, i2 = 0;
+      bool jok = true;
+      if (a.jones) {
+        const long long t = (long long)a.time_ids[row];
+        const unsigned a1 = a.ant1[row], a2 = a.ant2[row];
+        if (t < 0 || t >= a.ntimes || a1 >= (unsigned)a.nant || a2 >= (unsigned)a.nant) continue;
+        i1 = ((((t * a.nant + a1) * a.nfacets + f) * a.nspw + spw) * a.nchan + c) * 4;
+        i2 = ((((t * a.nant + a2) * a.nfacets + f) * a.nspw + spw) * a.nchan + c) * 4;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          Pm[k].re = a.jones[i1 + k].re; Pm[k].im = a.jones[i1 + k].im;
+          Qm[k].re = a.jones[i2 + k].re; Qm[k].im = a.jones[i2 + k].im;
+        }
+        jok = inv2(Pm) && inv2(Qm);
+        if (!jok) continue;
+      }
+      // geometry, exactly as the gridder's prologue
+      const FacetXform x = fx[f];
+      cplx ph;
+      ph.re = 1;
+      ph.im = 0;
+      if (a.faceting) ph = phase_factor(6.283185307179586476925286766559 * (u_l * x.dl + v_l * x.dm + w_l * x.dn));
+      double u = u_l, v = v_l, w = w_l;
+      if (a.faceting) {
+        u = u - w * x.u_term;
+        v = v - w * x.v_term;
+      }
+      u *= a.u_scale;
+      v *= a.v_scale;
+      const bool flip = WPROJ && w < 0;
+      if (flip) { u = -u; v = -v; w = -w; }
+      const double ru_ = WPROJ ? rint(u) : floor(u);
+      const double rv_ = WPROJ ? rint(v) : floor(v);
+      const double du_d = WPROJ ? rint(u + a.gcx) : floor(u + a.gcx);
+      const double dv_d = WPROJ ? rint(v + a.gcy) : floor(v + a.gcy);
+      long long plane = 0;
+      if (WPROJ) {
+        const double pl = rint(fabs(w) * plane_scale);
+        plane = (pl >= 0.0 && pl < (double)a.P) ? (long long)pl : -1;
+      }
+      if (!(du_d >= 0.0 && dv_d >= 0.0 && du_d + (W + 2) < (double)a.nx && dv_d + (W + 2) < (double)a.ny &&
+            plane >= 0 && plane < a.P))
+        continue;
+      const int u0 = (int)du_d, v0 = (int)dv_d;
+      const long long fu = plane * a.K + (long long)((1.0 - u + ru_) * (double)a.os);
+      const long long fv = plane * a.K + (long long)((1.0 - v + rv_) * (double)a.os);
+      const long long slice0 = ((long long)f * a.cube + (long long)g) * 4;
+      // gather: D_k = sum over the footprint of g_G conj(tap)
+      cplx D[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) { D[k].re = 0; D[k].im = 0; }
+      for (int t = lane; t < W * W; t += 32) {
+        const int jv = t / W, ju = t - jv * W;
+        const cplx tap = cmul(tap_at<WPROJ>(a.conv, fu + (long long)ju * a.os), tap_at<WPROJ>(a.conv, fv + (long long)jv * a.os));
+        const cplx ct = cconj(tap);
+        const long long cell = (long long)(v0 + jv) * a.nx + (u0 + ju);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const vis_complex gg = a.grad_grid[(slice0 + k) * nxy + cell];
+          cplx gc;
+          gc.re = gg.re;
+          gc.im = gg.im;
+          D[k] = cadd(D[k], cmul(gc, ct));
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+          D[k].re += __shfl_xor_sync(0xffffffffu, D[k].re, off);
+          D[k].im += __shfl_xor_sync(0xffffffffu, D[k].im, off);
+        }
+      }
+      // chain rule back to V (and the Jones terms)
+      cplx gM[4];
+      const cplx cph = cconj(ph);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const cplx gvp = flip ? cconj(D[k]) : D[k];
+        cplx t = cmul(cph, gvp);
+        t.re *= cw[k];
+        t.im *= cw[k];
+        gM[k] = t;
+      }
+      if (a.jones) {
+        cplx T[4], G1[4];
+        mat2(Pm, true, gM, false, T);  // P^H gM
+        mat2(T, false, Qm, false, G1);  // (P^H gM) Q
+#pragma unroll
+        for (int k = 0; k < 4; ++k) gV[k] = cadd(gV[k], G1[k]);
+        if (a.grad_jones && lane == 0) {
+          cplx VQ[4], M[4], gp[4], gq[4];
+          mat2(V, false, Qm, true, VQ);  // V Q^H
+          mat2(Pm, false, VQ, false, M);  // M = P V Q^H
+          mat2(T, false, M, true, gp);    // P^H gM M^H
+          cplx T2[4];
+          mat2(Qm, true, gM, true, T2);   // Q^H gM^H
+          mat2(T2, false, M, false, gq);  // Q^H gM^H M
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            gp[k].re = -gp[k].re; gp[k].im = -gp[k].im;
+            gq[k].re = -gq[k].re; gq[k].im = -gq[k].im;
+            atomic_add_c(a.grad_jones + i1 + k, gp[k]);
+            atomic_add_c(a.grad_jones + i2 + k, gq[k]);
+          }
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) gV[k] = cadd(gV[k], gM[k]);
+      }
+    }
+    if (lane < 4) {
+      // every lane holds the same sums after the xor reductions; lane k writes correlation k
+      cplx mine = gV[0];
+      if (lane == 1) mine = gV[1];
+      if (lane == 2) mine = gV[2];
+      if (lane == 3) mine = gV[3];
+      vis_complex o;
+      o.re = (vis_real)mine.re;
+      o.im = (vis_real)mine.im;
+      a.grad_vis[base + lane] = o;
+    }
+  }
+}
+
+}  // namespace
+
+// See include/bullseye_gb300.h.  Every pointer is a device pointer (as for the allocation-free
+// gridding entry); jones_terms holds the raw (not inverted) terms or is null.
+extern "C" int bullseye_grid_adjoint(const gridding_parameters *params, const void *grad_grid, void *grad_vis,
+                                     void *grad_jones, int faceting, void *stream) {
+  if (!params || !grad_grid || !grad_vis) return BZ_ERR_INVALID_ARGUMENT;
+  const gridding_parameters &p = *params;
+  if (p.number_of_polarization_terms != 4 || p.number_of_polarization_terms_being_gridded != 4) return BZ_ERR_INVALID_ARGUMENT;
+  if (!p.visibilities || !p.uvw_coords || !p.visibility_weights || !p.flags || !p.flagged_rows || !p.field_array ||
+      !p.spw_index_array || !p.conv || !p.reference_wavelengths || !p.enabled_channels || !p.channel_grid_indicies)
+    return BZ_ERR_INVALID_ARGUMENT;
+  if (p.jones_terms && (!p.antenna_1_ids || !p.antenna_2_ids || !p.timestamp_ids)) return BZ_ERR_INVALID_ARGUMENT;
+  AdjointArgs a;
+  std::memset(&a, 0, sizeof a);
+  a.vis = p.visibilities; a.weights = p.visibility_weights; a.flags = (const uint8_t *)p.flags;
+  a.uvw = (const vis_real *)p.uvw_coords; a.flagged_rows = (const uint8_t *)p.flagged_rows;
+  a.field = p.field_array; a.spw = p.spw_index_array; a.ant1 = p.antenna_1_ids; a.ant2 = p.antenna_2_ids;
+  a.time_ids = p.timestamp_ids; a.jones = p.jones_terms;
+  a.wavelengths = p.reference_wavelengths; a.enabled = (const uint8_t *)p.enabled_channels; a.cgi = p.channel_grid_indicies;
+  a.conv = p.conv; a.facet_centres = p.facet_centres;
+  a.grad_grid = (const vis_complex *)grad_grid;
+  a.grad_vis = (vis_complex *)grad_vis;
+  a.grad_jones = p.jones_terms ? (vis_complex *)grad_jones : nullptr;
+  a.nrows = (long long)p.row_count;
+  a.nchan = (int)p.channel_count; a.nspw = (int)p.spw_count; a.nant = (int)p.antenna_count;
+  a.ntimes = (int)p.no_timestamps_read;
+  a.nfacets = (int)(p.num_facet_centres ? p.num_facet_centres : 1);
+  a.cube = (int)p.cube_channel_dim_size;
+  a.nx = (int)p.nx; a.ny = (int)p.ny;
+  a.W = (int)(2 * p.conv_support + 1);
+  a.os = (int)p.conv_oversample;
+  a.K = (a.W + 2) + (a.W + 1) * (a.os - 1);
+  a.P = (int)(p.wplanes > 1 ? p.wplanes : 1);
+  a.faceting = faceting ? 1 : 0;
+  a.imaging_field = p.imaging_field;
+  a.u_scale = (double)p.nx * (double)p.cell_size_x * (double)kArcsecToRad;
+  a.v_scale = -((double)p.ny * (double)p.cell_size_y * (double)kArcsecToRad);
+  a.gcx = (double)(p.nx / 2 - p.conv_support);
+  a.gcy = (double)(p.ny / 2 - p.conv_support);
+  a.wmax = (double)(float)p.wmax_est;
+  a.ra0 = (double)p.phase_centre_ra;
+  a.dec0 = (double)p.phase_centre_dec;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t smem = sizeof(FacetXform) * (size_t)a.nfacets;
+  if (smem > 200 * 1024) return BZ_ERR_UNSUPPORTED;
+  if (cudaMemsetAsync(grad_vis, 0, sizeof(vis_complex) * (size_t)a.nrows * a.nchan * 4, st) != cudaSuccess) return BZ_ERR_CUDA;
+  if (a.nrows == 0) return BZ_OK;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long warps_needed = a.nrows * a.nchan;
+  const long long blocks = std::min<long long>((warps_needed + 7) / 8, (long long)sms * 16);
+  if (p.wplanes > 1) {
+    if (smem > 48 * 1024 && cudaFuncSetAttribute(degrid_adjoint_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return BZ_ERR_CUDA;
+    degrid_adjoint_kernel<true><<<(unsigned)blocks, 256, smem, st>>>(a);
+  } else {
+    if (smem > 48 * 1024 && cudaFuncSetAttribute(degrid_adjoint_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return BZ_ERR_CUDA;
+    degrid_adjoint_kernel<false><<<(unsigned)blocks, 256, smem, st>>>(a);
+  }
+  return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}

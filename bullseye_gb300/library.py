@@ -45,6 +45,8 @@ EXTENSIONS = {
     "bullseye_fp32_fma_tflops": (ctypes.c_double, [ctypes.c_int]),
     "bullseye_facet_4_cor_corrections_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "bullseye_grid_batched": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "bullseye_grid_adjoint": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                             ctypes.c_int, ctypes.c_void_p]),
     "bullseye_reset_counters": (None, []),
     "bullseye_zero_grids": (None, []),
     "bullseye_set_gridding_correction": (None, [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t]),

@@ -127,6 +127,22 @@ int bullseye_grid_batched(gridding_parameters *params, int call, int with_sampli
  * stream capture on that device.  Returns 0 when queued. */
 int bullseye_facet_4_cor_corrections_noalloc(const gridding_parameters *params, void *stream);
 
+/* Adjoint of four-correlation gridding (a degridder): given grad_grid = dL/dG for the grids
+ * G [facets][cube][4][ny][nx] that facet_4_cor_corrections (jones_terms set, faceting != 0),
+ * facet_4_cor (jones_terms null, faceting != 0) or grid_4_cor (faceting == 0) produce from these
+ * inputs, writes grad_vis = dL/dV [rows][channels][4] and, when jones_terms and grad_jones are
+ * both set, ACCUMULATES dL/dJ into grad_jones [T][A][F][S][Ch][4] (zero it first).  Complex
+ * gradients follow the real-inner-product convention dL = Re sum conj(g) dz (PyTorch's).  Cells,
+ * taps, w planes, phase rotation and flags are selected exactly as the gridder selects them; the
+ * normalisation sums carry no gradient.  No counterpart in the reference (its only degridder is
+ * the prototype in writing_and_wiki/notebooks/Resampling.ipynb, cell 17: with unit weights, no
+ * faceting and grad_grid = the model grid, grad_vis divided by the tap sum is that degridder).
+ * Every pointer in *params and the three arrays are DEVICE pointers; jones_terms holds the raw
+ * (not inverted) terms.  Rows may be in any order.  Work is queued on `stream`; nothing is
+ * allocated.  Returns 0 when queued. */
+int bullseye_grid_adjoint(const gridding_parameters *params, const void *grad_grid, void *grad_vis,
+                          void *grad_jones, int faceting, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
