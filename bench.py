@@ -19,7 +19,13 @@ Lines printed (rank 0, one JSON line):
   roofline  the gridder kernel against the measured FP32 FMA rate of this GPU (the gridder is
             FP32-issue bound; HBM traffic is reported alongside);
   cpu_baseline  the oracle port of the reference CPU library (OpenMP over facets) on a bounded
-            sample of rows, on this machine's host cores.
+            sample of rows, on this machine's host cores;
+  precision the precision form: per-facet max / RMS relative dirty-image error of the FP32
+            library (compensated and plain flushes) against the FP64 library, config 3 (80 km,
+            4 facets of 4096^2).
+
+With N ranks (torchrun) each rank grids its own 16 facets of a 16 N-facet field (facet sharding,
+no collective on the data path); the step time is the max over ranks.
 
 --impl reference prints the reference arm: the oracle port of the reference's CPU path, timed on
 bounded row samples of the same workload, all host threads.
@@ -63,12 +69,16 @@ def parse():
                     help="batched: bullseye_grid_batched; plain: the per-call drop-in ABI path")
     ap.add_argument("--no-other", action="store_true", help="skip timing the other form")
     ap.add_argument("--facets", type=int, default=0, help="override the facet count (profiling cases)")
+    ap.add_argument("--no-precision", action="store_true", help="skip the per-facet FP32 error report")
     return ap.parse_args()
 
 
 # ----------------------------------------------------------------------------- workload
-def geometry(n_times):
+def geometry(n_times, world=1, rank=0):
+    """Rows, baseline order and facet centres.  With N ranks the field holds 16 N facets and each
+    rank grids its own 16 (facet sharding, no collective on the data path)."""
     from bullseye_gb300 import synth
+    from bullseye_gb300.sharding import facet_shard
     dec = np.deg2rad(-30.0)
     enu = synth.y_layout(N_ANT, 600.0, seed=2)
     xyz = synth.enu_to_equatorial(enu, np.deg2rad(34.0))
@@ -77,9 +87,11 @@ def geometry(n_times):
     lam = synth.C_LIGHT / freqs
     rng = np.random.default_rng(9)
     lim = np.deg2rad(3.0)
-    fl, fm = rng.uniform(-lim, lim, N_FACETS), rng.uniform(-lim, lim, N_FACETS)
+    fl, fm = rng.uniform(-lim, lim, N_FACETS * world), rng.uniform(-lim, lim, N_FACETS * world)
     dec0 = dec / synth.ARCSEC
     facets = np.stack([fl / np.cos(dec) / synth.ARCSEC, dec0 + fm / synth.ARCSEC], axis=1)
+    shard = facet_shard(N_FACETS * world, world, rank)
+    facets = facets[shard.start:shard.stop]
     # baseline-major order (what repack_input_data produces), stable in time
     from bullseye_gb300.imaging import baseline_index
     b = baseline_index(a1, a2, N_ANT)
@@ -346,6 +358,45 @@ def cpu_baseline(geo, conv1d, target_s):
                       f"available, one thread per facet), {dt:.1f} s"}
 
 
+# ----------------------------------------------------------------------------- precision form
+def precision_report():
+    """Dirty-image error of the FP32 library against the FP64 library, per facet (config 3).
+
+    The config-1 observation on an 80 km disc, 4 facets of 4096^2 (0.25 arcsec) at l offsets of
+    0, 0.5, 1 and 2 deg, facet_4_cor + normalize + finalize through the C-ABI.  Both libraries get
+    the same input values (the single-precision arrays, widened for the FP64 run), so the figures
+    are the arithmetic error of the FP32 path: compensated (the precision form) and plain FP32
+    flushes.  max_rel = max|I32 - I64| / max|I64|, rms_rel = rms(I32 - I64) / rms(I64), on the XX
+    image of each facet.
+    """
+    from bullseye_gb300 import synth
+    from bullseye_gb300.imaging import run_imaging
+    from bullseye_gb300.library import check, load_library
+    p32 = synth.config3("single")
+    p64 = p32.astype("double")
+    lib64 = load_library("GPU", "double")
+    ref = run_imaging(lib64, p64, "facet_4_cor", repack=True, do_finalize=True)
+    check(lib64)
+    lib32 = load_library("GPU", "single")
+    out = {"workload": "config-1 observation, 80 km disc, 4 facets 4096^2 at 0/0.5/1/2 deg, PSWF W=7 os=63, "
+                       "facet_4_cor, XX dirty image", "reference": "64-bit library on the same input values",
+           "rows": p32.rows}
+    for comp in (1, 0):
+        lib32.bullseye_set_compensated(comp)
+        res = run_imaging(lib32, p32, "facet_4_cor", repack=True, do_finalize=True)
+        check(lib32)
+        rows = []
+        for f in range(ref.image.shape[0]):
+            a = ref.image[f, 0].astype(np.float64)
+            b = res.image[f, 0].astype(np.float64)
+            d = b - a
+            rows.append({"max_rel": float(np.max(np.abs(d)) / np.max(np.abs(a))),
+                         "rms_rel": float(np.sqrt(np.mean(d * d)) / np.sqrt(np.mean(a * a)))})
+        out["fp32_compensated" if comp else "fp32_plain"] = rows
+    lib32.bullseye_set_compensated(1)
+    return out
+
+
 # ----------------------------------------------------------------------------- main
 def main():
     args = parse()
@@ -357,7 +408,7 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     n_times = max(8, int(N_TIMES * args.time_frac))
-    geo = geometry(n_times)
+    geo = geometry(n_times, world, rank)
     conv, supports = kernel_stack(geo["wmax"])
     R = geo["uvw"].shape[0]
     pairs_per_step = R * N_CHAN * N_FACETS
@@ -451,9 +502,9 @@ def main():
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        from bullseye_gb300.sharding import max_over_ranks
+        torch.distributed.barrier()
+        ms = max_over_ranks(ms, device="cuda")
     clk = clocks.stop()
     launches = int(lib.bullseye_kernel_launches())
     cnt = ctypes.c_longlong(0)
@@ -542,6 +593,9 @@ def main():
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         cpu = cpu_baseline(geo, conv, args.cpu_seconds)
+    precision = None
+    if not args.no_precision and rank == 0:
+        precision = precision_report()
 
     if rank == 0:
         line = {
@@ -563,7 +617,7 @@ def main():
                          "flops_per_pair": flops_per_pair, "hbm_gbs": hbm_gbs,
                          "hbm_frac_of_measured": hbm_gbs / peaks["hbm_gbs"] if peaks.get("hbm_gbs") else None,
                          "sampling_kernel_ms": sf_kernel_ms / max(1, cnt.value)},
-            "clocks": clk, "gpu_launches": launches, "e2e": e2e, "cpu_baseline": cpu,
+            "clocks": clk, "gpu_launches": launches, "e2e": e2e, "cpu_baseline": cpu, "precision": precision,
         }
         print(json.dumps(line))
 

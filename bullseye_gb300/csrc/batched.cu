@@ -283,6 +283,20 @@ bool ensure_capacity(size_t rows, size_t tracks) {
   return true;
 }
 
+// The dynamic shared-memory limit is an attribute of the kernel function that a graph launch reads
+// when it runs, not when it was captured, and support classes of different sizes can share one
+// instantiation: open each instantiation to the device's opt-in maximum instead of a class's size.
+template <typename Kern>
+bool open_smem(Kern kern) {
+  cudaFuncAttributes fa;
+  int dev = 0, optin = 0;
+  if (cudaFuncGetAttributes(&fa, kern) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+    return false;
+  return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes) ==
+         cudaSuccess;
+}
+
 template <int NC, bool WPROJ, bool COMP>
 bool launch_class(const GridArgs &base, int k, const Variant &v, int nfacets, const int *count, int *next,
                   cudaStream_t st) {
@@ -296,7 +310,7 @@ bool launch_class(const GridArgs &base, int k, const Variant &v, int nfacets, co
   a.work_count = count;
   a.work_next = next;
   auto kern = seg_kernel<NC, WPROJ, COMP>(v.J, v.wide);
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem) != cudaSuccess) {
+  if (!open_smem(kern)) {
     bz_record_error(BZ_ERR_CUDA, "batched: cudaFuncSetAttribute failed");
     return false;
   }
@@ -310,7 +324,7 @@ bool launch_class(const GridArgs &base, int k, const Variant &v, int nfacets, co
 template <int NC, bool WPROJ, bool COMP>
 bool finish_variant(Variant &v) {
   auto kern = seg_kernel<NC, WPROJ, COMP>(v.J, v.wide);
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem) != cudaSuccess) return false;
+  if (!open_smem(kern)) return false;
   int per_sm = 0, dev = 0, sms = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, v.NT, v.smem) != cudaSuccess || per_sm < 1) return false;
   cudaGetDevice(&dev);

@@ -188,6 +188,31 @@ def config2(precision="single", *, n_ant=27, n_times=2000, n_chan=64, n_facets=1
                     phase_centre=(0.0, dec0), facet_centres=facet_centres, jones=g)
 
 
+def config3(precision="single", *, n_ant=64, n_times=120, nx=4096, cell=0.25, s=3, os=63,
+            diameter_m=80000.0, facet_offsets_deg=(0.0, 0.5, 1.0, 2.0), seed=1, noise=0.01) -> GriddingProblem:
+    """Precision form: the config-1 observation (64 antennas, 120 timesteps at dec -30 deg, 1 channel
+    at 1.4 GHz, 3 point sources + noise, PSWF W = 7, os = 63) on an 80 km disc, imaged on 4096^2
+    facets of 0.25 arcsec cells (3.7e5 lambda baselines, all on the grid).  Facets sit at the phase
+    centre and at the given offsets in l (the phase-rotation argument grows with the offset)."""
+    dec = np.deg2rad(-30.0)
+    enu = disc_layout(n_ant, diameter_m, seed)
+    xyz = enu_to_equatorial(enu, np.deg2rad(-30.0))
+    uvw, a1, a2, tid = earth_rotation_rows(xyz, n_times, dec, np.deg2rad(90.0))
+    freqs = np.array([1.4e9])
+    rng = np.random.default_rng(seed + 7)
+    fov = nx * cell * ARCSEC
+    ls = rng.uniform(-0.3, 0.3, 3) * fov
+    ms = rng.uniform(-0.3, 0.3, 3) * fov
+    flux = rng.uniform(0.1, 2.0, 3)
+    vis_c = point_source_vis(uvw, C_LIGHT / freqs, ls, ms, flux)
+    conv = pswf_kernel(s, os)
+    dec0 = dec / ARCSEC
+    off = np.deg2rad(np.asarray(facet_offsets_deg, dtype=np.float64))
+    facet_centres = np.stack([off / np.cos(dec) / ARCSEC, np.full(off.shape, dec0)], axis=1)
+    return _problem(precision, uvw, a1, a2, tid, n_ant, n_times, freqs, vis_c, seed, nx=nx, ny=nx, cell=cell,
+                    conv=conv, s=s, os=os, phase_centre=(0.0, dec0), facet_centres=facet_centres, noise=noise)
+
+
 def small_problem(precision="double", *, n_ant=8, n_times=12, n_chan=3, nx=96, ny=None, cell=60.0,
                   s=3, os=15, wplanes=1, n_facets=0, jones=False, seed=5, flag_fraction=0.1,
                   kernel="pswf", min_support=None, n_spw=1) -> GriddingProblem:
