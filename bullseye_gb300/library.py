@@ -47,6 +47,7 @@ EXTENSIONS = {
     "bullseye_grid_batched": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "bullseye_grid_adjoint": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                              ctypes.c_int, ctypes.c_void_p]),
+    "bullseye_sampling_counts_nn": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "bullseye_reset_counters": (None, []),
     "bullseye_zero_grids": (None, []),
     "bullseye_set_gridding_correction": (None, [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t]),

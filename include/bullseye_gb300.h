@@ -143,6 +143,17 @@ int bullseye_facet_4_cor_corrections_noalloc(const gridding_parameters *params, 
 int bullseye_grid_adjoint(const gridding_parameters *params, const void *grad_grid, void *grad_vis,
                           void *grad_jones, int faceting, void *stream);
 
+/* Integer sampling-function counts with the reference's nearest-neighbour policy
+ * (bullseye/mo/cpu_algorithm/convolution_policies.h:35-65 composed with the sampling-function policy,
+ * correlation_gridding_policies.h:190-245): every kept (row, channel) adds 1 to the cell
+ * lrint(u * u_scale + nx/2), lrint(v * v_scale + ny/2), computed in the library's data precision with
+ * the reference's operation order, so the counts are bit-exact.  ACCUMULATES into counts
+ * [facets][sampling_function_channel_count][ny][nx] (uint32, device; zero it first); the facets all
+ * receive the same counts (the sampling function's uv transform is the identity in facet mode).
+ * Row arrays, reference_wavelengths, enabled_channels and sampling_function_channel_grid_indicies
+ * are DEVICE pointers.  Synchronises `stream` to report index errors.  Returns 0 or a bz status. */
+int bullseye_sampling_counts_nn(const gridding_parameters *params, unsigned int *counts, int faceting, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -34,7 +34,16 @@ build() {
         "$MO/cpu_gpu_common/fft_and_repacking_routines.cpp" \
         "$OUT/fftw_shim.o" -o "$OUT/$name"
 }
+# the nearest-neighbour sampling-count harness (oracle/ref_nn_harness.cpp) over the same headers
+build_nn() {
+    local prec="$1" name="$2"
+    g++ -DBULLSEYE_"$prec" -fPIC -shared -O3 -fopenmp -pthread -std=c++11 -fno-strict-aliasing -w \
+        -I"$HERE/shim" -I"$MO/cpu_gpu_common" -I"$MO/cpu_algorithm" -I"$CUDA_INC" \
+        "$HERE/ref_nn_harness.cpp" -o "$OUT/$name"
+}
 build SINGLE libcpu_imaging32.so &
 build DOUBLE libcpu_imaging64.so &
+build_nn SINGLE libref_nn32.so &
+build_nn DOUBLE libref_nn64.so &
 wait
-echo "build_ref: built $OUT/libcpu_imaging32.so $OUT/libcpu_imaging64.so"
+echo "build_ref: built $OUT/libcpu_imaging32.so $OUT/libcpu_imaging64.so $OUT/libref_nn32.so $OUT/libref_nn64.so"
