@@ -70,6 +70,10 @@ def parse():
     ap.add_argument("--no-other", action="store_true", help="skip timing the other form")
     ap.add_argument("--facets", type=int, default=0, help="override the facet count (profiling cases)")
     ap.add_argument("--no-precision", action="store_true", help="skip the per-facet FP32 error report")
+    ap.add_argument("--no-class-profile", action="store_true",
+                    help="skip the eager, per-support-class timed step after the timed region")
+    ap.add_argument("--eager", action="store_true",
+                    help="batched form without graph replay (per-class launches with events; for profilers)")
     return ap.parse_args()
 
 
@@ -113,34 +117,51 @@ def kernel_stack(wmax):
     return stack.astype(np.complex64), supports
 
 
-def support_class_widths(conv, W, os_):
-    """Per w plane, the support-class width the batched gridder uses (same rule as the library:
-    the plane's possibly-nonzero support window rounded up to 16, 24, ..., 56 or W)."""
-    widths = [w for w in (16, 24, 32, 40, 48, 56) if w < W] + [W]
-    out = []
-    for row in conv:
-        nz = np.nonzero(np.abs(row) > 0)[0]
-        if nz.size == 0:
-            out.append(widths[0])
-            continue
-        slo = max(0, int(np.ceil((nz[0] - 2 * os_ + 1) / os_)))
-        shi = min(W - 1, nz[-1] // os_)
-        width = max(1, shi - slo + 1)
-        out.append(next((w for w in widths if w >= width), W))
-    return np.asarray(out)
-
-
-def effective_taps(geo, conv):
-    """Sum over (row, channel) of W_class^2: the taps the batched gridder processes per facet."""
-    W = 2 * S_HALF + 1
-    wc = support_class_widths(conv, W, OS)
+def plane_vis_counts(geo):
+    """Visibilities per w plane over all channels (the gridder's plane rule)."""
     w = np.abs(geo["uvw"][:, 2])
-    total = 0.0
+    cnt = np.zeros(WPLANES, np.int64)
     for lam in geo["lam"]:
         pl = np.rint(w / lam * ((WPLANES - 1) / geo["wmax"])).astype(np.int64)
-        pl = np.clip(pl, 0, WPLANES - 1)
-        total += float(np.sum(wc[pl].astype(np.float64) ** 2))
-    return total
+        cnt += np.bincount(np.clip(pl, 0, WPLANES - 1), minlength=WPLANES)
+    return cnt
+
+
+def class_taps(counts, plane_width):
+    """Per support-class width: (visibilities, sum of W_class^2) over (row, channel), per facet."""
+    out = {}
+    for p, cw in enumerate(plane_width):
+        vis, taps = out.get(int(cw), (0, 0.0))
+        out[int(cw)] = (vis + int(counts[p]), taps + float(counts[p]) * float(cw) ** 2)
+    return out
+
+
+def batched_plane_widths(lib):
+    arr = np.zeros(WPLANES, np.int32)
+    n = lib.bullseye_batched_plane_classes(arr.ctypes.data_as(ctypes.c_void_p), WPLANES)
+    return arr[:n] if n else None
+
+
+def class_profile(lib, step, counts, plane_width):
+    """One eager batched step with a CUDA event pair around each support-class launch."""
+    lib.bullseye_set_batched_profiling(1)
+    try:
+        step()
+    finally:
+        lib.bullseye_set_batched_profiling(0)
+    n = 32
+    arrs = [np.zeros(n, np.int32) for _ in range(5)] + [np.zeros(n, np.float32)]
+    cnt = lib.bullseye_batched_profile(*[a.ctypes.data_as(ctypes.c_void_p) for a in arrs], n)
+    width, nc, J, wide, items, ms = arrs
+    taps = class_taps(counts, plane_width)
+    rows = []
+    for i in range(min(cnt, n)):
+        vis, t = taps.get(int(width[i]), (0, 0.0))
+        flops = t * (N_FACETS * 8 * 4 if nc[i] == 4 else 8)
+        rows.append({"width": int(width[i]), "corr": int(nc[i]), "J": int(J[i]), "wide": bool(wide[i]),
+                     "work_items": int(items[i]), "vis": vis, "ms": float(ms[i]),
+                     "executed_tflops": flops / (float(ms[i]) * 1e-3) / 1e12 if ms[i] > 0 else None})
+    return rows
 
 
 def device_inputs(geo, torch):
@@ -459,6 +480,9 @@ def main():
         lib.facet_4_cor_corrections(ctypes.byref(st))
         lib.facet_sampling_function(ctypes.byref(st))
 
+    if args.eager:
+        lib.bullseye_set_batched_profiling(1)
+
     def step_batched():
         rc = lib.bullseye_grid_batched(ctypes.byref(st), 0, 1)
         if rc:
@@ -507,6 +531,12 @@ def main():
         ms = max_over_ranks(ms, device="cuda")
     clk = clocks.stop()
     launches = int(lib.bullseye_kernel_launches())
+    counts = plane_vis_counts(geo)
+    plane_width = batched_plane_widths(lib)
+    classes = None
+    if args.form == "batched" and rank == 0 and not args.no_class_profile and plane_width is not None:
+        classes = class_profile(lib, step, counts, plane_width)
+        check(lib)
     cnt = ctypes.c_longlong(0)
     vis_kernel_ms = lib.bullseye_gridder_kernel_ms(0, ctypes.byref(cnt))
     n_vis_launch = max(1, cnt.value)
@@ -517,20 +547,22 @@ def main():
     fp32_peak = lib.bullseye_fp32_fma_tflops(4096)
     W = 2 * S_HALF + 1
     bytes_per_pair = 8 * 4 + 4 * 4 + 4 + 12 + 64
+    # algorithmic flops: every visibility convolved with its own w plane's true support W_p
+    # (complex tap x complex visibility x 4 correlations per facet, the sampling function once),
+    # plus phase and Jones per pair -- whatever padding an implementation executes
+    true_taps = float(np.sum(counts.astype(np.float64) * np.asarray(supports, np.float64) ** 2))
+    step_flops = true_taps * N_FACETS * 8 * 4 + true_taps * 8 + pairs_per_step * (6 * 4 + 128)
+    flops_per_pair = step_flops / pairs_per_step
     if args.form == "plain":
-        # dominant kernel: the visibility gridder launch (CUDA events around it in the library)
-        flops_per_pair = 8 * 4 * W * W + 6 * 4 + 128
+        # the visibility gridder launch (CUDA events around it in the library), padded W = 63
         launch_ms = vis_kernel_ms / n_vis_launch
-        step_flops = pairs_per_step * flops_per_pair
+        step_flops = true_taps * N_FACETS * 8 * 4 + pairs_per_step * (6 * 4 + 128)  # visibility launch only
+        executed_taps = float(counts.sum()) * W * W
         kernel_name = "romein_grid_kernel<4,wproj,J=8,wide> (visibilities, padded W=63)"
     else:
-        # batched: the per-class persistent gridder launches make up the step; algorithmic flops
-        # are those of the support windows actually gridded (complex tap x 4 correlations, plus
-        # the facet-invariant sampling function once), over the whole step time
-        taps = effective_taps(geo, conv)
-        step_flops = taps * N_FACETS * 8 * 4 + taps * 8 + pairs_per_step * (6 * 4 + 128)
-        flops_per_pair = step_flops / pairs_per_step
+        # batched: the per-class persistent launches make up the step (timed whole)
         launch_ms = ms_per_step
+        executed_taps = sum(t for _, t in class_taps(counts, plane_width).values()) if plane_width is not None else None
         kernel_name = "romein_segment_kernel per support class (whole batched step)"
     achieved = step_flops / (launch_ms * 1e-3) / 1e12
     hbm_gbs = pairs_per_step * bytes_per_pair / (launch_ms * 1e-3) / 1e9
@@ -614,10 +646,16 @@ def main():
                          "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
                          "peak_source": "measured FP32 FMA probe on this GPU (MEASURED_PEAKS.json has no FP32 rate)",
                          "kernel": kernel_name, "launch_ms": launch_ms,
-                         "flops_per_pair": flops_per_pair, "hbm_gbs": hbm_gbs,
+                         "flops_per_pair": flops_per_pair,
+                         "flops_rule": "8 x 4 corr x W_p^2 per (vis, facet) with W_p the visibility's w-plane "
+                                       "support (+ sampling function once, + 152 for phase and Jones)",
+                         "executed_taps_per_vis": executed_taps / float(counts.sum()) if executed_taps else None,
+                         "true_taps_per_vis": true_taps / float(counts.sum()),
+                         "hbm_gbs": hbm_gbs,
                          "hbm_frac_of_measured": hbm_gbs / peaks["hbm_gbs"] if peaks.get("hbm_gbs") else None,
                          "sampling_kernel_ms": sf_kernel_ms / max(1, cnt.value)},
             "clocks": clk, "gpu_launches": launches, "e2e": e2e, "cpu_baseline": cpu, "precision": precision,
+            "class_profile": classes,
         }
         print(json.dumps(line))
 

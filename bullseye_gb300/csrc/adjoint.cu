@@ -12,9 +12,10 @@
 //   g_M  = conj(s) g_V'
 //   g_V  = P^H g_M Q                                      (P = J_p^-1, Q = J_q^-1)
 //   g_Jp = -P^H g_M M^H,   g_Jq = -Q^H g_M^H M            (d(J^-1) = -J^-1 dJ J^-1)
-// Cells and taps are selected exactly as the gridder does (FP64 uvw, phase and cell selection,
-// floor for 1-D AA kernels, round-half-even for w-projection, full support W).  The normalisation
-// sums depend only on weights and taps, so they carry no gradient.
+// Cells, taps, w plane and phase come from the gridder's own choose_cells (floor for 1-D AA
+// kernels, round-half-even for w-projection, full-support acceptance), so the adjoint reads exactly
+// the footprint the gridder wrote.  The normalisation sums depend only on weights and taps, so they
+// carry no gradient.
 //
 // One warp per (row, channel) loops over the facets: the lanes split the W x W footprint, the
 // partial sums are reduced with shuffles, lane 0 forms the gradients.  The visibility gradient
@@ -154,9 +155,13 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
     if (!a.enabled[sc]) continue;
     const size_t g = a.cgi[sc];
     if (g >= (size_t)a.cube) continue;
-    const double inv = 1.0 / (double)a.wavelengths[sc];
-    const double u_l = (double)a.uvw[3 * row] * inv, v_l = (double)a.uvw[3 * row + 1] * inv,
-                 w_l = (double)a.uvw[3 * row + 2] * inv;
+    ChanCache cc;
+    cc.spw = spw;
+    cc.inv = 1.0 / (double)a.wavelengths[sc];
+    cc.su = cc.inv * a.u_scale;
+    cc.sv = cc.inv * a.v_scale;
+    cc.sw = cc.inv * plane_scale;
+    const double um = (double)a.uvw[3 * row], vm = (double)a.uvw[3 * row + 1], wm = (double)a.uvw[3 * row + 2];
     const bool row_ok = !a.flagged_rows[row] && a.field[row] == a.imaging_field;
     const long long base = (row * a.nchan + c) * 4;
     acc_real cw[4];
@@ -191,36 +196,16 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
         jok = inv2(Pm) && inv2(Qm);
         if (!jok) continue;
       }
-      // geometry, exactly as the gridder's prologue
-      const FacetXform x = fx[f];
+      // geometry: the gridder's own cell choice (same cells, taps, plane and phase)
+      CellChoice cell;
       cplx ph;
-      ph.re = 1;
-      ph.im = 0;
-      if (a.faceting) ph = phase_factor(6.283185307179586476925286766559 * (u_l * x.dl + v_l * x.dm + w_l * x.dn));
-      double u = u_l, v = v_l, w = w_l;
-      if (a.faceting) {
-        u = u - w * x.u_term;
-        v = v - w * x.v_term;
-      }
-      u *= a.u_scale;
-      v *= a.v_scale;
-      const bool flip = WPROJ && w < 0;
-      if (flip) { u = -u; v = -v; w = -w; }
-      const double ru_ = WPROJ ? rint(u) : floor(u);
-      const double rv_ = WPROJ ? rint(v) : floor(v);
-      const double du_d = WPROJ ? rint(u + a.gcx) : floor(u + a.gcx);
-      const double dv_d = WPROJ ? rint(v + a.gcy) : floor(v + a.gcy);
-      long long plane = 0;
-      if (WPROJ) {
-        const double pl = rint(fabs(w) * plane_scale);
-        plane = (pl >= 0.0 && pl < (double)a.P) ? (long long)pl : -1;
-      }
-      if (!(du_d >= 0.0 && dv_d >= 0.0 && du_d + (W + 2) < (double)a.nx && dv_d + (W + 2) < (double)a.ny &&
-            plane >= 0 && plane < a.P))
+      if (!choose_cells<WPROJ>(um, vm, wm, cc, fx[f], a.faceting != 0, a.faceting != 0, a.u_scale, a.v_scale,
+                               plane_scale, a.gcx, a.gcy, a.nx, a.ny, W, a.P, a.os, ph, cell))
         continue;
-      const int u0 = (int)du_d, v0 = (int)dv_d;
-      const long long fu = plane * a.K + (long long)((1.0 - u + ru_) * (double)a.os);
-      const long long fv = plane * a.K + (long long)((1.0 - v + rv_) * (double)a.os);
+      const bool flip = cell.flip;
+      const int u0 = cell.du, v0 = cell.dv;
+      const long long fu = (long long)cell.plane * a.K + cell.fu;
+      const long long fv = (long long)cell.plane * a.K + cell.fv;
       const long long slice0 = ((long long)f * a.cube + (long long)g) * 4;
       // gather: D_k = sum over the footprint of g_G conj(tap)
       cplx D[4];

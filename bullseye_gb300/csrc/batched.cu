@@ -30,7 +30,7 @@ using namespace bz;
 
 namespace {
 
-constexpr int kMaxClasses = 8;
+constexpr int kMaxClasses = 16;
 
 __global__ void classify_kernel(const vis_real *__restrict__ uvw, const unsigned *__restrict__ spw,
                                 const vis_real *__restrict__ wavelengths, int nchan, int nspw, long long R,
@@ -202,21 +202,34 @@ struct BatchedState {
   // captured graph
   cudaGraphExec_t exec = nullptr;
   std::vector<unsigned char> key;
+  // eager, per-class timed mode (bullseye_set_batched_profiling)
+  bool profile = false;
+  struct ClassRecord {
+    int width, nc, J, wide, items;
+    float ms;
+  };
+  std::vector<ClassRecord> records;
+  std::vector<int> plane_width;  // class width of every w plane (plan_classes)
 };
 BatchedState g_bs;
 
-// Support windows of every w plane, rounded up to a class width.
+// Support windows of every w plane, rounded up to a class width.  A cell s of the footprint
+// reads table sample fu + s*os, where fu = trunc((1 - u + round(u)) * os) spans
+// [floor(os/2), floor(3 os/2)] with round-to-nearest (w-projection) and [0, os] with floor (AA);
+// the window keeps every s that can reach a nonzero sample for some fu in that range, so the
+// taps left out are exactly zero.  Only the class widths some plane uses get a launch.
 bool plan_classes() {
   Context &c = g_ctx;
   BatchedState &b = g_bs;
   const int W = (int)c.W, os = (int)c.os, K = (int)c.K, P = (int)c.P;
   const bool wproj = c.P > 1;
-  std::vector<int> widths;
-  for (int w : {16, 24, 32, 40, 48, 56})
-    if (w < W) widths.push_back(w);
-  widths.push_back(W);
-  std::vector<int> pcls(P), plo(P);
-  std::vector<int> used(widths.size(), 0);
+  std::vector<int> cand;
+  for (int w : {16, 18, 20, 22, 24, 28, 32, 36, 40, 44, 48, 56})
+    if (w < W) cand.push_back(w);
+  cand.push_back(W);
+  const int fu_min = wproj ? (int)std::floor(0.5 * os - 1e-6) : 0;
+  const int fu_max = wproj ? (int)std::floor(1.5 * os + 1e-6) : os;
+  std::vector<int> pw(P), plo(P);
   for (int p = 0; p < P; ++p) {
     int nzlo = -1, nzhi = -1;
     for (int i = 0; i < K; ++i) {
@@ -230,19 +243,23 @@ bool plan_classes() {
     }
     int slo = 0, shi = 0;
     if (nzlo >= 0) {
-      // a tap of support index s reads offset f + s*os with f in [0, 2 os): keep every s that can
-      // reach a nonzero sample
-      slo = std::max(0, (int)std::ceil((double)(nzlo - 2 * os + 1) / os));
-      shi = std::min(W - 1, nzhi / os);
+      slo = std::max(0, (int)std::ceil((double)(nzlo - fu_max) / os));
+      shi = std::min(W - 1, (int)std::floor((double)(nzhi - fu_min) / os));
+      if (shi < slo) shi = slo;
     }
-    const int width = std::max(1, shi - slo + 1);
-    int k = (int)widths.size() - 1;
-    for (int j = 0; j < (int)widths.size(); ++j)
-      if (widths[j] >= width) { k = j; break; }
-    pcls[p] = k;
-    plo[p] = std::min(slo, W - widths[k]);
-    used[k] = 1;
+    const int width = shi - slo + 1;
+    int cw = W;
+    for (int w : cand)
+      if (w >= width) { cw = w; break; }
+    pw[p] = cw;
+    plo[p] = std::min(slo, W - cw);
   }
+  std::vector<int> widths;
+  for (int w : cand)
+    if (std::find(pw.begin(), pw.end(), w) != pw.end()) widths.push_back(w);
+  std::vector<int> pcls(P);
+  for (int p = 0; p < P; ++p) pcls[p] = (int)(std::find(widths.begin(), widths.end(), pw[p]) - widths.begin());
+  b.plane_width = pw;
   b.ncls = (int)widths.size();
   if (b.ncls > kMaxClasses) return false;
   for (int k = 0; k < b.ncls; ++k) b.cls[k].width = widths[k];
@@ -402,12 +419,28 @@ bool tune_all(const GridArgs &base, int nfacets, bool sampling, const std::vecto
 }
 
 template <int NC, bool WPROJ, bool COMP>
-bool launch_all(const GridArgs &base, int nfacets, bool sampling, cudaStream_t st) {
-  for (int k = 0; k < g_bs.ncls; ++k) {
-    const Variant &v = sampling ? g_bs.cls[k].sf : g_bs.cls[k].vis;
-    if (!launch_class<NC, WPROJ, COMP>(base, k, v, nfacets, g_bs.class_count.ptr + k,
-                                       g_bs.work_next.ptr + (sampling ? kMaxClasses : 0) + k, st))
-      return false;
+bool launch_all(const GridArgs &base, int nfacets, bool sampling, cudaStream_t st, const std::vector<int> *counts) {
+  BatchedState &b = g_bs;
+  for (int k = 0; k < b.ncls; ++k) {
+    const Variant &v = sampling ? b.cls[k].sf : b.cls[k].vis;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (b.profile) {
+      cudaEventCreate(&e0);
+      cudaEventCreate(&e1);
+      cudaEventRecord(e0, st);
+    }
+    const bool ok = launch_class<NC, WPROJ, COMP>(base, k, v, nfacets, b.class_count.ptr + k,
+                                                  b.work_next.ptr + (sampling ? kMaxClasses : 0) + k, st);
+    if (b.profile) {
+      cudaEventRecord(e1, st);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      b.records.push_back({b.cls[k].width, NC, v.J, (int)v.wide, counts ? (*counts)[k] * nfacets : 0, ms});
+    }
+    if (!ok) return false;
   }
   return true;
 }
@@ -420,8 +453,8 @@ bool dispatch(const GridArgs &va, const GridArgs *sa, int nfacets, bool tune, co
     if (sa && !tune_all<1, WPROJ, COMP>(*sa, 1, true, counts)) return false;
     return true;
   }
-  if (!launch_all<4, WPROJ, COMP>(va, nfacets, false, st)) return false;
-  if (sa && !launch_all<1, WPROJ, COMP>(*sa, 1, true, st)) return false;
+  if (!launch_all<4, WPROJ, COMP>(va, nfacets, false, st, &counts)) return false;
+  if (sa && !launch_all<1, WPROJ, COMP>(*sa, 1, true, st, &counts)) return false;
   return true;
 }
 
@@ -473,6 +506,31 @@ void bz_release_batched() {
 }
 
 // See include/bullseye_gb300.h.
+extern "C" void bullseye_set_batched_profiling(int on) { g_bs.profile = on != 0; }
+
+// See include/bullseye_gb300.h.
+extern "C" int bullseye_batched_plane_classes(int *width, int max) {
+  const auto &w = g_bs.plane_width;
+  for (int i = 0; i < (int)w.size() && i < max; ++i) width[i] = w[i];
+  return g_bs.planned ? (int)w.size() : 0;
+}
+
+// See include/bullseye_gb300.h.
+extern "C" int bullseye_batched_profile(int *width, int *nc, int *J, int *wide, int *items, float *ms, int max) {
+  const auto &r = g_bs.records;
+  const int n = (int)std::min<size_t>(r.size(), max > 0 ? (size_t)max : 0);
+  for (int i = 0; i < n; ++i) {
+    if (width) width[i] = r[i].width;
+    if (nc) nc[i] = r[i].nc;
+    if (J) J[i] = r[i].J;
+    if (wide) wide[i] = r[i].wide;
+    if (items) items[i] = r[i].items;
+    if (ms) ms[i] = r[i].ms;
+  }
+  return (int)r.size();
+}
+
+// See include/bullseye_gb300.h.
 extern "C" int bullseye_grid_batched(gridding_parameters *pp, int call, int with_sampling) {
   if (!bz_check_ready("bullseye_grid_batched")) return bz_error_code() ? bz_error_code() : BZ_ERR_NOT_INITIALISED;
   gridding_parameters &p = *pp;
@@ -514,6 +572,23 @@ extern "C" int bullseye_grid_batched(gridding_parameters *pp, int call, int with
   key[sizeof(GridArgs) * 2] = (unsigned char)sf;
   key[sizeof(GridArgs) * 2 + 1] = (unsigned char)comp;
 
+  if (b.profile) {
+    // eager run with a CUDA event pair around every class launch (no graph)
+    if (!enqueue_schedule(va, c.stream)) return bz_error_code();
+    std::vector<int> counts(kMaxClasses, 0);
+    BZ_CUDA_TRY_RET(cudaMemcpyAsync(counts.data(), b.class_count.ptr, sizeof(int) * kMaxClasses, cudaMemcpyDeviceToHost,
+                                    c.stream), BZ_ERR_CUDA);
+    BZ_CUDA_TRY_RET(cudaStreamSynchronize(c.stream), BZ_ERR_CUDA);
+    if (!run_dispatch(va, sf ? &sa : nullptr, wproj, comp, true, counts, c.stream)) return bz_error_code();
+    b.records.clear();
+    if (!run_dispatch(va, sf ? &sa : nullptr, wproj, comp, false, counts, c.stream)) return bz_error_code();
+    if (p.is_final_data_chunk) {
+      bz_copy_back_grids(p, false);
+      if (sf) bz_copy_back_grids(p, true);
+    }
+    bz_timer_stop();
+    return bz_error_code();
+  }
   if (!b.exec || key != b.key) {
     // first run of this configuration: build the schedule eagerly, tune each class, then capture
     if (!enqueue_schedule(va, c.stream)) return bz_error_code();

@@ -292,10 +292,141 @@ __device__ __forceinline__ void queue_cell(const GridArgs &a, long long slice0, 
 #endif
 }
 
+// Per-visibility normalisation partial sums of a staged chunk (8 bytes per correlation either way).
+// The single-precision library accumulates them in FP32 with Kahan compensation and widens to
+// FP64 only when a partial sum leaves the CTA; the double library accumulates in FP64.
+#if defined(BULLSEYE_SINGLE)
+struct NormAcc {
+  float s, c;
+};
+__device__ __forceinline__ void norm_zero(NormAcc &n) { n.s = 0.f; n.c = 0.f; }
+__device__ __forceinline__ void norm_add(NormAcc &n, float x) {
+  const float y = x - n.c;
+  const float t = n.s + y;
+  n.c = (t - n.s) - y;
+  n.s = t;
+}
+__device__ __forceinline__ double norm_value(const NormAcc &n) { return (double)n.s - (double)n.c; }
+typedef float NormTerm;
+#else
+typedef double NormAcc;
+__device__ __forceinline__ void norm_zero(NormAcc &n) { n = 0.0; }
+__device__ __forceinline__ void norm_add(NormAcc &n, double x) { n += x; }
+__device__ __forceinline__ double norm_value(const NormAcc &n) { return n; }
+typedef double NormTerm;
+#endif
+static_assert(sizeof(NormAcc) == sizeof(double), "normalisation partial sums keep the shared-memory layout");
+
+// Per-channel constants of the prologue, recomputed only when the spw changes along a track.
+struct ChanCache {
+  unsigned spw = 0xffffffffu;
+  double inv = 0;     // 1 / lambda
+  double su = 0, sv = 0, sw = 0;  // (1 / lambda) x u_scale, v_scale, plane scale
+};
+
+// Cells, taps, w plane and phase factor of one visibility in one facet: the geometry shared by
+// the gridder and its adjoint, so both select exactly the same footprint.
+struct CellChoice {
+  int du, dv;    // footprint corner (full support)
+  int fu, fv;    // tap offsets into the plane's kernel row
+  int plane;     // w plane
+  bool flip;     // w < 0 with w-projection: grid the conjugate at (-u, -v)
+};
+
+// Returns false when the footprint leaves the grid or the w plane is out of range (the reference's
+// acceptance test: corner >= 0 and corner + W + 2 < n, convolution_policies.h:81-83,241-243).
+template <bool WPROJ>
+__device__ __forceinline__ bool choose_cells(double um, double vm, double wm, const ChanCache &cc,
+                                             const FacetXform &fx, bool phase, bool uvx, double u_scale,
+                                             double v_scale, double plane_scale, double gcx, double gcy, int nx,
+                                             int ny, int Wf, int P, int os, cplx &ph, CellChoice &out) {
+  ph.re = 1;
+  ph.im = 0;
+#if defined(BULLSEYE_SINGLE)
+  // Single-precision library: the same mathematics with fewer FP64 operations (GB300 issues FP64
+  // at 1/64 of FP32).  FP64 is kept for the phase argument, reduced in turns:
+  //   t = (u dl + v dm + w dn) / lambda (metres x 1/lambda),  phase = e^{2 pi i (t - rint(t))},
+  // and for the pixel coordinates, scaled from metres by the per-channel constants
+  // (1/lambda) x u_scale and (1/lambda) x v_scale, and the tap offsets.
+  (void)u_scale;
+  (void)v_scale;
+  (void)plane_scale;
+  if (phase) {
+    const double t = (um * fx.dl + vm * fx.dm + wm * fx.dn) * cc.inv;
+    const float f = (float)(t - rint(t));
+    float sn, cs;
+    sincospif(2.0f * f, &sn, &cs);
+    ph.re = cs;
+    ph.im = sn;
+  }
+  double u = um, v = vm;
+  if (uvx) {
+    u = fma(-wm, fx.u_term, um);
+    v = fma(-wm, fx.v_term, vm);
+  }
+  u *= cc.su;
+  v *= cc.sv;
+  double wabs = wm;
+  out.flip = WPROJ && wm < 0;
+  if (out.flip) {
+    u = -u; v = -v; wabs = -wm;
+  }
+  const double ru_ = WPROJ ? rint(u) : floor(u);
+  const double rv_ = WPROJ ? rint(v) : floor(v);
+  // the corner offsets nx/2 - s are integers, so round(u + gcx) = round(u) + gcx
+  const double du_d = ru_ + gcx;
+  const double dv_d = rv_ + gcy;
+  long long plane = 0;
+  if (WPROJ) {
+    double pl = rint(fabs(wabs) * cc.sw);
+    plane = (pl >= 0.0 && pl < (double)P) ? (long long)pl : -1;  // NaN and out of range -> dropped
+  }
+  if (!(du_d >= 0.0 && dv_d >= 0.0 && du_d + (Wf + 2) < (double)nx && dv_d + (Wf + 2) < (double)ny && plane >= 0 &&
+        plane < P))
+    return false;
+  // tap offsets in FP64: an FP32 fraction moves a tap by one oversampled step about once in 1e5
+  // samples, which shows in the dirty image at the 1e-5 level
+  out.fu = (int)((1.0 - (u - ru_)) * (double)os);
+  out.fv = (int)((1.0 - (v - rv_)) * (double)os);
+#else
+  // Double-precision library: the reference's operation order (parity at 1e-12 needs the same
+  // cells and taps): uvw / lambda, phase, uv transform, scale, round, tap offsets.
+  double u = um * cc.inv, v = vm * cc.inv, w = wm * cc.inv;
+  if (phase) ph = phase_factor(6.283185307179586476925286766559 * (u * fx.dl + v * fx.dm + w * fx.dn));
+  if (uvx) {
+    u = u - w * fx.u_term;
+    v = v - w * fx.v_term;
+  }
+  u *= u_scale;
+  v *= v_scale;
+  out.flip = WPROJ && w < 0;
+  if (out.flip) {
+    u = -u; v = -v; w = -w;
+  }
+  const double ru_ = WPROJ ? rint(u) : floor(u);
+  const double rv_ = WPROJ ? rint(v) : floor(v);
+  const double du_d = WPROJ ? rint(u + gcx) : floor(u + gcx);
+  const double dv_d = WPROJ ? rint(v + gcy) : floor(v + gcy);
+  long long plane = 0;
+  if (WPROJ) {
+    double pl = rint(fabs(w) * plane_scale);
+    plane = (pl >= 0.0 && pl < (double)P) ? (long long)pl : -1;  // NaN and out of range -> dropped
+  }
+  if (!(du_d >= 0.0 && dv_d >= 0.0 && du_d + (Wf + 2) < (double)nx && dv_d + (Wf + 2) < (double)ny && plane >= 0 &&
+        plane < P))
+    return false;
+  out.fu = (int)((1.0 - u + ru_) * (double)os);
+  out.fv = (int)((1.0 - v + rv_) * (double)os);
+#endif
+  out.du = (int)du_d;
+  out.dv = (int)dv_d;
+  out.plane = (int)plane;
+  return true;
+}
+
 template <int NC, bool WPROJ>
 __device__ __forceinline__ void prologue(const GridArgs &a, int f_local, int chan, long long row, bool in_range,
-                                         VisRec<NC> &rec, unsigned &cached_spw, double &cached_inv,
-                                         const double plane_scale) {
+                                         VisRec<NC> &rec, ChanCache &cc, const double plane_scale) {
   rec.valid = 0;
   if (!in_range) return;
   const int c = chan;
@@ -313,14 +444,14 @@ __device__ __forceinline__ void prologue(const GridArgs &a, int f_local, int cha
   }
   const int fglob = a.facet_base + f_local;
   const FacetXform fx = a.facets[f_local];
-  if (spw != cached_spw) {  // 1/lambda is constant along a track unless the spw changes
-    cached_spw = spw;
-    cached_inv = 1.0 / (double)a.wavelengths[sc];
+  if (spw != cc.spw) {  // 1/lambda is constant along a track unless the spw changes
+    cc.spw = spw;
+    cc.inv = 1.0 / (double)a.wavelengths[sc];
+    cc.su = cc.inv * a.u_scale;
+    cc.sv = cc.inv * a.v_scale;
+    cc.sw = cc.inv * plane_scale;
   }
-  const double inv_lambda = cached_inv;
-  double u = (double)a.uvw[3 * row] * inv_lambda;
-  double v = (double)a.uvw[3 * row + 1] * inv_lambda;
-  double w = (double)a.uvw[3 * row + 2] * inv_lambda;
+  const double um = (double)a.uvw[3 * row], vm = (double)a.uvw[3 * row + 1], wm = (double)a.uvw[3 * row + 2];
   bool row_ok = !a.flagged_rows[row] && (a.field[row] == a.imaging_field);
 
   cplx vis[NC];
@@ -384,38 +515,23 @@ __device__ __forceinline__ void prologue(const GridArgs &a, int f_local, int cha
     vis[k].re *= cw;
     vis[k].im *= cw;
   }
+  CellChoice cell;
+  cplx ph;
+  if (!choose_cells<WPROJ>(um, vm, wm, cc, fx, a.phase != 0, a.uvx != 0, a.u_scale, a.v_scale, plane_scale, a.gcx,
+                           a.gcy, a.nx, a.ny, a.W_full ? a.W_full : a.W, a.P, a.os, ph, cell))
+    return;
   if (a.phase) {
-    cplx ph = phase_factor(6.283185307179586476925286766559 * (u * fx.dl + v * fx.dm + w * fx.dn));
 #pragma unroll
     for (int k = 0; k < NC; ++k) vis[k] = cmul(vis[k], ph);
   }
-  if (a.uvx) {
-    u = u - w * fx.u_term;
-    v = v - w * fx.v_term;
-  }
-  u *= a.u_scale;
-  v *= a.v_scale;
-  if (WPROJ && w < 0) {
+  if (cell.flip) {
 #pragma unroll
     for (int k = 0; k < NC; ++k) vis[k].im = -vis[k].im;
-    u = -u; v = -v; w = -w;
   }
-  double ru_ = WPROJ ? rint(u) : floor(u);
-  double rv_ = WPROJ ? rint(v) : floor(v);
-  double du_d = WPROJ ? rint(u + a.gcx) : floor(u + a.gcx);
-  double dv_d = WPROJ ? rint(v + a.gcy) : floor(v + a.gcy);
-  long long plane = 0;
-  if (WPROJ) {
-    double pl = rint(fabs(w) * plane_scale);
-    plane = (pl >= 0.0 && pl < (double)a.P) ? (long long)pl : -1;  // NaN and out of range -> dropped
-  }
-  const int Wf = a.W_full ? a.W_full : a.W;  // acceptance uses the full support, as the reference
-  if (!(du_d >= 0.0 && dv_d >= 0.0 && du_d + (Wf + 2) < (double)a.nx && dv_d + (Wf + 2) < (double)a.ny &&
-        plane >= 0 && plane < a.P))
-    return;
-  int du = (int)du_d, dv = (int)dv_d;
-  rec.fu = (int)((1.0 - u + ru_) * (double)a.os);
-  rec.fv = (int)((1.0 - v + rv_) * (double)a.os);
+  const long long plane = cell.plane;
+  int du = cell.du, dv = cell.dv;
+  rec.fu = cell.fu;
+  rec.fv = cell.fv;
   if (a.plane_lo) {
     // support-aware: grid only the plane's nonzero window of a.W taps (the taps outside it are
     // exactly zero), shifting the footprint corner and the tap offsets by the window start
@@ -518,7 +634,7 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
   typedef typename TapT<WPROJ>::type tap_t;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   VisRec<NC> *recs = reinterpret_cast<VisRec<NC> *>(smem_raw);
-  double *s_nacc = reinterpret_cast<double *>(smem_raw + sizeof(VisRec<NC>) * a.V);  // [V][NC]
+  NormAcc *s_nacc = reinterpret_cast<NormAcc *>(smem_raw + sizeof(VisRec<NC>) * a.V);  // [V][NC]
   int *s_ng = reinterpret_cast<int *>(s_nacc + (size_t)a.V * NC);                    // [V]
   int *s_mixed = s_ng + a.V;                                                          // [V]
   tap_t *tu = reinterpret_cast<tap_t *>(smem_raw + ((sizeof(VisRec<NC>) + sizeof(double) * NC + 2 * sizeof(int)) * a.V + 15) / 16 * 16);
@@ -552,7 +668,7 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
   const bool want_norm = a.norm != nullptr;
   if (want_norm && tid < a.V) {
 #pragma unroll
-    for (int k = 0; k < NC; ++k) s_nacc[tid * NC + k] = 0.0;
+    for (int k = 0; k < NC; ++k) norm_zero(s_nacc[tid * NC + k]);
     s_ng[tid] = -1;
     s_mixed[tid] = 0;
   }
@@ -568,15 +684,14 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
   }
   unsigned dirty = 0;
   int cg = -1, pu0 = -1, pv0 = -1, ou = 0, ov0 = 0;
-  unsigned cached_spw = 0xffffffffu;
-  double cached_inv = 0.0;
+  ChanCache cc;
   const double plane_scale = WPROJ ? (double)(a.P - 1) / a.wmax : 0.0;
 
   for (long long base = r0; base < r1; base += a.V) {
     const int nv = (int)min((long long)a.V, r1 - base);
     if (tid < a.V) {
       VisRec<NC> rec;
-      prologue<NC, WPROJ>(a, f_local, chan, base + tid, tid < nv, rec, cached_spw, cached_inv, plane_scale);
+      prologue<NC, WPROJ>(a, f_local, chan, base + tid, tid < nv, rec, cc, plane_scale);
       recs[tid] = rec;
     }
     __syncthreads();
@@ -627,21 +742,21 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
         }
         if (act && part == 0 && recs[vi].valid) {
           const VisRec<NC> &r = recs[vi];
-          const double nt = (double)sur * (double)svr - (double)sui * (double)svi;
-          double *na = s_nacc + vi * NC;
+          const NormTerm nt = (NormTerm)sur * (NormTerm)svr - (NormTerm)sui * (NormTerm)svi;
+          NormAcc *na = s_nacc + vi * NC;
           if (s_ng[vi] != r.g) {
             if (s_ng[vi] >= 0) {
               s_mixed[vi] = 1;
 #pragma unroll
               for (int k = 0; k < NC; ++k)
-                if (na[k] != 0.0) atomicAdd(&a.norm[(fslice + s_ng[vi]) * NC + k], na[k]);
+                if (norm_value(na[k]) != 0.0) atomicAdd(&a.norm[(fslice + s_ng[vi]) * NC + k], norm_value(na[k]));
             }
 #pragma unroll
-            for (int k = 0; k < NC; ++k) na[k] = 0;
+            for (int k = 0; k < NC; ++k) norm_zero(na[k]);
             s_ng[vi] = r.g;
           }
 #pragma unroll
-          for (int k = 0; k < NC; ++k) na[k] += (double)r.cw[k] * nt;
+          for (int k = 0; k < NC; ++k) norm_add(na[k], (NormTerm)r.cw[k] * nt);
         }
       }
     }
@@ -735,15 +850,15 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
     const bool uniform_here = tid >= a.V || (!s_mixed[tid] && (my_g < 0 || my_g == gmax));
     const int all_uniform = __syncthreads_and(uniform_here ? 1 : 0);
     if (tid < a.V && my_g >= 0) {
-      const double *na = s_nacc + tid * NC;
+      const NormAcc *na = s_nacc + tid * NC;
       if (all_uniform) {
 #pragma unroll
         for (int k = 0; k < NC; ++k)
-          if (na[k] != 0.0) atomicAdd(&s_norm[k], na[k]);
+          if (norm_value(na[k]) != 0.0) atomicAdd(&s_norm[k], norm_value(na[k]));
       } else {
 #pragma unroll
         for (int k = 0; k < NC; ++k)
-          if (na[k] != 0.0) atomicAdd(&a.norm[(fslice + my_g) * NC + k], na[k]);
+          if (norm_value(na[k]) != 0.0) atomicAdd(&a.norm[(fslice + my_g) * NC + k], norm_value(na[k]));
       }
     }
     __syncthreads();

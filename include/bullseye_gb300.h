@@ -108,6 +108,17 @@ double bullseye_fp32_fma_tflops(int iters);
  * after its first use (layouts per support class are picked by timing on that first use).
  * Returns 0 or the error code (also reported by bullseye_last_error). */
 int bullseye_grid_batched(gridding_parameters *params, int call, int with_sampling);
+/* Profiling mode of bullseye_grid_batched (off by default): when on, each call runs eagerly (no
+ * graph) with a CUDA event pair around every support-class launch, synchronising after each. */
+void bullseye_set_batched_profiling(int on);
+/* The last profiled call's class launches: support width, correlations (4 visibilities, 1
+ * sampling function), layout (J rows per thread, WIDE), (track run, facet) work items and
+ * milliseconds, up to max entries; returns the number of launches recorded. */
+int bullseye_batched_profile(int *width, int *nc, int *J, int *wide, int *items, float *ms, int max);
+/* Support-class width the batched gridder uses for every w plane (the plane's nonzero window,
+ * rounded up to a class width), up to max planes; returns the plane count (0 before the first
+ * batched call after initLibrary). */
+int bullseye_batched_plane_classes(int *width, int max);
 
 /* Allocation-free facet_4_cor_corrections, for callers that cannot allocate device memory while
  * they grid (a fixed device arena with no further cudaMalloc/cudaFree, or code where a device
