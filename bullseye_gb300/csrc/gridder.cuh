@@ -569,12 +569,17 @@ __host__ __device__ inline size_t flush_queue_bytes(int nwarps) {
 // last, so the J consecutive row classes of a thread read consecutive addresses without a wrap.
 constexpr int kTvPad = 15;
 
+// Bytes before the tap arrays: V staged records, their normalisation state (partial sums, grid
+// group, mixed flag), the V + 1 run starts of the chunk; rounded up to 16.
+template <int NC>
+__host__ __device__ inline size_t stage_head_bytes(int V) {
+  return ((sizeof(VisRec<NC>) + sizeof(double) * NC + 3 * sizeof(int)) * (size_t)V + sizeof(int) + 15) / 16 * 16;
+}
+
 template <int NC, bool WPROJ>
 __host__ __device__ inline size_t grid_smem_bytes(int V, int W, int nthreads) {
-  size_t recs = sizeof(VisRec<NC>) * (size_t)V;
-  size_t norm = (sizeof(double) * NC + 2 * sizeof(int)) * (size_t)V;  // per-lane normalisation state
   size_t taps = sizeof(typename TapT<WPROJ>::type) * (size_t)V * (2 * W + kTvPad);
-  return recs + norm + taps + flush_queue_bytes<NC>((nthreads + 31) / 32) + 64;
+  return stage_head_bytes<NC>(V) + taps + flush_queue_bytes<NC>((nthreads + 31) / 32) + 64;
 }
 
 // Staged-chunk size V for a CTA of nthreads: one visibility per thread at most, and shared memory
@@ -584,9 +589,9 @@ __host__ inline int grid_chunk_size(int W, int nthreads) {
   const int ctas = std::max(1, std::min(8, 65536 / (nthreads * 128)));
   const size_t smem_sm = 227 * 1024;
   size_t budget = std::min<size_t>(200 * 1024, smem_sm / ctas - 1024);
-  const size_t fixed = flush_queue_bytes<NC>((nthreads + 31) / 32) + 64;
+  const size_t fixed = flush_queue_bytes<NC>((nthreads + 31) / 32) + 64 + sizeof(int) + 15;
   budget = budget > fixed ? budget - fixed : 0;
-  const size_t per = sizeof(VisRec<NC>) + sizeof(double) * NC + 2 * sizeof(int) +
+  const size_t per = sizeof(VisRec<NC>) + sizeof(double) * NC + 3 * sizeof(int) +
                      sizeof(typename TapT<WPROJ>::type) * (2 * (size_t)W + kTvPad);
   return std::max(1, (int)std::min<size_t>(nthreads, budget / per));
 }
@@ -637,7 +642,8 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
   NormAcc *s_nacc = reinterpret_cast<NormAcc *>(smem_raw + sizeof(VisRec<NC>) * a.V);  // [V][NC]
   int *s_ng = reinterpret_cast<int *>(s_nacc + (size_t)a.V * NC);                    // [V]
   int *s_mixed = s_ng + a.V;                                                          // [V]
-  tap_t *tu = reinterpret_cast<tap_t *>(smem_raw + ((sizeof(VisRec<NC>) + sizeof(double) * NC + 2 * sizeof(int)) * a.V + 15) / 16 * 16);
+  int *s_runs = s_mixed + a.V;  // [V + 1]: first slot of every run of the staged chunk, then nv
+  tap_t *tu = reinterpret_cast<tap_t *>(smem_raw + stage_head_bytes<NC>(a.V));
   const int TVS = a.W + kTvPad;  // row-tap stride per staged visibility
   tap_t *tv = tu + a.V * a.W;
   // per-warp flush queues follow the taps
@@ -648,6 +654,7 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
   int *fqn = reinterpret_cast<int *>(qbase + nwarps * sizeof(FlushRec<NC>) * kFlushQueueCap) + warp_id * 4;
   if (COMP && (threadIdx.x & 31) == 0) *fqn = 0;
   __shared__ int s_same_g;
+  __shared__ int s_nruns;
   __shared__ double s_norm[NC];
 
   const int W = a.W;
@@ -695,6 +702,33 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
       recs[tid] = rec;
     }
     __syncthreads();
+    // runs: maximal stretches of valid staged visibilities with one footprint corner and grid
+    // group (a Romein thread keeps its cells across a run); an invalid slot is a run of its own
+    if (warp_id == 0) {
+      const int lane = tid & 31;
+      int count = 0;
+      for (int b = 0; b < nv; b += 32) {
+        const int t = b + lane;
+        bool start = false;
+        if (t < nv) {
+          const int4 c0 = *reinterpret_cast<const int4 *>(&recs[t].u0);
+          const int4 c1 = *reinterpret_cast<const int4 *>(&recs[t].g);
+          start = !c1.y || t == 0;
+          if (!start) {
+            const int4 p0 = *reinterpret_cast<const int4 *>(&recs[t - 1].u0);
+            const int4 p1 = *reinterpret_cast<const int4 *>(&recs[t - 1].g);
+            start = !p1.y || p0.x != c0.x || p0.y != c0.y || p1.x != c1.x;
+          }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, start);
+        if (start) s_runs[count + __popc(m & ((1u << lane) - 1u))] = t;
+        count += __popc(m);
+      }
+      if (lane == 0) {
+        s_runs[count] = nv;
+        s_nruns = count;
+      }
+    }
     // gather the taps of every staged visibility: W column taps, W + kTvPad row taps
     const int per = 2 * W + kTvPad;
     for (int idx = tid; idx < nv * per; idx += blockDim.x) {
@@ -763,9 +797,11 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
     // grid the staged chunk (every lane of a warp with any owned cell takes part, so the
     // queue drains below are warp-uniform)
     if (__any_sync(0xffffffffu, rows_mask != 0)) {
-      for (int vi = 0; vi < nv; ++vi) {
-        const int4 h0 = *reinterpret_cast<const int4 *>(&recs[vi].u0);
-        const int4 h1 = *reinterpret_cast<const int4 *>(&recs[vi].g);
+      const int nruns = s_nruns;
+      for (int ri = 0; ri < nruns; ++ri) {
+        const int rs = s_runs[ri], re = s_runs[ri + 1];
+        const int4 h0 = *reinterpret_cast<const int4 *>(&recs[rs].u0);
+        const int4 h1 = *reinterpret_cast<const int4 *>(&recs[rs].g);
         if (!h1.y) continue;
         if (h0.x != pu0 || h0.y != pv0 || h1.x != cg) {
           // footprint moved: recompute the owned cells, flush those that changed
@@ -807,22 +843,26 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
           ov0 = nov0;
           pu0 = h0.x;
           pv0 = h0.y;
+          if (COMP) {  // the queue only grows here; the branch is uniform over the CTA
+            __syncwarp();
+            if (*fqn >= kDrainAt) drain_queue<NC>(a, nxy, fq, fqn);
+          }
         }
-        if (COMP) {
-          __syncwarp();
-          if (*fqn >= kDrainAt) drain_queue<NC>(a, nxy, fq, fqn);
-        }
-        const tap_t tuv = tu[vi * W + ou];
-        cplx pre[NC];
+        // the run's visibilities share the owned cells: a branch-free multiply-add loop
+#pragma unroll 2
+        for (int vi = rs; vi < re; ++vi) {
+          const tap_t tuv = tu[vi * W + ou];
+          cplx pre[NC];
 #pragma unroll
-        for (int k = 0; k < NC; ++k) pre[k] = premul(recs[vi].vis[k], tuv);
-        // J consecutive row taps from one base (rows past W are in-bounds padding, never flushed)
-        const tap_t *tvrow = tv + vi * TVS + ov0;
+          for (int k = 0; k < NC; ++k) pre[k] = premul(recs[vi].vis[k], tuv);
+          // J consecutive row taps from one base (rows past W are in-bounds padding, never flushed)
+          const tap_t *tvrow = tv + vi * TVS + ov0;
 #pragma unroll
-        for (int j = 0; j < J; ++j) {
-          const tap_t t = tvrow[j];
+          for (int j = 0; j < J; ++j) {
+            const tap_t t = tvrow[j];
 #pragma unroll
-          for (int k = 0; k < NC; ++k) mac(acc[j][k], pre[k], t);
+            for (int k = 0; k < NC; ++k) mac(acc[j][k], pre[k], t);
+          }
         }
         dirty = rows_mask;
       }
