@@ -61,6 +61,10 @@ struct Context {
   // device tables
   DevBuf<vis_real> conv, wavelengths, facet_centres;
   std::vector<vis_real> conv_host;  // host copy of the kernel table (support windows)
+  // sum over the W taps of every (plane, tap offset) kernel row, FP64 complex [P][2 os + 1][2]:
+  // a visibility's normalisation term is Re(S[plane][fu] * S[plane][fv])
+  DevBuf<double> tap_sums;
+  size_t tap_f = 0;
   DevBuf<uint8_t> enabled;
   DevBuf<size_t> cgi, sf_cgi;
   // device row buffers (chunk_max_row_count rows)

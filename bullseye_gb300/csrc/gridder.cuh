@@ -84,6 +84,8 @@ struct GridArgs {
   const uint8_t *enabled;
   const size_t *cgi;
   const void *conv;              // real [K] or complex [P][K]
+  const double *tap_sums;        // FP64 complex [P][tap_f] row sums of the kernel, or null
+  int tap_f;
   const FacetXform *facets;
   // outputs
   vis_complex *grid;             // slices [(f*groups + g)*NC + k][ny][nx]
@@ -131,7 +133,7 @@ template <int NC>
 struct __align__(16) VisRec {
   int u0, v0, ru, rv;      // footprint corner and its residues mod W
   int g, valid, fu, fv;    // grid group, validity, tap offsets
-  int plane, pad0, pad1, pad2;
+  int plane, fu0, fv0, pad0;  // w plane; tap offsets before the support-window shift
   cplx vis[NC];            // weighted, corrected, rotated visibility
   acc_real cw[NC];         // weight x flag per correlation (normalisation)
 };
@@ -532,6 +534,8 @@ __device__ __forceinline__ void prologue(const GridArgs &a, int f_local, int cha
   int du = cell.du, dv = cell.dv;
   rec.fu = cell.fu;
   rec.fv = cell.fv;
+  rec.fu0 = cell.fu;
+  rec.fv0 = cell.fv;
   if (a.plane_lo) {
     // support-aware: grid only the plane's nonzero window of a.W taps (the taps outside it are
     // exactly zero), shifting the footprint corner and the tap offsets by the window start
@@ -700,6 +704,26 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
       VisRec<NC> rec;
       prologue<NC, WPROJ>(a, f_local, chan, base + tid, tid < nv, rec, cc, plane_scale);
       recs[tid] = rec;
+      // normalisation from the precomputed row sums: the staging thread owns slot tid's sums
+      if (want_norm && a.tap_sums && rec.valid) {
+        const double *su = a.tap_sums + 2 * ((long long)rec.plane * a.tap_f + rec.fu0);
+        const double *sv = a.tap_sums + 2 * ((long long)rec.plane * a.tap_f + rec.fv0);
+        const NormTerm nt = (NormTerm)(su[0] * sv[0] - su[1] * sv[1]);
+        NormAcc *na = s_nacc + tid * NC;
+        if (s_ng[tid] != rec.g) {
+          if (s_ng[tid] >= 0) {
+            s_mixed[tid] = 1;
+#pragma unroll
+            for (int k = 0; k < NC; ++k)
+              if (norm_value(na[k]) != 0.0) atomicAdd(&a.norm[(fslice + s_ng[tid]) * NC + k], norm_value(na[k]));
+          }
+#pragma unroll
+          for (int k = 0; k < NC; ++k) norm_zero(na[k]);
+          s_ng[tid] = rec.g;
+        }
+#pragma unroll
+        for (int k = 0; k < NC; ++k) norm_add(na[k], (NormTerm)rec.cw[k] * nt);
+      }
     }
     __syncthreads();
     // runs: maximal stretches of valid staged visibilities with one footprint corner and grid
@@ -746,10 +770,10 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
       *dst = t;
     }
     __syncthreads();
-    // normalisation, four lanes per staged visibility: Re(sum_u k_u * sum_v k_v) x weight x flag
-    // (loop bounds are warp-uniform so the shuffles always see full warps); lane 4i owns the
-    // running sums of staged slot i in shared memory
-    if (want_norm) {
+    // normalisation without precomputed row sums (the allocation-free entry), four lanes per
+    // staged visibility: Re(sum_u k_u * sum_v k_v) x weight x flag (loop bounds are warp-uniform
+    // so the shuffles always see full warps); lane 4i owns the running sums of staged slot i
+    if (want_norm && !a.tap_sums) {
       for (int b4 = tid & ~31; b4 < 4 * nv; b4 += blockDim.x) {
         const int q = b4 + (tid & 31);
         const int vi = q >> 2, part = q & 3;

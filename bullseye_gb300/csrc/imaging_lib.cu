@@ -291,6 +291,30 @@ extern "C" void initLibrary(gridding_parameters *pp) {
   if (!ok) return;
   BZ_CUDA_TRY(cudaMemcpy(c.conv.ptr, p.conv, sizeof(vis_real) * conv_elems, cudaMemcpyHostToDevice));
   c.conv_host.assign(p.conv, p.conv + conv_elems);
+  {
+    // row sums of the kernel for every (plane, tap offset): tap offsets span [0, 2 os]
+    c.tap_f = 2 * c.os + 1;
+    std::vector<double> sums(2 * c.P * c.tap_f, 0.0);
+    const size_t W = c.W;
+    for (size_t pl = 0; pl < c.P; ++pl)
+      for (size_t f = 0; f < c.tap_f; ++f) {
+        double re = 0, im = 0;
+        for (size_t j = 0; j < W; ++j) {
+          const size_t i = f + j * c.os;
+          if (i >= c.K) break;
+          if (wproj) {
+            re += (double)c.conv_host[2 * (pl * c.K + i)];
+            im += (double)c.conv_host[2 * (pl * c.K + i) + 1];
+          } else {
+            re += (double)c.conv_host[i];
+          }
+        }
+        sums[2 * (pl * c.tap_f + f)] = re;
+        sums[2 * (pl * c.tap_f + f) + 1] = im;
+      }
+    if (!c.tap_sums.alloc(sums.size())) return;
+    BZ_CUDA_TRY(cudaMemcpy(c.tap_sums.ptr, sums.data(), sizeof(double) * sums.size(), cudaMemcpyHostToDevice));
+  }
   BZ_CUDA_TRY(cudaMemcpy(c.wavelengths.ptr, p.reference_wavelengths, sizeof(vis_real) * sc, cudaMemcpyHostToDevice));
   BZ_CUDA_TRY(cudaMemcpy(c.enabled.ptr, p.enabled_channels, sc, cudaMemcpyHostToDevice));
   BZ_CUDA_TRY(cudaMemcpy(c.cgi.ptr, p.channel_grid_indicies, sizeof(size_t) * sc, cudaMemcpyHostToDevice));
@@ -340,7 +364,7 @@ extern "C" void releaseLibrary() {
   Context &c = g_ctx;
   if (!c.initialized) return;
   if (c.stream) cudaStreamSynchronize(c.stream);
-  c.conv.release(); c.wavelengths.release(); c.facet_centres.release(); c.enabled.release();
+  c.conv.release(); c.tap_sums.release(); c.wavelengths.release(); c.facet_centres.release(); c.enabled.release();
   c.cgi.release(); c.sf_cgi.release(); c.vis.release(); c.weights.release(); c.uvw.release();
   c.flags.release(); c.flagged_rows.release(); c.field.release(); c.spw.release(); c.ant1.release();
   c.ant2.release(); c.time_ids.release(); c.starts.release(); c.jones_raw.release(); c.jones_inv.release();
@@ -711,6 +735,8 @@ bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool f
   a.wavelengths = c.wavelengths.ptr; a.enabled = c.enabled.ptr;
   a.cgi = sampling ? c.sf_cgi.ptr : c.cgi.ptr;
   a.conv = c.conv.ptr;
+  a.tap_sums = c.tap_sums.ptr;
+  a.tap_f = (int)c.tap_f;
   a.facets = table.ptr;
   a.grid = sampling ? c.sf_acc.ptr : c.grid.ptr;
   a.grid_lo = nullptr;
