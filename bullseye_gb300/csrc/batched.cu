@@ -267,7 +267,7 @@ bool plan_classes() {
   BZ_CUDA_TRY_RET(cudaMemcpy(b.plane_class.ptr, pcls.data(), sizeof(int) * P, cudaMemcpyHostToDevice), false);
   BZ_CUDA_TRY_RET(cudaMemcpy(b.plane_lo.ptr, plo.data(), sizeof(int) * P, cudaMemcpyHostToDevice), false);
   if (!b.class_count.alloc(kMaxClasses) || !b.class_off.alloc(kMaxClasses) || !b.class_cursor.alloc(kMaxClasses) ||
-      !b.work_next.alloc(2 * kMaxClasses) || !b.seg_total.alloc(1) || !b.sample_count.alloc(kMaxClasses))
+      !b.work_next.alloc(2 * kMaxClasses) || !b.seg_total.alloc(1) || !b.sample_count.alloc(2 * kMaxClasses))
     return false;
   b.planned = true;
   return true;
@@ -378,9 +378,13 @@ bool tune_class(const GridArgs &base, int k, int nfacets, Variant &out, int host
     b.tuned[key] = {out.J, (int)out.wide};
     return true;
   }
-  // sample: up to 512 segments of the class, into the scratch grid (no effect on results)
-  const int sample = std::min(host_count, 512);
-  BZ_CUDA_TRY_RET(cudaMemcpy(b.sample_count.ptr + k, &sample, sizeof(int), cudaMemcpyHostToDevice), false);
+  // Each candidate grids a quarter of the class's runs (at least 4096, when there are that many)
+  // into the scratch grid (no effect on results): smaller samples leave the persistent grid
+  // underfilled and favour the wrong layout.  A short first launch loads the variant's code.
+  const int counts2[2] = {std::min(host_count, 64), std::min(host_count, std::max(4096, host_count / 4))};
+  BZ_CUDA_TRY_RET(cudaMemcpyAsync(b.sample_count.ptr + 2 * k, counts2, sizeof(counts2), cudaMemcpyHostToDevice, c.stream),
+                  false);
+  BZ_CUDA_TRY_RET(cudaStreamSynchronize(c.stream), false);
   GridArgs a = base;
   a.grid = c.scratch.ptr;
   a.grid_lo = COMP ? c.scratch.ptr : nullptr;
@@ -390,9 +394,10 @@ bool tune_class(const GridArgs &base, int k, int nfacets, Variant &out, int host
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   for (auto &v : cands) {
-    if (!launch_class<NC, WPROJ, COMP>(a, k, v, nfacets, b.sample_count.ptr + k, b.work_next.ptr + k, c.stream)) break;
+    if (!launch_class<NC, WPROJ, COMP>(a, k, v, nfacets, b.sample_count.ptr + 2 * k, b.work_next.ptr + k, c.stream))
+      break;
     cudaEventRecord(e0, c.stream);
-    launch_class<NC, WPROJ, COMP>(a, k, v, nfacets, b.sample_count.ptr + k, b.work_next.ptr + k, c.stream);
+    launch_class<NC, WPROJ, COMP>(a, k, v, nfacets, b.sample_count.ptr + 2 * k + 1, b.work_next.ptr + k, c.stream);
     cudaEventRecord(e1, c.stream);
     cudaEventSynchronize(e1);
     float ms = 0;

@@ -65,6 +65,9 @@ struct Context {
   // a visibility's normalisation term is Re(S[plane][fu] * S[plane][fv])
   DevBuf<double> tap_sums;
   size_t tap_f = 0;
+  // the kernel table regrouped by tap offset, [P][tap_f][W] (real or complex like conv): the W taps
+  // a visibility reads are contiguous, so staging them is a coalesced copy
+  DevBuf<vis_real> conv_t;
   DevBuf<uint8_t> enabled;
   DevBuf<size_t> cgi, sf_cgi;
   // device row buffers (chunk_max_row_count rows)

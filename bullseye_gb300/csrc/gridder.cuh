@@ -86,6 +86,7 @@ struct GridArgs {
   const void *conv;              // real [K] or complex [P][K]
   const double *tap_sums;        // FP64 complex [P][tap_f] row sums of the kernel, or null
   int tap_f;
+  const void *conv_t;            // kernel regrouped by tap offset [P][tap_f][W], or null
   const FacetXform *facets;
   // outputs
   vis_complex *grid;             // slices [(f*groups + g)*NC + k][ny][nx]
@@ -536,14 +537,21 @@ __device__ __forceinline__ void prologue(const GridArgs &a, int f_local, int cha
   rec.fv = cell.fv;
   rec.fu0 = cell.fu;
   rec.fv0 = cell.fv;
+  int lo = 0;
   if (a.plane_lo) {
     // support-aware: grid only the plane's nonzero window of a.W taps (the taps outside it are
     // exactly zero), shifting the footprint corner and the tap offsets by the window start
-    const int lo = a.plane_lo[plane];
+    lo = a.plane_lo[plane];
     du += lo;
     dv += lo;
     rec.fu += lo * a.os;
     rec.fv += lo * a.os;
+  }
+  if (a.conv_t) {
+    // index of the first staged tap in the regrouped table
+    const int Wfull = a.W_full ? a.W_full : a.W;
+    rec.fu = (int)(((long long)plane * a.tap_f + cell.fu) * Wfull + lo);
+    rec.fv = (int)(((long long)plane * a.tap_f + cell.fv) * Wfull + lo);
   }
   rec.plane = (int)plane;
   rec.u0 = du;
@@ -569,9 +577,9 @@ __host__ __device__ inline size_t flush_queue_bytes(int nwarps) {
 #endif
 }
 
-// Row taps are stored W + kTvPad long per visibility: the first kTvPad taps are repeated after the
-// last, so the J consecutive row classes of a thread read consecutive addresses without a wrap.
-constexpr int kTvPad = 15;
+// Row taps are stored W long per visibility (no padding: a thread's J consecutive owned rows
+// wrap modulo W through per-run row offsets).
+constexpr int kTvPad = 0;
 
 // Bytes before the tap arrays: V staged records, their normalisation state (partial sums, grid
 // group, mixed flag), the V + 1 run starts of the chunk; rounded up to 16.
@@ -753,21 +761,32 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
         s_nruns = count;
       }
     }
-    // gather the taps of every staged visibility: W column taps, W + kTvPad row taps
-    const int per = 2 * W + kTvPad;
-    for (int idx = tid; idx < nv * per; idx += blockDim.x) {
-      const int vi = idx / per, j = idx - vi * per;
-      const VisRec<NC> &r = recs[vi];
-      if (!r.valid) continue;
-      const bool isv = j >= W;
-      int jj = isv ? j - W : j;
-      tap_t *dst = isv ? tv + vi * TVS + jj : tu + vi * W + jj;
-      if (jj >= W) jj -= W;  // repeated leading row taps
-      if (jj >= W) jj = W - 1;
-      const long long ti = (long long)r.plane * a.K + (isv ? r.fv : r.fu) + (long long)jj * a.os;
-      tap_t t;
-      load_tap(a.conv, ti, t);
-      *dst = t;
+    // gather the taps of every staged visibility: W column taps, then W row taps.  Thread tid
+    // walks (visibility, tap) pairs with a stride of blockDim.x pairs, stepped without division.
+    {
+      const int per = 2 * W;
+      int vi = tid / per, j = tid - vi * per;
+      const int svi = (int)blockDim.x / per, sj = (int)blockDim.x - svi * per;
+      while (vi < nv) {
+        const int4 h1 = *reinterpret_cast<const int4 *>(&recs[vi].g);  // g, valid, fu, fv
+        if (h1.y) {
+          const bool isv = j >= W;
+          const int jj = isv ? j - W : j;
+          tap_t t;
+          if (a.conv_t) {
+            load_tap(a.conv_t, (long long)(isv ? h1.w : h1.z) + jj, t);
+          } else {
+            load_tap(a.conv, (long long)recs[vi].plane * a.K + (isv ? h1.w : h1.z) + (long long)jj * a.os, t);
+          }
+          (isv ? tv : tu)[vi * W + jj] = t;
+        }
+        vi += svi;
+        j += sj;
+        if (j >= per) {
+          j -= per;
+          ++vi;
+        }
+      }
     }
     __syncthreads();
     // normalisation without precomputed row sums (the allocation-free entry), four lanes per
@@ -872,18 +891,22 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
             if (*fqn >= kDrainAt) drain_queue<NC>(a, nxy, fq, fqn);
           }
         }
-        // the run's visibilities share the owned cells: a branch-free multiply-add loop
+        // the run's visibilities share the owned cells: a branch-free multiply-add loop over
+        // the J owned rows (offsets modulo W; rows of non-owning lanes stay in bounds and are
+        // never flushed)
+        int ro[J];
+#pragma unroll
+        for (int j = 0; j < J; ++j) ro[j] = (ov0 + j) % W;
 #pragma unroll 2
         for (int vi = rs; vi < re; ++vi) {
           const tap_t tuv = tu[vi * W + ou];
           cplx pre[NC];
 #pragma unroll
           for (int k = 0; k < NC; ++k) pre[k] = premul(recs[vi].vis[k], tuv);
-          // J consecutive row taps from one base (rows past W are in-bounds padding, never flushed)
-          const tap_t *tvrow = tv + vi * TVS + ov0;
+          const tap_t *tvrow = tv + vi * W;
 #pragma unroll
           for (int j = 0; j < J; ++j) {
-            const tap_t t = tvrow[j];
+            const tap_t t = tvrow[ro[j]];
 #pragma unroll
             for (int k = 0; k < NC; ++k) mac(acc[j][k], pre[k], t);
           }

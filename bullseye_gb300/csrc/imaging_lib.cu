@@ -314,6 +314,19 @@ extern "C" void initLibrary(gridding_parameters *pp) {
       }
     if (!c.tap_sums.alloc(sums.size())) return;
     BZ_CUDA_TRY(cudaMemcpy(c.tap_sums.ptr, sums.data(), sizeof(double) * sums.size(), cudaMemcpyHostToDevice));
+    // regrouped table: entry (plane, f, j) = conv[plane][f + j os], zero past the row
+    const size_t ncomp = wproj ? 2 : 1;
+    std::vector<vis_real> regrouped(ncomp * c.P * c.tap_f * W, (vis_real)0);
+    for (size_t pl = 0; pl < c.P; ++pl)
+      for (size_t f = 0; f < c.tap_f; ++f)
+        for (size_t j = 0; j < W; ++j) {
+          const size_t i = f + j * c.os;
+          if (i >= c.K) break;
+          for (size_t q = 0; q < ncomp; ++q)
+            regrouped[ncomp * ((pl * c.tap_f + f) * W + j) + q] = c.conv_host[ncomp * (pl * c.K + i) + q];
+        }
+    if (!c.conv_t.alloc(regrouped.size())) return;
+    BZ_CUDA_TRY(cudaMemcpy(c.conv_t.ptr, regrouped.data(), sizeof(vis_real) * regrouped.size(), cudaMemcpyHostToDevice));
   }
   BZ_CUDA_TRY(cudaMemcpy(c.wavelengths.ptr, p.reference_wavelengths, sizeof(vis_real) * sc, cudaMemcpyHostToDevice));
   BZ_CUDA_TRY(cudaMemcpy(c.enabled.ptr, p.enabled_channels, sc, cudaMemcpyHostToDevice));
@@ -364,7 +377,7 @@ extern "C" void releaseLibrary() {
   Context &c = g_ctx;
   if (!c.initialized) return;
   if (c.stream) cudaStreamSynchronize(c.stream);
-  c.conv.release(); c.tap_sums.release(); c.wavelengths.release(); c.facet_centres.release(); c.enabled.release();
+  c.conv.release(); c.tap_sums.release(); c.conv_t.release(); c.wavelengths.release(); c.facet_centres.release(); c.enabled.release();
   c.cgi.release(); c.sf_cgi.release(); c.vis.release(); c.weights.release(); c.uvw.release();
   c.flags.release(); c.flagged_rows.release(); c.field.release(); c.spw.release(); c.ant1.release();
   c.ant2.release(); c.time_ids.release(); c.starts.release(); c.jones_raw.release(); c.jones_inv.release();
@@ -737,6 +750,7 @@ bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool f
   a.conv = c.conv.ptr;
   a.tap_sums = c.tap_sums.ptr;
   a.tap_f = (int)c.tap_f;
+  a.conv_t = c.conv_t.ptr;
   a.facets = table.ptr;
   a.grid = sampling ? c.sf_acc.ptr : c.grid.ptr;
   a.grid_lo = nullptr;
