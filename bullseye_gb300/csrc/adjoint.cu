@@ -127,7 +127,8 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
     const double k = (double)kArcsecToRad;
     double d_ra = (ra - a.ra0) * k, n_dec = dec * k, o_dec = a.dec0 * k;
     double c_d_ra = cos(d_ra), s_d_ra = sin(d_ra), c_n = cos(n_dec), s_n = sin(n_dec), c_o = cos(o_dec), s_o = sin(o_dec);
-    FacetXform x = {0, 0, 0, 0, 0};
+    FacetXform x;
+    memset(&x, 0, sizeof x);
     if (a.faceting) {
       double li0 = c_n * s_d_ra, mi0 = s_n * c_o - c_n * s_o * c_d_ra, ni0 = s_n * s_o + c_n * c_o * c_d_ra;
       x.u_term = li0 / ni0;

@@ -63,6 +63,11 @@ enum CorrMode { CORR_SINGLE = 0, CORR_DUAL = 1, CORR_QUAD = 2, CORR_QUAD_JONES =
 struct FacetXform {
   double u_term, v_term;  // planar uv transform: u -= w u_term, v -= w v_term
   double dl, dm, dn;      // phase rotation offsets
+  // the facet's grid: uv scale (pixels per wavelength), footprint-corner offsets nx/2 - s and
+  // ny/2 - s, the complex-element offset of its [groups][NC][ny][nx] block, and its size
+  double u_scale, v_scale, gcx, gcy;
+  long long grid_base;
+  int nx, ny;
 };
 
 struct GridArgs {
@@ -87,6 +92,7 @@ struct GridArgs {
   const double *tap_sums;        // FP64 complex [P][tap_f] row sums of the kernel, or null
   int tap_f;
   const void *conv_t;            // kernel regrouped by tap offset [P][tap_f][W], or null
+  const uint8_t *facet_row_mask; // [facets][rows]: 0 leaves the row out of that facet, or null
   const FacetXform *facets;
   // outputs
   vis_complex *grid;             // slices [(f*groups + g)*NC + k][ny][nx]
@@ -195,15 +201,15 @@ __device__ __forceinline__ cplx phase_factor(double x) {
 // (TwoSum: s = a + b, e = (a - (s - (s - a))) + (b - (s - a))) and adds it to the lo grid; the
 // final grid is hi + lo.  The NC atomics of a cell are issued before any result is consumed.
 template <int NC, bool COMP>
-__device__ __forceinline__ void flush_cell(const GridArgs &a, long long slice0, long long nxy, int x, int y,
+__device__ __forceinline__ void flush_cell(const GridArgs &a, long long base, long long nxy, int nx, int x, int y,
                                            cplx (&acc)[NC]) {
-  const long long cell = (long long)y * a.nx + x;
+  const long long cell = base + (long long)y * nx + x;
 #if defined(BULLSEYE_SINGLE)
   if (COMP) {
     float2 old[NC];
 #pragma unroll
     for (int k = 0; k < NC; ++k)
-      old[k] = atomicAdd(reinterpret_cast<float2 *>(a.grid + (slice0 + k) * nxy + cell), make_float2(acc[k].re, acc[k].im));
+      old[k] = atomicAdd(reinterpret_cast<float2 *>(a.grid + k * nxy + cell), make_float2(acc[k].re, acc[k].im));
 #pragma unroll
     for (int k = 0; k < NC; ++k) {
       float s0 = old[k].x + acc[k].re, b0 = s0 - old[k].x;
@@ -211,18 +217,18 @@ __device__ __forceinline__ void flush_cell(const GridArgs &a, long long slice0, 
       float s1 = old[k].y + acc[k].im, b1 = s1 - old[k].y;
       float e1 = (old[k].y - (s1 - b1)) + (acc[k].im - b1);
       if (e0 != 0.0f || e1 != 0.0f)
-        atomicAdd(reinterpret_cast<float2 *>(a.grid_lo + (slice0 + k) * nxy + cell), make_float2(e0, e1));
+        atomicAdd(reinterpret_cast<float2 *>(a.grid_lo + k * nxy + cell), make_float2(e0, e1));
     }
   } else {
 #pragma unroll
     for (int k = 0; k < NC; ++k)
-      atomicAdd(reinterpret_cast<float2 *>(a.grid + (slice0 + k) * nxy + cell), make_float2(acc[k].re, acc[k].im));
+      atomicAdd(reinterpret_cast<float2 *>(a.grid + k * nxy + cell), make_float2(acc[k].re, acc[k].im));
   }
 #else
 #pragma unroll
   for (int k = 0; k < NC; ++k) {
-    atomicAdd(&a.grid[(slice0 + k) * nxy + cell].re, acc[k].re);
-    atomicAdd(&a.grid[(slice0 + k) * nxy + cell].im, acc[k].im);
+    atomicAdd(&a.grid[k * nxy + cell].re, acc[k].re);
+    atomicAdd(&a.grid[k * nxy + cell].im, acc[k].im);
   }
 #endif
 #pragma unroll
@@ -241,7 +247,7 @@ constexpr int kDrainAt = 32;
 
 template <int NC>
 struct FlushRec {
-  long long cell;        // slice0 * nxy + y * nx + x of correlation 0
+  long long cell;        // grid element of correlation 0 (base + y * nx + x)
   float2 v[NC];
 };
 
@@ -277,20 +283,20 @@ __device__ __forceinline__ void drain_queue(const GridArgs &a, long long nxy, Fl
 
 // Queue one owned cell's accumulator (falls back to a direct flush when the queue is full).
 template <int NC>
-__device__ __forceinline__ void queue_cell(const GridArgs &a, long long slice0, long long nxy, int x, int y,
+__device__ __forceinline__ void queue_cell(const GridArgs &a, long long base, long long nxy, int nx, int x, int y,
                                            cplx (&acc)[NC], FlushRec<NC> *q, int *qn) {
 #if defined(BULLSEYE_SINGLE)
   const int slot = atomicAdd(qn, 1);
   if (slot < kFlushQueueCap) {
     FlushRec<NC> r;
-    r.cell = slice0 * nxy + (long long)y * a.nx + x;
+    r.cell = base + (long long)y * nx + x;
 #pragma unroll
     for (int k = 0; k < NC; ++k) r.v[k] = make_float2(acc[k].re, acc[k].im);
     q[slot] = r;
 #pragma unroll
     for (int k = 0; k < NC; ++k) { acc[k].re = 0; acc[k].im = 0; }
   } else {
-    flush_cell<NC, true>(a, slice0, nxy, x, y, acc);
+    flush_cell<NC, true>(a, base, nxy, nx, x, y, acc);
   }
 #endif
 }
@@ -446,12 +452,14 @@ __device__ __forceinline__ void prologue(const GridArgs &a, int f_local, int cha
     return;
   }
   const int fglob = a.facet_base + f_local;
-  const FacetXform fx = a.facets[f_local];
+  // a row left out of this facet (uneven facet layouts) is skipped like an off-grid visibility
+  if (a.facet_row_mask && !a.facet_row_mask[(long long)fglob * a.nrows + row]) return;
+  const FacetXform &fx = a.facets[f_local];
   if (spw != cc.spw) {  // 1/lambda is constant along a track unless the spw changes
     cc.spw = spw;
     cc.inv = 1.0 / (double)a.wavelengths[sc];
-    cc.su = cc.inv * a.u_scale;
-    cc.sv = cc.inv * a.v_scale;
+    cc.su = cc.inv * fx.u_scale;
+    cc.sv = cc.inv * fx.v_scale;
     cc.sw = cc.inv * plane_scale;
   }
   const double um = (double)a.uvw[3 * row], vm = (double)a.uvw[3 * row + 1], wm = (double)a.uvw[3 * row + 2];
@@ -520,8 +528,8 @@ __device__ __forceinline__ void prologue(const GridArgs &a, int f_local, int cha
   }
   CellChoice cell;
   cplx ph;
-  if (!choose_cells<WPROJ>(um, vm, wm, cc, fx, a.phase != 0, a.uvx != 0, a.u_scale, a.v_scale, plane_scale, a.gcx,
-                           a.gcy, a.nx, a.ny, a.W_full ? a.W_full : a.W, a.P, a.os, ph, cell))
+  if (!choose_cells<WPROJ>(um, vm, wm, cc, fx, a.phase != 0, a.uvx != 0, fx.u_scale, fx.v_scale, plane_scale, fx.gcx,
+                           fx.gcy, fx.nx, fx.ny, a.W_full ? a.W_full : a.W, a.P, a.os, ph, cell))
     return;
   if (a.phase) {
 #pragma unroll
@@ -670,7 +678,10 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
   __shared__ double s_norm[NC];
 
   const int W = a.W;
-  const long long nxy = (long long)a.nx * a.ny;
+  const FacetXform &fxt = a.facets[f_local];
+  const int gnx = fxt.nx;
+  const long long nxy = (long long)fxt.nx * fxt.ny;
+  const long long fbase = fxt.grid_base;  // element offset of this facet's grid block
   if (r1 > a.nrows) r1 = a.nrows;
   if (r0 >= r1) return;
 
@@ -859,9 +870,9 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
                 if (dirty & (1u << j)) {
                   const int oy = ov0 + j >= W ? ov0 + j - W : ov0 + j;
                   if (COMP)
-                    queue_cell<NC>(a, (fslice + cg) * NC, nxy, pu0 + ou, pv0 + oy, acc[j], fq, fqn);
+                    queue_cell<NC>(a, fbase + (long long)cg * NC * nxy, nxy, gnx, pu0 + ou, pv0 + oy, acc[j], fq, fqn);
                   else
-                    flush_cell<NC, false>(a, (fslice + cg) * NC, nxy, pu0 + ou, pv0 + oy, acc[j]);
+                    flush_cell<NC, false>(a, fbase + (long long)cg * NC * nxy, nxy, gnx, pu0 + ou, pv0 + oy, acc[j]);
                 }
               dirty = 0;
             }
@@ -874,9 +885,9 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
               const int ny = nov0 + j >= W ? nov0 + j - W : nov0 + j;
               if ((dirty & (1u << j)) && h0.y + ny != pv0 + oy) {
                 if (COMP)
-                  queue_cell<NC>(a, (fslice + cg) * NC, nxy, pu0 + ou, pv0 + oy, acc[j], fq, fqn);
+                  queue_cell<NC>(a, fbase + (long long)cg * NC * nxy, nxy, gnx, pu0 + ou, pv0 + oy, acc[j], fq, fqn);
                 else
-                  flush_cell<NC, false>(a, (fslice + cg) * NC, nxy, pu0 + ou, pv0 + oy, acc[j]);
+                  flush_cell<NC, false>(a, fbase + (long long)cg * NC * nxy, nxy, gnx, pu0 + ou, pv0 + oy, acc[j]);
                 dirty &= ~(1u << j);
               }
             }
@@ -922,7 +933,7 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
 #pragma unroll
     for (int j = 0; j < J; ++j) {
       const int oy = ov0 + j >= W ? ov0 + j - W : ov0 + j;
-      if (dirty & (1u << j)) flush_cell<NC, COMP>(a, (fslice + cg) * NC, nxy, pu0 + ou, pv0 + oy, acc[j]);
+      if (dirty & (1u << j)) flush_cell<NC, COMP>(a, fbase + (long long)cg * NC * nxy, nxy, gnx, pu0 + ou, pv0 + oy, acc[j]);
     }
   }
   // normalisation: one reduction per CTA when every staged slot saw a single grid group

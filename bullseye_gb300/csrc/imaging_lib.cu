@@ -452,7 +452,8 @@ extern "C" void repack_input_data(gridding_parameters *pp) {
 // ---------------------------------------------------------------- gridding launch
 static FacetXform facet_xform(double ra0, double dec0, double ra, double dec, bool phase, bool uvx) {
   // phase_transform_policies.h:110-134 and baseline_transform_policies.h:117-149, in FP64
-  FacetXform x = {0, 0, 0, 0, 0};
+  FacetXform x;
+  std::memset(&x, 0, sizeof x);
   const double k = (double)kArcsecToRad;
   double d_ra = (ra - ra0) * k, n_dec = dec * k, o_dec = dec0 * k;
   double c_d_ra = cos(d_ra), s_d_ra = sin(d_ra), c_n = cos(n_dec), s_n = sin(n_dec), c_o = cos(o_dec),
@@ -727,6 +728,16 @@ bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool f
     // the sampling-function policy reports the phase centre as facet centre
     // (phase_transform_policies.h:77-82), so its uv transform is the identity
     fx[f] = facet_xform(ra0, dec0, ra, dec, phase, faceting);
+    // every facet shares the library's grid size: u_scale = nx * cell * ARCSEC_TO_RAD,
+    // v_scale = -(ny * cell * ARCSEC_TO_RAD) (templated_gridder.h:23-24)
+    fx[f].nx = (int)c.nx;
+    fx[f].ny = (int)c.ny;
+    fx[f].u_scale = (double)c.nx * (double)p.cell_size_x * (double)kArcsecToRad;
+    fx[f].v_scale = -((double)c.ny * (double)p.cell_size_y * (double)kArcsecToRad);
+    fx[f].gcx = (double)(c.nx / 2 - p.conv_support);
+    fx[f].gcy = (double)(c.ny / 2 - p.conv_support);
+    fx[f].grid_base = (long long)f * (long long)(sampling ? c.sf_count : c.cube) * (sampling ? 1 : nc) *
+                      (long long)(c.nx * c.ny);
   }
   DevBuf<FacetXform> &table = sampling ? c.facets_sf : c.facets;
   if (table.n < c.F && !table.alloc(c.F)) return false;

@@ -45,7 +45,9 @@ namespace {
 
 // Per-facet transform constants (FP64) from device-resident facet centres (arcsec):
 // phase_transform_policies.h:110-134 and baseline_transform_policies.h:117-149.
-__global__ void noalloc_facet_table_kernel(FacetXform *out, const vis_real *centres, int nf, double ra0, double dec0) {
+__global__ void noalloc_facet_table_kernel(FacetXform *out, const vis_real *centres, int nf, double ra0, double dec0,
+                                           int nx, int ny, double u_scale, double v_scale, double gcx, double gcy,
+                                           long long facet_elems) {
   int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
   const double k = (double)kArcsecToRad;
@@ -59,6 +61,13 @@ __global__ void noalloc_facet_table_kernel(FacetXform *out, const vis_real *cent
   x.dl = -c_n * s_d_ra;
   x.dm = -(s_n * c_o - c_n * s_o * c_d_ra);
   x.dn = 1.0 - sqrt(1.0 - x.dl * x.dl - x.dm * x.dm);
+  x.nx = nx;
+  x.ny = ny;
+  x.u_scale = u_scale;
+  x.v_scale = v_scale;
+  x.gcx = gcx;
+  x.gcy = gcy;
+  x.grid_base = (long long)f * facet_elems;
   out[f] = x;
 }
 
@@ -211,9 +220,11 @@ extern "C" int bullseye_facet_4_cor_corrections_noalloc(const gridding_parameter
   if (cudaMemsetAsync(lo, 0, grid_elems * sizeof(vis_complex), st) != cudaSuccess) return BZ_ERR_CUDA;
 #endif
   if (cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess) return BZ_ERR_CUDA;
-  noalloc_facet_table_kernel<<<(unsigned)((F + 127) / 128), 128, 0, st>>>(table, p.facet_centres, (int)F,
-                                                                          (double)p.phase_centre_ra,
-                                                                          (double)p.phase_centre_dec);
+  noalloc_facet_table_kernel<<<(unsigned)((F + 127) / 128), 128, 0, st>>>(
+      table, p.facet_centres, (int)F, (double)p.phase_centre_ra, (double)p.phase_centre_dec, (int)p.nx, (int)p.ny,
+      (double)p.nx * (double)p.cell_size_x * (double)kArcsecToRad,
+      -((double)p.ny * (double)p.cell_size_y * (double)kArcsecToRad), (double)(p.nx / 2 - p.conv_support),
+      (double)(p.ny / 2 - p.conv_support), (long long)(p.cube_channel_dim_size * 4 * nxy));
   const long long nj = (long long)(p.no_timestamps_read * p.antenna_count * F * p.spw_count * p.channel_count);
   if (nj > 0) noalloc_invert_kernel<<<(unsigned)((nj + 255) / 256), 256, 0, st>>>(p.jones_terms, nj, err);
   if (p.row_count == 0) return BZ_OK;
