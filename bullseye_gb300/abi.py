@@ -134,3 +134,11 @@ def bind_exports(lib, extra_double=(), extra_int=()):
             fn.restype = None
             fn.argtypes = [c_void_p]
     return lib
+
+
+class BullseyeFacet(ctypes.Structure):
+    """One facet of an uneven layout for ``bullseye_grid_batched_facets`` (include/bullseye_gb300.h):
+    centre and cell sizes in arcsec, grid size, and the complex-element offset of its
+    [cube][4][ny][nx] block in the caller's grid buffer."""
+    _fields_ = [("ra", c_double), ("dec", c_double), ("cell_x", c_double), ("cell_y", c_double),
+                ("nx", c_size_t), ("ny", c_size_t), ("grid_offset", c_size_t)]

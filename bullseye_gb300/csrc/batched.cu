@@ -196,6 +196,7 @@ struct BatchedState {
   DevBuf<unsigned char> row_class;
   DevBuf<int> nseg, seg_off, seg_total, class_count, class_off, class_cursor, work_next, sample_count;
   DevBuf<int4> segs, sorted;
+  DevBuf<FacetXform> facet_table;  // per-facet geometry of bullseye_grid_batched_facets
   size_t rows_cap = 0, tracks_cap = 0, segs_cap = 0;
   // tuning decisions, by (class width, NC, WPROJ, COMP)
   std::map<std::tuple<int, int, int, int>, std::pair<int, int>> tuned;
@@ -464,8 +465,8 @@ bool dispatch(const GridArgs &va, const GridArgs *sa, int nfacets, bool tune, co
 }
 
 bool run_dispatch(const GridArgs &va, const GridArgs *sa, bool wproj, bool comp, bool tune, const std::vector<int> &counts,
-                  cudaStream_t st) {
-  const int F = (int)g_ctx.F;
+                  cudaStream_t st, int nfacets = -1) {
+  const int F = nfacets > 0 ? nfacets : (int)g_ctx.F;
 #if defined(BULLSEYE_SINGLE)
   if (comp) return wproj ? dispatch<true, true>(va, sa, F, tune, counts, st) : dispatch<false, true>(va, sa, F, tune, counts, st);
 #else
@@ -504,7 +505,7 @@ void bz_release_batched() {
   b.key.clear();
   b.plane_class.release(); b.plane_lo.release(); b.row_class.release(); b.nseg.release(); b.seg_off.release();
   b.seg_total.release(); b.class_count.release(); b.class_off.release(); b.class_cursor.release();
-  b.work_next.release(); b.sample_count.release(); b.segs.release(); b.sorted.release();
+  b.work_next.release(); b.sample_count.release(); b.segs.release(); b.sorted.release(); b.facet_table.release();
   b.rows_cap = b.tracks_cap = b.segs_cap = 0;
   b.planned = false;
   b.ncls = 0;
@@ -535,6 +536,83 @@ extern "C" int bullseye_batched_profile(int *width, int *nc, int *J, int *wide, 
   return (int)r.size();
 }
 
+namespace {
+
+// Runs one batched call: builds the schedule on the device, on first use tunes every support class
+// (tuning launches use `ta` over `tune_facets` facets and grid into the library's scratch grid),
+// then replays the call as a CUDA graph keyed on the launch arguments; eager with per-class events
+// in profiling mode.
+int run_batched(const GridArgs &va, const GridArgs *sa, int nfacets, const GridArgs &ta, int tune_facets, bool wproj,
+                bool comp, const char *name) {
+  Context &c = g_ctx;
+  BatchedState &b = g_bs;
+  const bool sf = sa != nullptr;
+  // graph key: everything the captured launches read by value
+  std::vector<unsigned char> key(sizeof(GridArgs) * 2 + 16);
+  std::memcpy(key.data(), &va, sizeof(GridArgs));
+  if (sf) std::memcpy(key.data() + sizeof(GridArgs), sa, sizeof(GridArgs));
+  key[sizeof(GridArgs) * 2] = (unsigned char)sf;
+  key[sizeof(GridArgs) * 2 + 1] = (unsigned char)comp;
+  std::memcpy(key.data() + sizeof(GridArgs) * 2 + 4, &nfacets, sizeof(int));
+
+  auto schedule_counts = [&](std::vector<int> &counts) -> bool {
+    if (!enqueue_schedule(va, c.stream)) return false;
+    BZ_CUDA_TRY_RET(cudaMemcpyAsync(counts.data(), b.class_count.ptr, sizeof(int) * kMaxClasses, cudaMemcpyDeviceToHost,
+                                    c.stream), false);
+    BZ_CUDA_TRY_RET(cudaStreamSynchronize(c.stream), false);
+    return true;
+  };
+  if (b.profile) {
+    std::vector<int> counts(kMaxClasses, 0);
+    if (!schedule_counts(counts)) return bz_error_code() ? bz_error_code() : BZ_ERR_CUDA;
+    if (!run_dispatch(ta, sa, wproj, comp, true, counts, c.stream, tune_facets)) return bz_error_code();
+    b.records.clear();
+    if (!run_dispatch(va, sa, wproj, comp, false, counts, c.stream, nfacets)) return bz_error_code();
+    return BZ_OK;
+  }
+  if (!b.exec || key != b.key) {
+    // first run of this configuration: build the schedule eagerly, tune each class, then capture
+    std::vector<int> counts(kMaxClasses, 0);
+    if (!schedule_counts(counts)) return bz_error_code() ? bz_error_code() : BZ_ERR_CUDA;
+    if (!run_dispatch(ta, sa, wproj, comp, true, counts, c.stream, tune_facets)) return bz_error_code();
+    if (b.exec) cudaGraphExecDestroy(b.exec);
+    b.exec = nullptr;
+    cudaGraph_t graph;
+    BZ_CUDA_TRY_RET(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal), BZ_ERR_CUDA);
+    const long long launches0 = c.launches;
+    bool ok = enqueue_schedule(va, c.stream) && run_dispatch(va, sa, wproj, comp, false, counts, c.stream, nfacets);
+    cudaError_t ce = cudaStreamEndCapture(c.stream, &graph);
+    if (!ok || ce != cudaSuccess) {
+      bz_record_error(BZ_ERR_CUDA, "%s: graph capture failed (%s)", name, cudaGetErrorString(ce));
+      return BZ_ERR_CUDA;
+    }
+    c.launches = launches0;  // counted again when the graph is launched
+    ce = cudaGraphInstantiate(&b.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) {
+      bz_record_error(BZ_ERR_CUDA, "%s: graph instantiation failed (%s)", name, cudaGetErrorString(ce));
+      return BZ_ERR_CUDA;
+    }
+    b.key = key;
+  }
+  BZ_CUDA_TRY_RET(cudaGraphLaunch(b.exec, c.stream), BZ_ERR_CUDA);
+  c.launches += 6 + (long long)b.ncls * (sf ? 2 : 1);
+  return BZ_OK;
+}
+
+bool call_mode(int call, int &mode, bool &faceting, const char *name) {
+  switch (call) {
+    case 0: mode = CORR_QUAD_JONES; faceting = true; return true;  // facet_4_cor_corrections
+    case 1: mode = CORR_QUAD; faceting = true; return true;        // facet_4_cor
+    case 2: mode = CORR_QUAD; faceting = false; return true;       // grid_4_cor
+    default:
+      bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: unknown call %d", name, call);
+      return false;
+  }
+}
+
+}  // namespace
+
 // See include/bullseye_gb300.h.
 extern "C" int bullseye_grid_batched(gridding_parameters *pp, int call, int with_sampling) {
   if (!bz_check_ready("bullseye_grid_batched")) return bz_error_code() ? bz_error_code() : BZ_ERR_NOT_INITIALISED;
@@ -543,14 +621,7 @@ extern "C" int bullseye_grid_batched(gridding_parameters *pp, int call, int with
   BatchedState &b = g_bs;
   int mode;
   bool faceting;
-  switch (call) {
-    case 0: mode = CORR_QUAD_JONES; faceting = true; break;   // facet_4_cor_corrections
-    case 1: mode = CORR_QUAD; faceting = true; break;         // facet_4_cor
-    case 2: mode = CORR_QUAD; faceting = false; break;        // grid_4_cor
-    default:
-      bz_record_error(BZ_ERR_INVALID_ARGUMENT, "bullseye_grid_batched: unknown call %d", call);
-      return BZ_ERR_INVALID_ARGUMENT;
-  }
+  if (!call_mode(call, mode, faceting, "bullseye_grid_batched")) return BZ_ERR_INVALID_ARGUMENT;
   if (c.C != 4) {
     bz_record_error(BZ_ERR_UNSUPPORTED, "bullseye_grid_batched grids 4 correlations");
     return BZ_ERR_UNSUPPORTED;
@@ -567,67 +638,91 @@ extern "C" int bullseye_grid_batched(gridding_parameters *pp, int call, int with
   }
   if (!b.planned && !plan_classes()) return bz_error_code() ? bz_error_code() : BZ_ERR_CUDA;
   if (!ensure_capacity(p.row_count, (size_t)nslots * c.nchan)) return bz_error_code();
-  const bool wproj = p.wplanes > 1;
-  const bool comp = va.grid_lo != nullptr;
-
-  // graph key: everything the captured launches read by value
-  std::vector<unsigned char> key(sizeof(GridArgs) * 2 + 8);
-  std::memcpy(key.data(), &va, sizeof(GridArgs));
-  if (sf) std::memcpy(key.data() + sizeof(GridArgs), &sa, sizeof(GridArgs));
-  key[sizeof(GridArgs) * 2] = (unsigned char)sf;
-  key[sizeof(GridArgs) * 2 + 1] = (unsigned char)comp;
-
-  if (b.profile) {
-    // eager run with a CUDA event pair around every class launch (no graph)
-    if (!enqueue_schedule(va, c.stream)) return bz_error_code();
-    std::vector<int> counts(kMaxClasses, 0);
-    BZ_CUDA_TRY_RET(cudaMemcpyAsync(counts.data(), b.class_count.ptr, sizeof(int) * kMaxClasses, cudaMemcpyDeviceToHost,
-                                    c.stream), BZ_ERR_CUDA);
-    BZ_CUDA_TRY_RET(cudaStreamSynchronize(c.stream), BZ_ERR_CUDA);
-    if (!run_dispatch(va, sf ? &sa : nullptr, wproj, comp, true, counts, c.stream)) return bz_error_code();
-    b.records.clear();
-    if (!run_dispatch(va, sf ? &sa : nullptr, wproj, comp, false, counts, c.stream)) return bz_error_code();
-    if (p.is_final_data_chunk) {
-      bz_copy_back_grids(p, false);
-      if (sf) bz_copy_back_grids(p, true);
-    }
-    bz_timer_stop();
-    return bz_error_code();
-  }
-  if (!b.exec || key != b.key) {
-    // first run of this configuration: build the schedule eagerly, tune each class, then capture
-    if (!enqueue_schedule(va, c.stream)) return bz_error_code();
-    std::vector<int> counts(kMaxClasses, 0);
-    BZ_CUDA_TRY_RET(cudaMemcpyAsync(counts.data(), b.class_count.ptr, sizeof(int) * kMaxClasses, cudaMemcpyDeviceToHost,
-                                    c.stream), BZ_ERR_CUDA);
-    BZ_CUDA_TRY_RET(cudaStreamSynchronize(c.stream), BZ_ERR_CUDA);
-    if (!run_dispatch(va, sf ? &sa : nullptr, wproj, comp, true, counts, c.stream)) return bz_error_code();
-    if (b.exec) cudaGraphExecDestroy(b.exec);
-    b.exec = nullptr;
-    cudaGraph_t graph;
-    BZ_CUDA_TRY_RET(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal), BZ_ERR_CUDA);
-    const long long launches0 = c.launches;
-    bool ok = enqueue_schedule(va, c.stream) && run_dispatch(va, sf ? &sa : nullptr, wproj, comp, false, counts, c.stream);
-    cudaError_t ce = cudaStreamEndCapture(c.stream, &graph);
-    if (!ok || ce != cudaSuccess) {
-      bz_record_error(BZ_ERR_CUDA, "bullseye_grid_batched: graph capture failed (%s)", cudaGetErrorString(ce));
-      return BZ_ERR_CUDA;
-    }
-    c.launches = launches0;  // counted again when the graph is launched
-    ce = cudaGraphInstantiate(&b.exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (ce != cudaSuccess) {
-      bz_record_error(BZ_ERR_CUDA, "bullseye_grid_batched: graph instantiation failed (%s)", cudaGetErrorString(ce));
-      return BZ_ERR_CUDA;
-    }
-    b.key = key;
-  }
-  BZ_CUDA_TRY_RET(cudaGraphLaunch(b.exec, c.stream), BZ_ERR_CUDA);
-  c.launches += 6 + (long long)b.ncls * (sf ? 2 : 1);
+  const int rc = run_batched(va, sf ? &sa : nullptr, (int)c.F, va, (int)c.F, p.wplanes > 1, va.grid_lo != nullptr,
+                             "bullseye_grid_batched");
+  if (rc != BZ_OK) return rc;
   if (p.is_final_data_chunk) {
     bz_copy_back_grids(p, false);
     if (sf) bz_copy_back_grids(p, true);
   }
+  bz_timer_stop();
+  return bz_error_code();
+}
+
+// See include/bullseye_gb300.h.
+extern "C" int bullseye_grid_batched_facets(gridding_parameters *pp, const bullseye_facet *facets, int nfacets,
+                                            const unsigned char *row_mask, void *grids, void *grid_lo, double *norms,
+                                            int call) {
+  const char *name = "bullseye_grid_batched_facets";
+  if (!bz_check_ready(name)) return bz_error_code() ? bz_error_code() : BZ_ERR_NOT_INITIALISED;
+  gridding_parameters &p = *pp;
+  Context &c = g_ctx;
+  BatchedState &b = g_bs;
+  int mode;
+  bool faceting;
+  if (!call_mode(call, mode, faceting, name)) return BZ_ERR_INVALID_ARGUMENT;
+  if (!facets || nfacets <= 0 || !grids || !norms) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: facets, grids and norms are required", name);
+    return BZ_ERR_INVALID_ARGUMENT;
+  }
+  if (c.C != 4) {
+    bz_record_error(BZ_ERR_UNSUPPORTED, "%s grids 4 correlations", name);
+    return BZ_ERR_UNSUPPORTED;
+  }
+  if (call == 0 && (size_t)nfacets != c.F) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: Jones terms are laid out for %zu facets, not %d", name, c.F, nfacets);
+    return BZ_ERR_INVALID_ARGUMENT;
+  }
+  const long long s = (long long)p.conv_support;
+  for (int f = 0; f < nfacets; ++f) {
+    const bullseye_facet &d = facets[f];
+    if (d.nx < (size_t)(2 * s + 4) || d.ny < (size_t)(2 * s + 4) || d.nx > (1u << 20) || d.ny > (1u << 20)) {
+      bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: facet %d has a %zu x %zu grid", name, f, d.nx, d.ny);
+      return BZ_ERR_INVALID_ARGUMENT;
+    }
+  }
+  bz_timer_start();
+  GridArgs va;
+  int nslots = 0;
+  if (!bz_prepare_grid_args(p, 4, mode, faceting, va, nslots, name)) return bz_error_code();
+  if (p.row_count == 0) {
+    bz_timer_stop();
+    return BZ_OK;
+  }
+  // tuning runs on facet 0 of the library's own layout, into its scratch grid
+  const GridArgs ta = va;
+  std::vector<FacetXform> fx(nfacets);
+  const double ra0 = (double)p.phase_centre_ra, dec0 = (double)p.phase_centre_dec;
+  for (int f = 0; f < nfacets; ++f) {
+    const bullseye_facet &d = facets[f];
+    fx[f] = bz_facet_xform(ra0, dec0, faceting ? d.ra : ra0, faceting ? d.dec : dec0, faceting, faceting);
+    fx[f].nx = (int)d.nx;
+    fx[f].ny = (int)d.ny;
+    fx[f].u_scale = (double)d.nx * d.cell_x * (double)kArcsecToRad;
+    fx[f].v_scale = -((double)d.ny * d.cell_y * (double)kArcsecToRad);
+    fx[f].gcx = (double)((long long)(d.nx / 2) - s);
+    fx[f].gcy = (double)((long long)(d.ny / 2) - s);
+    fx[f].grid_base = (long long)d.grid_offset;
+  }
+  if (b.facet_table.n < (size_t)nfacets && !b.facet_table.alloc(nfacets)) return bz_error_code();
+  BZ_CUDA_TRY_RET(cudaMemcpyAsync(b.facet_table.ptr, fx.data(), sizeof(FacetXform) * nfacets, cudaMemcpyHostToDevice,
+                                  c.stream), BZ_ERR_CUDA);
+  va.facets = b.facet_table.ptr;
+  va.nfacets_total = nfacets;
+  va.facet_base = 0;
+  va.facet_row_mask = row_mask;
+  va.grid = static_cast<vis_complex *>(grids);
+  va.grid_lo = nullptr;
+#if defined(BULLSEYE_SINGLE)
+  va.grid_lo = static_cast<vis_complex *>(grid_lo);
+#else
+  (void)grid_lo;
+#endif
+  va.norm = norms;
+  if (!b.planned && !plan_classes()) return bz_error_code() ? bz_error_code() : BZ_ERR_CUDA;
+  if (!ensure_capacity(p.row_count, (size_t)nslots * c.nchan)) return bz_error_code();
+  const int rc = run_batched(va, nullptr, nfacets, ta, 1, p.wplanes > 1, va.grid_lo != nullptr, name);
+  if (rc != BZ_OK) return rc;
   bz_timer_stop();
   return bz_error_code();
 }

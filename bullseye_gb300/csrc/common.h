@@ -129,3 +129,15 @@ int bz_error_code();
       return ret;                                                                          \
     }                                                                                      \
   } while (0)
+
+// One facet of an uneven layout (bullseye_grid_batched_facets): centre and cell size in arcsec,
+// grid size, and the complex-element offset of its [cube][4][ny][nx] block in the caller's grids.
+extern "C" {
+struct bullseye_facet {
+  double ra, dec;
+  double cell_x, cell_y;
+  size_t nx, ny;
+  size_t grid_offset;
+};
+}
+static_assert(sizeof(bullseye_facet) == 56, "bullseye_facet layout");

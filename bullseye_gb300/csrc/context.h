@@ -98,6 +98,8 @@ extern Context g_ctx;
 // helpers defined in imaging_lib.cu
 bool bz_check_ready(const char *fn);
 void bz_copy_back_grids(gridding_parameters &p, bool sampling);
+// Phase-rotation and uv-transform constants of a facet centred at (ra, dec), arcsec (FP64, host).
+FacetXform bz_facet_xform(double ra0, double dec0, double ra, double dec, bool phase, bool uvx);
 void bz_timer_start();
 void bz_timer_stop();
 bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool faceting, GridArgs &a,

@@ -450,7 +450,7 @@ extern "C" void repack_input_data(gridding_parameters *pp) {
 }
 
 // ---------------------------------------------------------------- gridding launch
-static FacetXform facet_xform(double ra0, double dec0, double ra, double dec, bool phase, bool uvx) {
+FacetXform bz_facet_xform(double ra0, double dec0, double ra, double dec, bool phase, bool uvx) {
   // phase_transform_policies.h:110-134 and baseline_transform_policies.h:117-149, in FP64
   FacetXform x;
   std::memset(&x, 0, sizeof x);
@@ -727,7 +727,7 @@ bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool f
     }
     // the sampling-function policy reports the phase centre as facet centre
     // (phase_transform_policies.h:77-82), so its uv transform is the identity
-    fx[f] = facet_xform(ra0, dec0, ra, dec, phase, faceting);
+    fx[f] = bz_facet_xform(ra0, dec0, ra, dec, phase, faceting);
     // every facet shares the library's grid size: u_scale = nx * cell * ARCSEC_TO_RAD,
     // v_scale = -(ny * cell * ARCSEC_TO_RAD) (templated_gridder.h:23-24)
     fx[f].nx = (int)c.nx;

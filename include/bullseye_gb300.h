@@ -24,6 +24,16 @@ extern "C" {
 
 typedef struct gridding_parameters gridding_parameters;
 
+/* One facet of an uneven facet layout (bullseye_grid_batched_facets): centre (ra, dec) and cell
+ * sizes in arcsec, grid size, and the offset in complex elements of the facet's [cube][4][ny][nx]
+ * block within the caller's grid buffer. */
+typedef struct bullseye_facet {
+  double ra, dec;
+  double cell_x, cell_y;
+  size_t nx, ny;
+  size_t grid_offset;
+} bullseye_facet;
+
 /* ---- reference entry points (bullseye/mo/cpu_gpu_common/wrapper.h:41-61) ---- */
 
 /* Seconds of device time spent in gridding calls (wrapper.cu:73-75, gpu_algorithm/timer.h). */
@@ -108,6 +118,23 @@ double bullseye_fp32_fma_tflops(int iters);
  * after its first use (layouts per support class are picked by timing on that first use).
  * Returns 0 or the error code (also reported by bullseye_last_error). */
 int bullseye_grid_batched(gridding_parameters *params, int call, int with_sampling);
+/* Batched gridding of facets of UNEVEN sizes and cell sizes, each with its own rows: the same
+ * support-aware persistent schedule and graph replay as bullseye_grid_batched, over `nfacets`
+ * facets described by `facets` (host array), accumulated into CALLER-OWNED device buffers:
+ * grids (complex, each facet's block at its grid_offset), grid_lo (the 32-bit library's
+ * compensation buffer, same size as grids and zeroed by the caller, or null for plain FP32
+ * accumulation; a cell's value is then grids + grid_lo; ignored by the 64-bit library) and norms
+ * (float64 [nfacets][cube][4]).  Work is queued on the library stream (bullseye_get_stream).
+ * row_mask, if not null, is a device array [nfacets][row_count] of bytes: 0 leaves that row out of
+ * that facet (the facet then sees fewer visibilities).  `call` 1 grids like facet_4_cor, 2 like
+ * grid_4_cor, 0 like facet_4_cor_corrections (then nfacets must equal the facet count given to
+ * initLibrary, which lays out the Jones terms).  Tables (kernel, wavelengths, channels) and rows
+ * come from params as for the other gridding calls, after initLibrary; the library's own grids
+ * are not touched and nothing is copied back.  The sampling function is not gridded.  No
+ * counterpart in the reference (its ABI has one grid size for every facet). */
+int bullseye_grid_batched_facets(gridding_parameters *params, const bullseye_facet *facets, int nfacets,
+                                 const unsigned char *row_mask, void *grids, void *grid_lo, double *norms,
+                                 int call);
 /* Profiling mode of bullseye_grid_batched (off by default): when on, each call runs eagerly (no
  * graph) with a CUDA event pair around every support-class launch, synchronising after each. */
 void bullseye_set_batched_profiling(int on);
