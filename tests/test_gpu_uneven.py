@@ -99,7 +99,7 @@ def test_uneven_facets_match_per_facet_calls(precision, call, wplanes, gpu_requi
     for f, (n, cf) in enumerate(SIZES):
         pf = replace(p, nx=n, ny=n, cell_x=p.cell_x * cf, cell_y=p.cell_y * cf,
                      facet_centres=p.facet_centres[f:f + 1], flagged_rows=p.flagged_rows | ~masks[f])
-        refs.append(run_imaging(lib, pf, call, keep_raw=True))
+        refs.append(run_imaging(lib, pf, call, keep_raw=True, norm_bins=(2 * p.conv_support + 1) ** 2))
         check(lib)
     # one batched call over the uneven layout
     keep = []
