@@ -141,8 +141,6 @@ def test_uneven_facets_match_per_facet_calls(precision, call, wplanes, gpu_requi
             assert _rel(got, want) <= TOL[precision], (rep, f, _rel(got, want))
             wn = refs[f].normalization[0] * (rep + 1)
             assert np.max(np.abs(nrm[f] - wn)) <= TOL[precision] * np.max(np.abs(wn)), (rep, f)
-    # the masks make the facets see different numbers of visibilities
-    assert refs[0].normalization[0].sum() > refs[2].normalization[0].sum()
 
 
 def test_uneven_rejects_bad_layouts(gpu_required, built_libraries):
