@@ -70,6 +70,8 @@ def parse():
     ap.add_argument("--no-other", action="store_true", help="skip timing the other form")
     ap.add_argument("--facets", type=int, default=0, help="override the facet count (profiling cases)")
     ap.add_argument("--no-precision", action="store_true", help="skip the per-facet FP32 error report")
+    ap.add_argument("--workload", default="facets16", choices=["facets16", "uneven"],
+                    help="facets16: the 16-facet Jones workload (default); uneven: 96 facets of uneven sizes and masks")
     ap.add_argument("--no-class-profile", action="store_true",
                     help="skip the eager, per-support-class timed step after the timed region")
     ap.add_argument("--eager", action="store_true",
@@ -418,9 +420,148 @@ def precision_report():
     return out
 
 
+# ----------------------------------------------------------------------------- uneven facets
+UNEVEN_FACETS, UNEVEN_TIMES, UNEVEN_PLANES = 96, 2226, 128
+
+
+def uneven_layout(seed=21):
+    """96 facets with sizes log-uniform in [256, 4096] (multiples of 64), 5 arcsec cells, centres
+    within 3 deg, and per-facet row masks dropping a fraction in [0, 0.6] of the rows through
+    whole baselines and whole time ranges."""
+    rng = np.random.default_rng(seed)
+    sizes = (np.exp(rng.uniform(np.log(256), np.log(4096), UNEVEN_FACETS)) // 64 * 64).astype(np.int64)
+    sizes = np.clip(sizes, 256, 4096)
+    lim = np.deg2rad(3.0)
+    return sizes, rng.uniform(-lim, lim, UNEVEN_FACETS), rng.uniform(-lim, lim, UNEVEN_FACETS), \
+        rng.uniform(0.0, 0.6, UNEVEN_FACETS)
+
+
+def uneven_masks(geo, fracs, seed=22):
+    """[F][R] uint8 masks: each facet drops baselines and time ranges until about `frac` of its rows go."""
+    from bullseye_gb300.imaging import baseline_index
+    rng = np.random.default_rng(seed)
+    b = baseline_index(geo["a1"], geo["a2"], N_ANT)
+    t = np.asarray(geo["tid"], np.int64)
+    T = int(t.max()) + 1
+    nb = int(b.max()) + 1
+    out = np.ones((len(fracs), b.size), np.uint8)
+    for f, frac in enumerate(fracs):
+        drop_b = rng.uniform(0, 1, nb) < frac / 2                  # half the loss from whole baselines
+        t0 = int(rng.integers(0, T))
+        span = int(T * frac / 2)                                   # the other half from one time range
+        drop_t = ((t - t0) % T) < span
+        out[f] = ~(drop_b[b] | drop_t)
+    return out
+
+
+def uneven_main(args):
+    """The batching form on an uneven layout: one bullseye_grid_batched_facets call per step over 96
+    facets of different sizes with different row masks, w-projection with 128 planes."""
+    global N_FACETS, WPLANES, NX
+    import torch
+    from bullseye_gb300.abi import BullseyeFacet, gridding_parameters_type
+    from bullseye_gb300.library import check, load_library
+    N_FACETS, WPLANES = 1, UNEVEN_PLANES
+    torch.cuda.set_device(0)
+    geo = geometry(UNEVEN_TIMES)
+    conv, supports = kernel_stack(geo["wmax"])  # w kernels for a 1024-pixel field
+    NX = 256  # the library's own grid only hosts the tuner
+    R = geo["uvw"].shape[0]
+    sizes, fl, fm, fracs = uneven_layout()
+    masks = uneven_masks(geo, fracs)
+    kept_rows = masks.sum(axis=1).astype(np.int64)
+    pairs_per_step = int(kept_rows.sum()) * N_CHAN
+    dec = geo["dec0"] * np.pi / (180 * 3600)
+    facets = (BullseyeFacet * UNEVEN_FACETS)()
+    off = 0
+    for f in range(UNEVEN_FACETS):
+        ra_as = fl[f] / np.cos(dec) * 180 * 3600 / np.pi
+        dec_as = geo["dec0"] + fm[f] * 180 * 3600 / np.pi
+        n = int(sizes[f])
+        facets[f] = BullseyeFacet(float(ra_as), float(dec_as), CELL, CELL, n, n, off)
+        off += 4 * n * n
+    lib = load_library("GPU", "single")
+    d = device_inputs(geo, torch)
+    grids = torch.zeros(off, dtype=torch.complex64, device="cuda")
+    lo = torch.zeros(off, dtype=torch.complex64, device="cuda")
+    norms = torch.zeros(UNEVEN_FACETS * 4, dtype=torch.float64, device="cuda")
+    mask_dev = torch.as_tensor(masks, device="cuda")
+    torch.cuda.synchronize()
+    tab = Tables(geo, conv)
+    st = gridding_parameters_type("single")()
+    tab.fill(st, geo, R)
+    st.should_grid_sampling_function = False
+    lib.bullseye_set_device_inputs(1)
+    lib.bullseye_set_compensated(0 if args.no_comp else 1)
+    lib.initLibrary(ctypes.byref(st))
+    check(lib)
+    set_rows(st, d, lambda t: ctypes.c_void_p(t.data_ptr()))
+    st.is_final_data_chunk = False
+    stream = torch.cuda.ExternalStream(lib.bullseye_get_stream())
+    lo_ptr = None if args.no_comp else ctypes.c_void_p(lo.data_ptr())
+
+    def step():
+        rc = lib.bullseye_grid_batched_facets(ctypes.byref(st), ctypes.cast(facets, ctypes.c_void_p), UNEVEN_FACETS,
+                                              ctypes.c_void_p(mask_dev.data_ptr()), ctypes.c_void_p(grids.data_ptr()),
+                                              lo_ptr, ctypes.c_void_p(norms.data_ptr()), 1)
+        if rc:
+            check(lib)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    check(lib)
+    lib.bullseye_reset_counters()
+    clocks = ClockSampler(os.path.join(REPO, "gpurun_out", "clocks.csv") if os.path.isdir(os.path.join(REPO, "gpurun_out"))
+                          else "/tmp/bullseye_clocks.csv")
+    clocks.start()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    clk = clocks.stop()
+    launches = int(lib.bullseye_kernel_launches())
+    check(lib)
+    fp32_peak = lib.bullseye_fp32_fma_tflops(4096)
+    # algorithmic flops on each visibility's true w-plane support, over the rows each facet keeps
+    w = np.abs(geo["uvw"][:, 2])
+    true_taps = 0.0
+    sup2 = np.asarray(supports, np.float64) ** 2
+    for lam in geo["lam"]:
+        pl = np.clip(np.rint(w / lam * ((WPLANES - 1) / geo["wmax"])).astype(np.int64), 0, WPLANES - 1)
+        true_taps += float((masks.astype(np.float64) @ sup2[pl]).sum())
+    step_flops = true_taps * 8 * 4 + pairs_per_step * (6 * 4)
+    achieved = step_flops / (ms * 1e-3) / 1e12
+    lib.releaseLibrary()
+    lib.bullseye_set_device_inputs(0)
+    value = pairs_per_step / (ms * 1e-3) / 1e6
+    line = {"metric": "gridded Mvis/s (vis x facet pairs)", "value": value, "unit": "Mvis/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"uneven facets: {UNEVEN_FACETS} facets of {int(sizes.min())}^2..{int(sizes.max())}^2 "
+                                   f"(log-uniform), 5 arcsec cells, per-facet row masks dropping 0-60% of rows, "
+                                   f"27 ant x {UNEVEN_TIMES} t x {N_CHAN} ch ({R * N_CHAN / 1e6:.1f}M vis), w-proj "
+                                   f"{WPLANES} planes support {MIN_SUPPORT}-{2 * S_HALF + 1}, facet_4_cor, compensated FP32",
+                       "facet_vis_min": int(kept_rows.min()) * N_CHAN, "facet_vis_max": int(kept_rows.max()) * N_CHAN,
+                       "grid_cells": off, "vis_facet_pairs_per_step": pairs_per_step,
+                       "form": "bullseye_grid_batched_facets (persistent per-class launches, CUDA graph replay)"},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                         "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
+                         "peak_source": "measured FP32 FMA probe on this GPU"},
+            "clocks": clk, "gpu_launches": launches, "e2e": None, "cpu_baseline": None}
+    print(json.dumps(line))
+
+
 # ----------------------------------------------------------------------------- main
 def main():
     args = parse()
+    if args.workload == "uneven":
+        return uneven_main(args)
     global N_CHAN, N_FACETS
     if args.chans:
         N_CHAN = args.chans
