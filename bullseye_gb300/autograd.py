@@ -5,8 +5,8 @@
 planar uv transform, Romein gridding with the AA or w-projection kernel:
 bullseye/mo/cpu_gpu_common/wrapper.cu:988-1150 and the CPU policies it mirrors,
 correlation_gridding_policies.h:503-542, phase_transform_policies.h:110-134,
-baseline_transform_policies.h:117-149).  The forward pass runs the library's allocation-free entry
-point on torch's current stream; the backward pass runs the library's adjoint (degridding) kernel
+baseline_transform_policies.h:117-149).  The forward pass runs the library's workspace entry point
+(bullseye_facet_4_cor_corrections_ws, with a torch-allocated workspace) on torch's current stream; the backward pass runs the library's adjoint (degridding) kernel
 and returns dL/dV and dL/dJ in PyTorch's complex-gradient convention (dL = Re sum conj(g) dz).
 
 Both passes are the CUDA library: there is no PyTorch or CPU implementation here, and a missing
@@ -161,10 +161,13 @@ class _FacetGrid(torch.autograd.Function):
         norm = torch.zeros(geom.grid_shape[:3], dtype=torch.float64, device=vis.device)
         work = jones.detach().clone()  # the entry point inverts the terms in place
         st = geom.struct(vis.detach(), work, grid, norm)
-        rc = lib.bullseye_facet_4_cor_corrections_noalloc(ctypes.byref(st), _stream())
+        nbytes = int(lib.bullseye_facet_4_cor_corrections_ws_bytes(ctypes.byref(st)))
+        ws = torch.empty(nbytes + 256, dtype=torch.uint8, device=vis.device)
+        aligned = (ws.data_ptr() + 255) // 256 * 256
+        rc = lib.bullseye_facet_4_cor_corrections_ws(ctypes.byref(st), ctypes.c_void_p(aligned), nbytes, _stream())
         if rc != 0:
             check(lib)
-            raise ImagingError(f"bullseye_facet_4_cor_corrections_noalloc failed with status {rc}")
+            raise ImagingError(f"bullseye_facet_4_cor_corrections_ws failed with status {rc}")
         ctx.geom = geom
         ctx.save_for_backward(vis, jones)
         ctx.mark_non_differentiable(norm)

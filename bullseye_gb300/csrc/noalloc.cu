@@ -163,23 +163,19 @@ bool noalloc_dispatch(GridArgs a, long long blocks, cudaStream_t st) {
 
 }  // namespace
 
-// See include/bullseye_gb300.h.  Every pointer in *params is a device pointer; returns 0 when
-// the work was queued on `stream`, or a bz_status code (nothing queued) when the arguments are
-// rejected.  The first call on each device resolves the scratch array's device address
-// (cudaGetSymbolAddress) and should therefore come before any stream capture on that device.
-extern "C" int bullseye_facet_4_cor_corrections_noalloc(const gridding_parameters *params, void *stream) {
-  if (!params) return BZ_ERR_INVALID_ARGUMENT;
-  const gridding_parameters &p = *params;
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= BZ_NOALLOC_MAX_DEVICES) return BZ_ERR_CUDA;
-  if (!g_noalloc_addr[dev]) {
-    void *ptr = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-    if (e != cudaSuccess || !ptr) return BZ_ERR_CUDA;
-    g_noalloc_addr[dev] = ptr;
-  }
-  unsigned char *scratch = static_cast<unsigned char *>(g_noalloc_addr[dev]);
+namespace {
 
+// Device scratch of one gridding call: the compensation grid (single precision), the facet table
+// and an error word, with the capacities the call checks its sizes against.
+struct Workspace {
+  vis_complex *lo;
+  size_t lo_bytes;
+  FacetXform *table;
+  size_t table_bytes;
+  int *err;
+};
+
+int grid_4cor_jones(const gridding_parameters &p, const Workspace &ws, void *stream) {
   const size_t F = p.num_facet_centres ? p.num_facet_centres : 1;
   const size_t nxy = p.nx * p.ny;
   const size_t grid_elems = F * p.cube_channel_dim_size * 4 * nxy;
@@ -195,7 +191,7 @@ extern "C" int bullseye_facet_4_cor_corrections_noalloc(const gridding_parameter
       p.cube_channel_dim_size == 0)
     return BZ_ERR_INVALID_ARGUMENT;
 #if defined(BULLSEYE_SINGLE)
-  if (grid_elems * sizeof(vis_complex) > BZ_NOALLOC_LO_BYTES) {
+  if (grid_elems * sizeof(vis_complex) > ws.lo_bytes) {
     bz_record_error(BZ_ERR_UNSUPPORTED,
                     "bullseye_facet_4_cor_corrections_noalloc: %zu grid cells need %zu bytes of compensation scratch, "
                     "more than the fixed %u-byte scratch array",
@@ -203,7 +199,7 @@ extern "C" int bullseye_facet_4_cor_corrections_noalloc(const gridding_parameter
     return BZ_ERR_UNSUPPORTED;
   }
 #endif
-  if (F * sizeof(FacetXform) + 256 > BZ_NOALLOC_TABLE_BYTES) {
+  if (F * sizeof(FacetXform) > ws.table_bytes) {
     bz_record_error(BZ_ERR_UNSUPPORTED, "bullseye_facet_4_cor_corrections_noalloc: %zu facets exceed the scratch facet table", F);
     return BZ_ERR_UNSUPPORTED;
   }
@@ -213,9 +209,9 @@ extern "C" int bullseye_facet_4_cor_corrections_noalloc(const gridding_parameter
   }
 
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  vis_complex *lo = reinterpret_cast<vis_complex *>(scratch);
-  FacetXform *table = reinterpret_cast<FacetXform *>(scratch + BZ_NOALLOC_LO_BYTES);
-  int *err = reinterpret_cast<int *>(scratch + BZ_NOALLOC_LO_BYTES + BZ_NOALLOC_TABLE_BYTES - 256);
+  vis_complex *lo = ws.lo;
+  FacetXform *table = ws.table;
+  int *err = ws.err;
 #if defined(BULLSEYE_SINGLE)
   if (cudaMemsetAsync(lo, 0, grid_elems * sizeof(vis_complex), st) != cudaSuccess) return BZ_ERR_CUDA;
 #endif
@@ -276,3 +272,75 @@ extern "C" int bullseye_facet_4_cor_corrections_noalloc(const gridding_parameter
 #endif
   return BZ_OK;
 }
+
+}  // namespace
+
+// See include/bullseye_gb300.h.  Every pointer in *params is a device pointer; returns 0 when
+// the work was queued on `stream`, or a bz_status code (nothing queued) when the arguments are
+// rejected.  The first call on each device resolves the scratch array's device address
+// (cudaGetSymbolAddress) and should therefore come before any stream capture on that device.
+extern "C" int bullseye_facet_4_cor_corrections_noalloc(const gridding_parameters *params, void *stream) {
+  if (!params) return BZ_ERR_INVALID_ARGUMENT;
+  const gridding_parameters &p = *params;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= BZ_NOALLOC_MAX_DEVICES) return BZ_ERR_CUDA;
+  if (!g_noalloc_addr[dev]) {
+    void *ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr) return BZ_ERR_CUDA;
+    g_noalloc_addr[dev] = ptr;
+  }
+  unsigned char *scratch = static_cast<unsigned char *>(g_noalloc_addr[dev]);
+
+  Workspace ws;
+  ws.lo = reinterpret_cast<vis_complex *>(scratch);
+  ws.lo_bytes = BZ_NOALLOC_LO_BYTES;
+  ws.table = reinterpret_cast<FacetXform *>(scratch + BZ_NOALLOC_LO_BYTES);
+  ws.table_bytes = BZ_NOALLOC_TABLE_BYTES - 256;
+  ws.err = reinterpret_cast<int *>(scratch + BZ_NOALLOC_LO_BYTES + BZ_NOALLOC_TABLE_BYTES - 256);
+  return grid_4cor_jones(p, ws, stream);
+}
+
+// Bytes of caller workspace bullseye_facet_4_cor_corrections_ws needs for these parameters.
+static size_t ws_lo_bytes(const gridding_parameters &p) {
+#if defined(BULLSEYE_SINGLE)
+  const size_t F = p.num_facet_centres ? p.num_facet_centres : 1;
+  return (F * p.cube_channel_dim_size * 4 * p.nx * p.ny * sizeof(vis_complex) + 255) / 256 * 256;
+#else
+  (void)p;
+  return 0;
+#endif
+}
+static size_t ws_table_bytes(const gridding_parameters &p) {
+  const size_t F = p.num_facet_centres ? p.num_facet_centres : 1;
+  return (F * sizeof(FacetXform) + 255) / 256 * 256;
+}
+
+// See include/bullseye_gb300.h.
+extern "C" size_t bullseye_facet_4_cor_corrections_ws_bytes(const gridding_parameters *params) {
+  if (!params) return 0;
+  return ws_lo_bytes(*params) + ws_table_bytes(*params) + 256;
+}
+
+// See include/bullseye_gb300.h.
+extern "C" int bullseye_facet_4_cor_corrections_ws(const gridding_parameters *params, void *workspace, size_t bytes,
+                                                   void *stream) {
+  if (!params || !workspace) return BZ_ERR_INVALID_ARGUMENT;
+  const gridding_parameters &p = *params;
+  const size_t need = bullseye_facet_4_cor_corrections_ws_bytes(params);
+  if (bytes < need || (reinterpret_cast<uintptr_t>(workspace) & 255)) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT,
+                    "bullseye_facet_4_cor_corrections_ws: workspace of %zu bytes at %p, need %zu bytes 256-byte aligned",
+                    bytes, workspace, need);
+    return BZ_ERR_INVALID_ARGUMENT;
+  }
+  unsigned char *w = static_cast<unsigned char *>(workspace);
+  Workspace ws;
+  ws.lo = reinterpret_cast<vis_complex *>(w);
+  ws.lo_bytes = ws_lo_bytes(p);
+  ws.table = reinterpret_cast<FacetXform *>(w + ws.lo_bytes);
+  ws.table_bytes = ws_table_bytes(p);
+  ws.err = reinterpret_cast<int *>(w + ws.lo_bytes + ws.table_bytes);
+  return grid_4cor_jones(p, ws, stream);
+}
+

@@ -53,6 +53,9 @@ EXTENSIONS = {
     "bullseye_batched_plane_classes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "bullseye_grid_batched_facets": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "bullseye_facet_4_cor_corrections_ws_bytes": (ctypes.c_size_t, [ctypes.c_void_p]),
+    "bullseye_facet_4_cor_corrections_ws": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                                           ctypes.c_void_p]),
     "bullseye_reset_counters": (None, []),
     "bullseye_zero_grids": (None, []),
     "bullseye_set_gridding_correction": (None, [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t]),

@@ -165,6 +165,16 @@ int bullseye_batched_plane_classes(int *width, int max);
  * stream capture on that device.  Returns 0 when queued. */
 int bullseye_facet_4_cor_corrections_noalloc(const gridding_parameters *params, void *stream);
 
+/* The same gridding on device pointers with a CALLER-PROVIDED device workspace instead of the fixed
+ * scratch array, so grids of any size are accepted and concurrent calls with their own workspaces
+ * do not share state.  The workspace must be 256-byte aligned and at least
+ * bullseye_facet_4_cor_corrections_ws_bytes(params) bytes (the 32-bit library's compensation grid,
+ * the facet table and an error word); its contents need not be initialised.  jones_terms is
+ * inverted in place.  No counterpart in the reference. */
+size_t bullseye_facet_4_cor_corrections_ws_bytes(const gridding_parameters *params);
+int bullseye_facet_4_cor_corrections_ws(const gridding_parameters *params, void *workspace, size_t bytes,
+                                        void *stream);
+
 /* Adjoint of four-correlation gridding (a degridder): given grad_grid = dL/dG for the grids
  * G [facets][cube][4][ny][nx] that facet_4_cor_corrections (jones_terms set, faceting != 0),
  * facet_4_cor (jones_terms null, faceting != 0) or grid_4_cor (faceting == 0) produce from these
