@@ -70,8 +70,9 @@ def parse():
     ap.add_argument("--no-other", action="store_true", help="skip timing the other form")
     ap.add_argument("--facets", type=int, default=0, help="override the facet count (profiling cases)")
     ap.add_argument("--no-precision", action="store_true", help="skip the per-facet FP32 error report")
-    ap.add_argument("--workload", default="facets16", choices=["facets16", "uneven"],
-                    help="facets16: the 16-facet Jones workload (default); uneven: 96 facets of uneven sizes and masks")
+    ap.add_argument("--workload", default="facets16", choices=["facets16", "uneven", "adjoint"],
+                    help="facets16: the 16-facet Jones workload (default); uneven: 96 facets of uneven sizes and masks; "
+                         "adjoint: the differentiation form at scale with a finite-difference check")
     ap.add_argument("--no-class-profile", action="store_true",
                     help="skip the eager, per-support-class timed step after the timed region")
     ap.add_argument("--eager", action="store_true",
@@ -557,11 +558,180 @@ def uneven_main(args):
     print(json.dumps(line))
 
 
+# ----------------------------------------------------------------------------- differentiation
+ADJ_ANT, ADJ_TIMES, ADJ_CHAN, ADJ_NX, ADJ_PLANES, ADJ_S, ADJ_MINSUP, ADJ_OS, ADJ_CELL = 64, 1000, 32, 4096, 32, 15, 7, 15, 2.0
+
+
+def adjoint_main(args):
+    """The differentiation form at scale: 64 antennas (2016 baselines) x 1000 timesteps x 32
+    channels (64.5 M visibilities), one 4096^2 facet with Jones, w-projection with 32 planes.
+    Loss = sum over the central 512^2 pixels of the (XX + YY) dirty image squared.  Times the
+    forward (gridding) and the backward (adjoint + FFT) through torch.autograd, then checks the
+    gradients by central finite differences (eps 1e-3) on 200 random coordinates (100 visibility,
+    100 Jones).  Each difference is evaluated exactly on the full loss: gridding is linear in the
+    visibilities and a Jones term touches only the rows of its antenna and time, so the grid change
+    is gridded from those rows alone (64-bit library) and added to the full grid."""
+    import torch
+    from bullseye_gb300 import synth
+    from bullseye_gb300.autograd import FacetGeometry, facet_grid
+    from bullseye_gb300.filters import wproj_kernels
+    from bullseye_gb300.imaging import GriddingProblem
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda")
+    dec = np.deg2rad(-30.0)
+    xyz = synth.enu_to_equatorial(synth.disc_layout(ADJ_ANT, 2000.0, 1), np.deg2rad(-30.0))
+    uvw, a1, a2, tid = synth.earth_rotation_rows(xyz, ADJ_TIMES, dec, np.deg2rad(90.0))
+    R = uvw.shape[0]
+    freqs = np.linspace(1.0e9, 1.5e9, ADJ_CHAN)
+    lam = synth.C_LIGHT / freqs
+    wmax = np.max(np.linalg.norm(uvw, axis=1)) / lam.min()
+    fov = ADJ_NX * ADJ_CELL * synth.ARCSEC
+    conv, _ = wproj_kernels(ADJ_S, ADJ_OS, ADJ_PLANES, wmax, fov, min_support=ADJ_MINSUP)
+    dec0 = dec / synth.ARCSEC
+
+    def problem(rows, prec, weights=None):
+        n = len(rows)
+        return GriddingProblem(
+            precision=prec, vis=np.broadcast_to(np.zeros((1, 1, 1), np.complex64), (n, ADJ_CHAN, 4)),
+            uvw=uvw[rows].astype(np.float32).astype(np.float64 if prec == "double" else np.float32),
+            wavelengths=lam.reshape(1, -1).astype(np.float32).astype(np.float64 if prec == "double" else np.float32),
+            weights=weights if weights is not None else np.broadcast_to(np.ones((1, 1, 1), np.float32), (n, ADJ_CHAN, 4)),
+            flags=np.broadcast_to(np.zeros((1, 1, 1), bool), (n, ADJ_CHAN, 4)), flagged_rows=np.zeros(n, bool),
+            field_ids=np.zeros(n, np.uint32), spw_ids=np.zeros(n, np.uint32), antenna1=a1[rows], antenna2=a2[rows],
+            timestamp_ids=tid[rows], n_antennas=ADJ_ANT, n_timestamps=ADJ_TIMES, nx=ADJ_NX, ny=ADJ_NX, cell_x=ADJ_CELL,
+            cell_y=ADJ_CELL, conv=conv.astype(np.complex64 if prec == "single" else np.complex128), conv_support=ADJ_S,
+            conv_oversample=ADJ_OS, wplanes=ADJ_PLANES, wmax=float(wmax), phase_centre=(0.0, dec0),
+            facet_centres=np.array([[0.0, dec0]]), jones=None)
+
+    geom = FacetGeometry.from_problem(problem(np.arange(R), "single"), device=dev)
+    order = geom.order
+    # visibilities of 20 point sources (row order of the geometry) and near-identity gains
+    rng = np.random.default_rng(5)
+    lim = 0.4 * fov / 2
+    ls, ms = rng.uniform(-lim, lim, 20), rng.uniform(-lim, lim, 20)
+    flux = torch.tensor(rng.uniform(0.1, 2.0, 20), dtype=torch.complex64, device=dev)
+    l_t = torch.tensor(ls, dtype=torch.float32, device=dev)
+    m_t = torch.tensor(ms, dtype=torch.float32, device=dev)
+    nm1 = torch.sqrt(1 - l_t * l_t - m_t * m_t) - 1
+    uvw_o = torch.tensor(uvw[order], dtype=torch.float32, device=dev)
+    V = torch.empty((R, ADJ_CHAN, 4), dtype=torch.complex64, device=dev)
+    for ci, lm in enumerate(lam):
+        for lo in range(0, R, 1 << 16):
+            hi = min(R, lo + (1 << 16))
+            u, v, w = uvw_o[lo:hi, 0:1], uvw_o[lo:hi, 1:2], uvw_o[lo:hi, 2:3]
+            sv = torch.polar(torch.ones_like(u * l_t), (u * l_t + v * m_t + w * nm1) * (-2 * np.pi / lm)) @ flux
+            V[lo:hi, ci, 0] = sv
+            V[lo:hi, ci, 3] = sv
+            V[lo:hi, ci, 1] = 0
+            V[lo:hi, ci, 2] = 0
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(3)
+    shape = (ADJ_TIMES, ADJ_ANT, 1, 1, ADJ_CHAN)
+    J = torch.zeros(shape + (4,), dtype=torch.complex64, device=dev)
+    for k in (0, 3):
+        J[..., k] = torch.polar(1 + 0.2 * (torch.rand(shape, device=dev, generator=gen) - 0.5),
+                                (2 * torch.rand(shape, device=dev, generator=gen) - 1) * np.pi)
+    for k in (1, 2):
+        J[..., k] = 0.05 * torch.randn(shape, dtype=torch.complex64, device=dev, generator=gen)
+    c0, c1 = ADJ_NX // 2 - 256, ADJ_NX // 2 + 256
+
+    def loss_of(G):
+        s_ = G[0, 0, 0] + G[0, 0, 3]
+        img = torch.fft.fftshift(torch.fft.ifft2(torch.fft.ifftshift(s_))).real
+        cut = img[c0:c1, c0:c1]
+        return (cut * cut).sum()
+
+    def run(timed):
+        Vg = V.clone().requires_grad_(True)
+        Jg = J.clone().requires_grad_(True)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ev[0].record()
+        G, _ = facet_grid(geom, Vg, Jg)
+        ev[1].record()
+        L = loss_of(G)
+        L.backward()
+        ev[2].record()
+        torch.cuda.synchronize()
+        return ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2]), G.detach(), L.item(), Vg.grad, Jg.grad
+
+    for _ in range(args.warmup):
+        run(False)
+    fwd, bwd = [], []
+    for _ in range(args.steps):
+        f_ms, b_ms, G, Lval, gV, gJ = run(True)
+        fwd.append(f_ms)
+        bwd.append(b_ms)
+    f_ms, b_ms = float(np.median(fwd)), float(np.median(bwd))
+    # finite differences on 200 coordinates, the loss evaluated in FP64
+    G0 = G[0, 0][[0, 3]].to(torch.complex128)
+    del G
+
+    def loss64(dG):  # dG: [2][ny][nx] change of the XX and YY grids
+        s_ = (G0[0] + dG[0]) + (G0[1] + dG[1])
+        img = torch.fft.fftshift(torch.fft.ifft2(torch.fft.ifftshift(s_))).real
+        cut = img[c0:c1, c0:c1]
+        return float((cut * cut).sum())
+
+    J64 = J.to(torch.complex128)
+    eps = 1e-3
+    rng = np.random.default_rng(17)
+    errs = {"vis": [], "jones": []}
+    scale = {"vis": float(gV.abs().max()), "jones": float(gJ.abs().max())}
+    for i in range(100):
+        r = int(rng.integers(R))
+        ch, k, part = int(rng.integers(ADJ_CHAN)), int(rng.choice([0, 3])), int(rng.integers(2))
+        g1 = FacetGeometry.from_problem(problem(np.array([order[r]]), "double"), device=dev)
+        e = torch.zeros((1, ADJ_CHAN, 4), dtype=torch.complex128, device=dev)
+        e[0, ch, k] = 1.0 if part == 0 else 1j
+        Ge, _ = facet_grid(g1, e, J64)
+        dG = Ge[0, 0][[0, 3]]
+        fd = (loss64(eps * dG) - loss64(-eps * dG)) / (2 * eps)
+        an = float(gV[r, ch, k].real if part == 0 else gV[r, ch, k].imag)
+        errs["vis"].append(abs(fd - an) / scale["vis"])
+    inv = np.empty(R, np.int64)
+    inv[order] = np.arange(R)
+    for i in range(100):
+        t, a = int(rng.integers(ADJ_TIMES)), int(rng.integers(ADJ_ANT))
+        ch, k, part = int(rng.integers(ADJ_CHAN)), int(rng.integers(4)), int(rng.integers(2))
+        rows = np.nonzero((tid == t) & ((a1 == a) | (a2 == a)))[0]
+        wts = np.zeros((rows.size, ADJ_CHAN, 4), np.float64)
+        wts[:, ch, :] = 1.0
+        gs = FacetGeometry.from_problem(problem(rows, "double", weights=wts), device=dev)
+        Vs = V[torch.as_tensor(inv[rows][gs.order], device=dev)].to(torch.complex128).contiguous()
+        grids = []
+        for sign in (1, -1, 0):
+            Jp = J64.clone()
+            Jp[t, a, 0, 0, ch, k] += sign * eps * (1.0 if part == 0 else 1j)
+            Gs, _ = facet_grid(gs, Vs, Jp)
+            grids.append(Gs[0, 0][[0, 3]])
+        fd = (loss64(grids[0] - grids[2]) - loss64(grids[1] - grids[2])) / (2 * eps)
+        g = gJ[t, a, 0, 0, ch, k]
+        an = float(g.real if part == 0 else g.imag)
+        errs["jones"].append(abs(fd - an) / scale["jones"])
+    vis_pairs = R * ADJ_CHAN
+    line = {"metric": "gridded Mvis/s (vis x facet pairs)", "value": vis_pairs / (f_ms * 1e-3) / 1e6, "unit": "Mvis/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": f_ms + b_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"differentiation: {ADJ_ANT} ant ({ADJ_ANT * (ADJ_ANT - 1) // 2} baselines) x "
+                                   f"{ADJ_TIMES} t x {ADJ_CHAN} ch ({vis_pairs / 1e6:.1f}M vis), one {ADJ_NX}^2 facet with "
+                                   f"Jones, w-proj {ADJ_PLANES} planes; loss = sum over the central 512^2 pixels of the "
+                                   f"(XX+YY) dirty image squared"},
+            "forward_ms": f_ms, "backward_ms": b_ms,
+            "backward_mvis_s": vis_pairs / (b_ms * 1e-3) / 1e6, "loss": Lval,
+            "finite_differences": {"eps": eps, "coordinates": 200,
+                                   "max_err_vis": max(errs["vis"]), "max_err_jones": max(errs["jones"]),
+                                   "tolerance": 1e-4, "relative_to": "largest gradient magnitude of each kind",
+                                   "pass": max(errs["vis"]) <= 1e-4 and max(errs["jones"]) <= 1e-4}}
+    print(json.dumps(line))
+
+
 # ----------------------------------------------------------------------------- main
 def main():
     args = parse()
     if args.workload == "uneven":
         return uneven_main(args)
+    if args.workload == "adjoint":
+        return adjoint_main(args)
     global N_CHAN, N_FACETS
     if args.chans:
         N_CHAN = args.chans
