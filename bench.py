@@ -591,17 +591,20 @@ def adjoint_main(args):
 
     def problem(rows, prec, weights=None):
         n = len(rows)
+        rd = np.float64 if prec == "double" else np.float32
+        if weights is None:
+            weights = np.broadcast_to(np.ones((1, 1, 1), rd), (n, ADJ_CHAN, 4))
         return GriddingProblem(
             precision=prec, vis=np.broadcast_to(np.zeros((1, 1, 1), np.complex64), (n, ADJ_CHAN, 4)),
             uvw=uvw[rows].astype(np.float32).astype(np.float64 if prec == "double" else np.float32),
             wavelengths=lam.reshape(1, -1).astype(np.float32).astype(np.float64 if prec == "double" else np.float32),
-            weights=weights if weights is not None else np.broadcast_to(np.ones((1, 1, 1), np.float32), (n, ADJ_CHAN, 4)),
+            weights=weights.astype(rd),
             flags=np.broadcast_to(np.zeros((1, 1, 1), bool), (n, ADJ_CHAN, 4)), flagged_rows=np.zeros(n, bool),
             field_ids=np.zeros(n, np.uint32), spw_ids=np.zeros(n, np.uint32), antenna1=a1[rows], antenna2=a2[rows],
             timestamp_ids=tid[rows], n_antennas=ADJ_ANT, n_timestamps=ADJ_TIMES, nx=ADJ_NX, ny=ADJ_NX, cell_x=ADJ_CELL,
             cell_y=ADJ_CELL, conv=conv.astype(np.complex64 if prec == "single" else np.complex128), conv_support=ADJ_S,
             conv_oversample=ADJ_OS, wplanes=ADJ_PLANES, wmax=float(wmax), phase_centre=(0.0, dec0),
-            facet_centres=np.array([[0.0, dec0]]), jones=None)
+            facet_centres=np.array([[0.0, dec0]], dtype=rd), jones=None)
 
     geom = FacetGeometry.from_problem(problem(np.arange(R), "single"), device=dev)
     order = geom.order
