@@ -585,9 +585,8 @@ __host__ __device__ inline size_t flush_queue_bytes(int nwarps) {
 #endif
 }
 
-// Row taps are stored W long per visibility (no padding: a thread's J consecutive owned rows
-// wrap modulo W through per-run row offsets).
-constexpr int kTvPad = 0;
+// Row taps are stored W + J - 1 long per visibility: the first J - 1 taps are repeated after the
+// last, so a thread's J consecutive owned rows read J consecutive taps without a wrap.
 
 // Bytes before the tap arrays: V staged records, their normalisation state (partial sums, grid
 // group, mixed flag), the V + 1 run starts of the chunk; rounded up to 16.
@@ -597,22 +596,22 @@ __host__ __device__ inline size_t stage_head_bytes(int V) {
 }
 
 template <int NC, bool WPROJ>
-__host__ __device__ inline size_t grid_smem_bytes(int V, int W, int nthreads) {
-  size_t taps = sizeof(typename TapT<WPROJ>::type) * (size_t)V * (2 * W + kTvPad);
+__host__ __device__ inline size_t grid_smem_bytes(int V, int W, int nthreads, int J) {
+  size_t taps = sizeof(typename TapT<WPROJ>::type) * (size_t)V * (2 * W + J - 1);
   return stage_head_bytes<NC>(V) + taps + flush_queue_bytes<NC>((nthreads + 31) / 32) + 64;
 }
 
 // Staged-chunk size V for a CTA of nthreads: one visibility per thread at most, and shared memory
 // small enough that the CTAs the register file allows (128 registers per thread) fit on an SM.
 template <int NC, bool WPROJ>
-__host__ inline int grid_chunk_size(int W, int nthreads) {
+__host__ inline int grid_chunk_size(int W, int nthreads, int J) {
   const int ctas = std::max(1, std::min(8, 65536 / (nthreads * 128)));
   const size_t smem_sm = 227 * 1024;
   size_t budget = std::min<size_t>(200 * 1024, smem_sm / ctas - 1024);
   const size_t fixed = flush_queue_bytes<NC>((nthreads + 31) / 32) + 64 + sizeof(int) + 15;
   budget = budget > fixed ? budget - fixed : 0;
   const size_t per = sizeof(VisRec<NC>) + sizeof(double) * NC + 3 * sizeof(int) +
-                     sizeof(typename TapT<WPROJ>::type) * (2 * (size_t)W + kTvPad);
+                     sizeof(typename TapT<WPROJ>::type) * (2 * (size_t)W + J - 1);
   return std::max(1, (int)std::min<size_t>(nthreads, budget / per));
 }
 
@@ -664,7 +663,7 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
   int *s_mixed = s_ng + a.V;                                                          // [V]
   int *s_runs = s_mixed + a.V;  // [V + 1]: first slot of every run of the staged chunk, then nv
   tap_t *tu = reinterpret_cast<tap_t *>(smem_raw + stage_head_bytes<NC>(a.V));
-  const int TVS = a.W + kTvPad;  // row-tap stride per staged visibility
+  const int TVS = a.W + J - 1;  // row-tap stride per staged visibility
   tap_t *tv = tu + a.V * a.W;
   // per-warp flush queues follow the taps
   unsigned char *qbase = reinterpret_cast<unsigned char *>(tv + a.V * TVS);
@@ -772,24 +771,27 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
         s_nruns = count;
       }
     }
-    // gather the taps of every staged visibility: W column taps, then W row taps.  Thread tid
-    // walks (visibility, tap) pairs with a stride of blockDim.x pairs, stepped without division.
+    // gather the taps of every staged visibility: W column taps, then W + J - 1 row taps.  Thread
+    // tid walks (visibility, tap) pairs with a stride of blockDim.x pairs, stepped without division.
     {
-      const int per = 2 * W;
+      const int per = W + TVS;
       int vi = tid / per, j = tid - vi * per;
       const int svi = (int)blockDim.x / per, sj = (int)blockDim.x - svi * per;
       while (vi < nv) {
         const int4 h1 = *reinterpret_cast<const int4 *>(&recs[vi].g);  // g, valid, fu, fv
         if (h1.y) {
           const bool isv = j >= W;
-          const int jj = isv ? j - W : j;
+          const int js = isv ? j - W : j;  // slot in the staged row
+          int jj = js >= W ? js - W : js;  // repeated leading row taps
+          if (jj >= W) jj = W - 1;
           tap_t t;
           if (a.conv_t) {
             load_tap(a.conv_t, (long long)(isv ? h1.w : h1.z) + jj, t);
           } else {
             load_tap(a.conv, (long long)recs[vi].plane * a.K + (isv ? h1.w : h1.z) + (long long)jj * a.os, t);
           }
-          (isv ? tv : tu)[vi * W + jj] = t;
+          if (isv) tv[vi * TVS + js] = t;
+          else tu[vi * W + js] = t;
         }
         vi += svi;
         j += sj;
@@ -894,7 +896,7 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
           }
           // columns beyond W (padding lanes) read in-bounds taps and are never flushed
           ou = o < W ? o : W - 1;
-          ov0 = nov0;
+          ov0 = nov0 < W ? nov0 : 0;  // lanes past the last strip own nothing: keep their reads in bounds
           pu0 = h0.x;
           pv0 = h0.y;
           if (COMP) {  // the queue only grows here; the branch is uniform over the CTA
@@ -905,19 +907,16 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
         // the run's visibilities share the owned cells: a branch-free multiply-add loop over
         // the J owned rows (offsets modulo W; rows of non-owning lanes stay in bounds and are
         // never flushed)
-        int ro[J];
-#pragma unroll
-        for (int j = 0; j < J; ++j) ro[j] = (ov0 + j) % W;
 #pragma unroll 2
         for (int vi = rs; vi < re; ++vi) {
           const tap_t tuv = tu[vi * W + ou];
           cplx pre[NC];
 #pragma unroll
           for (int k = 0; k < NC; ++k) pre[k] = premul(recs[vi].vis[k], tuv);
-          const tap_t *tvrow = tv + vi * W;
+          const tap_t *tvrow = tv + vi * TVS + ov0;
 #pragma unroll
           for (int j = 0; j < J; ++j) {
-            const tap_t t = tvrow[ro[j]];
+            const tap_t t = tvrow[j];
 #pragma unroll
             for (int k = 0; k < NC; ++k) mac(acc[j][k], pre[k], t);
           }

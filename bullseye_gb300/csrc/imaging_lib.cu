@@ -505,8 +505,8 @@ static LaunchShape choose_shape(int W) {
   if (!s.J) s.J = 16;
   const int owners = s.wide ? cols * ((W + s.J - 1) / s.J) : W * ((W + s.J - 1) / s.J);
   s.NT = std::max(32, ((owners + 31) / 32) * 32);
-  s.V = grid_chunk_size<NC, WPROJ>(W, s.NT);
-  s.smem = grid_smem_bytes<NC, WPROJ>(s.V, W, s.NT);
+  s.V = grid_chunk_size<NC, WPROJ>(W, s.NT, s.J);
+  s.smem = grid_smem_bytes<NC, WPROJ>(s.V, W, s.NT, s.J);
   return s;
 }
 
