@@ -70,6 +70,7 @@ def parse():
     ap.add_argument("--no-other", action="store_true", help="skip timing the other form")
     ap.add_argument("--facets", type=int, default=0, help="override the facet count (profiling cases)")
     ap.add_argument("--no-precision", action="store_true", help="skip the per-facet FP32 error report")
+    ap.add_argument("--adj-times", type=int, default=0, help="differentiation workload: override the timestep count")
     ap.add_argument("--workload", default="facets16", choices=["facets16", "uneven", "adjoint"],
                     help="facets16: the 16-facet Jones workload (default); uneven: 96 facets of uneven sizes and masks; "
                          "adjoint: the differentiation form at scale with a finite-difference check")
@@ -580,6 +581,9 @@ def adjoint_main(args):
     dev = torch.device("cuda")
     dec = np.deg2rad(-30.0)
     xyz = synth.enu_to_equatorial(synth.disc_layout(ADJ_ANT, 2000.0, 1), np.deg2rad(-30.0))
+    global ADJ_TIMES
+    if args.adj_times:
+        ADJ_TIMES = args.adj_times
     uvw, a1, a2, tid = synth.earth_rotation_rows(xyz, ADJ_TIMES, dec, np.deg2rad(90.0))
     R = uvw.shape[0]
     freqs = np.linspace(1.0e9, 1.5e9, ADJ_CHAN)
