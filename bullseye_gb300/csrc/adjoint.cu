@@ -17,8 +17,7 @@
 // the footprint the gridder wrote.  The normalisation sums depend only on weights and taps, so they
 // carry no gradient.
 //
-// One warp per (row, channel) loops over the facets (consecutive warps take consecutive rows of one
-// channel, so their footprints overlap in L1): the lanes split the W x W footprint, the
+// One warp per (row, channel) loops over the facets: the lanes split the W x W footprint, the
 // partial sums are reduced with shuffles, lane 0 forms the gradients.  The visibility gradient
 // (summed over facets) is written once; Jones gradients are accumulated with atomics because
 // every antenna appears on many baselines.
@@ -148,11 +147,9 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
   const long long nxy = (long long)a.nx * a.ny;
   const double plane_scale = WPROJ ? (double)(a.P - 1) / a.wmax : 0.0;
 
-  // items run channel-major, so the warps of a CTA take consecutive rows of one channel: with
-  // time-ordered rows their footprints overlap and the grid reads hit the SM's L1
   for (long long item = warp; item < a.nrows * a.nchan; item += nwarps) {
-    const int c = (int)(item / a.nrows);
-    const long long row = item - (long long)c * a.nrows;
+    const long long row = item / a.nchan;
+    const int c = (int)(item - row * a.nchan);
     const unsigned spw = a.spw[row];
     if (spw >= (unsigned)a.nspw) continue;
     const long long sc = (long long)spw * a.nchan + c;
