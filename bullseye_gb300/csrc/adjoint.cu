@@ -17,9 +17,10 @@
 // the footprint the gridder wrote.  The normalisation sums depend only on weights and taps, so they
 // carry no gradient.
 //
-// One warp per (row, channel) loops over the facets: the lanes split the W x W footprint, the
-// partial sums are reduced with shuffles, lane 0 forms the gradients.  The visibility gradient
-// (summed over facets) is written once; Jones gradients are accumulated with atomics because
+// One warp per (row, channel) loops over the facets: lane 0 resolves Jones and geometry, the lanes
+// split the W x W footprint, the partial sums are reduced with shuffles, lane 0 forms the
+// gradients.  The visibility gradient (summed over facets) is written once; Jones gradients are
+// accumulated with atomics because
 // every antenna appears on many baselines.
 #include <cstring>
 
@@ -179,34 +180,47 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
     for (int k = 0; k < 4; ++k) { gV[k].re = 0; gV[k].im = 0; }
 
     for (int f = 0; f < a.nfacets; ++f) {
-      // Jones inverses of this row and facet
+      // lane 0 resolves the Jones inverses and the geometry (FP64 is scarce on this GPU: no lane
+      // repeats it); the lanes share the footprint through shuffles
       cplx Pm[4], Qm[4];
       long long i1 = 0, i2 = 0;
-      bool jok = true;
-      if (a.jones) {
-        const long long t = (long long)a.time_ids[row];
-        const unsigned a1 = a.ant1[row], a2 = a.ant2[row];
-        if (t < 0 || t >= a.ntimes || a1 >= (unsigned)a.nant || a2 >= (unsigned)a.nant) continue;
-        i1 = ((((t * a.nant + a1) * a.nfacets + f) * a.nspw + spw) * a.nchan + c) * 4;
-        i2 = ((((t * a.nant + a2) * a.nfacets + f) * a.nspw + spw) * a.nchan + c) * 4;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          Pm[k].re = a.jones[i1 + k].re; Pm[k].im = a.jones[i1 + k].im;
-          Qm[k].re = a.jones[i2 + k].re; Qm[k].im = a.jones[i2 + k].im;
-        }
-        jok = inv2(Pm) && inv2(Qm);
-        if (!jok) continue;
-      }
-      // geometry: the gridder's own cell choice (same cells, taps, plane and phase)
       CellChoice cell;
+      cell.du = cell.dv = cell.fu = cell.fv = cell.plane = 0;
+      cell.flip = false;
       cplx ph;
-      if (!choose_cells<WPROJ>(um, vm, wm, cc, fx[f], a.faceting != 0, a.faceting != 0, a.u_scale, a.v_scale,
-                               plane_scale, a.gcx, a.gcy, a.nx, a.ny, W, a.P, a.os, ph, cell))
-        continue;
+      ph.re = 1;
+      ph.im = 0;
+      int ok = 0;
+      if (lane == 0) {
+        ok = 1;
+        if (a.jones) {
+          const long long t = (long long)a.time_ids[row];
+          const unsigned a1 = a.ant1[row], a2 = a.ant2[row];
+          if (t < 0 || t >= a.ntimes || a1 >= (unsigned)a.nant || a2 >= (unsigned)a.nant) {
+            ok = 0;
+          } else {
+            i1 = ((((t * a.nant + a1) * a.nfacets + f) * a.nspw + spw) * a.nchan + c) * 4;
+            i2 = ((((t * a.nant + a2) * a.nfacets + f) * a.nspw + spw) * a.nchan + c) * 4;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              Pm[k].re = a.jones[i1 + k].re; Pm[k].im = a.jones[i1 + k].im;
+              Qm[k].re = a.jones[i2 + k].re; Qm[k].im = a.jones[i2 + k].im;
+            }
+            ok = inv2(Pm) && inv2(Qm);
+          }
+        }
+        // geometry: the gridder's own cell choice (same cells, taps, plane and phase)
+        if (ok)
+          ok = choose_cells<WPROJ>(um, vm, wm, cc, fx[f], a.faceting != 0, a.faceting != 0, a.u_scale, a.v_scale,
+                                   plane_scale, a.gcx, a.gcy, a.nx, a.ny, W, a.P, a.os, ph, cell) ? 1 : 0;
+      }
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) continue;
       const bool flip = cell.flip;
-      const int u0 = cell.du, v0 = cell.dv;
-      const long long fu = (long long)cell.plane * a.K + cell.fu;
-      const long long fv = (long long)cell.plane * a.K + cell.fv;
+      const int u0 = __shfl_sync(0xffffffffu, cell.du, 0), v0 = __shfl_sync(0xffffffffu, cell.dv, 0);
+      const int plane = __shfl_sync(0xffffffffu, cell.plane, 0);
+      const long long fu = (long long)plane * a.K + __shfl_sync(0xffffffffu, cell.fu, 0);
+      const long long fv = (long long)plane * a.K + __shfl_sync(0xffffffffu, cell.fv, 0);
       const long long slice0 = ((long long)f * a.cube + (long long)g) * 4;
       // gather: D_k = sum over the footprint of g_G conj(tap)
       cplx D[4];
@@ -234,7 +248,8 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
           D[k].im += __shfl_xor_sync(0xffffffffu, D[k].im, off);
         }
       }
-      // chain rule back to V (and the Jones terms)
+      // chain rule back to V (and the Jones terms), in lane 0
+      if (lane != 0) continue;
       cplx gM[4];
       const cplx cph = cconj(ph);
 #pragma unroll
@@ -251,7 +266,7 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
         mat2(T, false, Qm, false, G1);  // (P^H gM) Q
 #pragma unroll
         for (int k = 0; k < 4; ++k) gV[k] = cadd(gV[k], G1[k]);
-        if (a.grad_jones && lane == 0) {
+        if (a.grad_jones) {
           cplx VQ[4], M[4], gp[4], gq[4];
           mat2(V, false, Qm, true, VQ);  // V Q^H
           mat2(Pm, false, VQ, false, M);  // M = P V Q^H
@@ -272,16 +287,14 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
         for (int k = 0; k < 4; ++k) gV[k] = cadd(gV[k], gM[k]);
       }
     }
-    if (lane < 4) {
-      // every lane holds the same sums after the xor reductions; lane k writes correlation k
-      cplx mine = gV[0];
-      if (lane == 1) mine = gV[1];
-      if (lane == 2) mine = gV[2];
-      if (lane == 3) mine = gV[3];
-      vis_complex o;
-      o.re = (vis_real)mine.re;
-      o.im = (vis_real)mine.im;
-      a.grad_vis[base + lane] = o;
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        vis_complex o;
+        o.re = (vis_real)gV[k].re;
+        o.im = (vis_real)gV[k].im;
+        a.grad_vis[base + k] = o;
+      }
     }
   }
 }
