@@ -157,13 +157,18 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
     if (!a.enabled[sc]) continue;
     const size_t g = a.cgi[sc];
     if (g >= (size_t)a.cube) continue;
-    ChanCache cc;
-    cc.spw = spw;
-    cc.inv = 1.0 / (double)a.wavelengths[sc];
-    cc.su = cc.inv * a.u_scale;
-    cc.sv = cc.inv * a.v_scale;
-    cc.sw = cc.inv * plane_scale;
-    const double um = (double)a.uvw[3 * row], vm = (double)a.uvw[3 * row + 1], wm = (double)a.uvw[3 * row + 2];
+    ChanCache cc;  // used by lane 0 only
+    double um = 0, vm = 0, wm = 0;
+    if (lane == 0) {
+      cc.spw = spw;
+      cc.inv = 1.0 / (double)a.wavelengths[sc];
+      cc.su = cc.inv * a.u_scale;
+      cc.sv = cc.inv * a.v_scale;
+      cc.sw = cc.inv * plane_scale;
+      um = (double)a.uvw[3 * row];
+      vm = (double)a.uvw[3 * row + 1];
+      wm = (double)a.uvw[3 * row + 2];
+    }
     const bool row_ok = !a.flagged_rows[row] && a.field[row] == a.imaging_field;
     const long long base = (row * a.nchan + c) * 4;
     acc_real cw[4];
@@ -226,8 +231,15 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
       cplx D[4];
 #pragma unroll
       for (int k = 0; k < 4; ++k) { D[k].re = 0; D[k].im = 0; }
-      for (int t = lane; t < W * W; t += 32) {
-        const int jv = t / W, ju = t - jv * W;
+      // lane walks footprint cells lane, lane + 32, ... as (ju, jv) without division
+      int ju = lane % W, jv = lane / W;
+      const int sju = 32 % W, sjv = 32 / W;
+      for (; jv < W; ju += sju, jv += sjv) {
+        if (ju >= W) {
+          ju -= W;
+          ++jv;
+          if (jv >= W) break;
+        }
         const cplx tap = cmul(tap_at<WPROJ>(a.conv, fu + (long long)ju * a.os), tap_at<WPROJ>(a.conv, fv + (long long)jv * a.os));
         const cplx ct = cconj(tap);
         const long long cell = (long long)(v0 + jv) * a.nx + (u0 + ju);
