@@ -140,6 +140,38 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
     }
     fx[f] = x;
   }
+  // nonzero window [lo, hi] of every w plane's kernel row, one warp per plane: a footprint cell s
+  // reads sample fu + s*os with fu in [floor(os/2), floor(3 os/2)] (w-projection, round to nearest)
+  // or [0, os] (AA, floor); cells that cannot reach a nonzero sample carry a zero tap and are skipped
+  int2 *win = reinterpret_cast<int2 *>(smem_raw + sizeof(FacetXform) * a.nfacets);
+  {
+    const int ln = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int fu_min = WPROJ ? (int)floor(0.5 * a.os - 1e-6) : 0;
+    const int fu_max = WPROJ ? (int)floor(1.5 * a.os + 1e-6) : a.os;
+    for (int pl = wid; pl < a.P; pl += nw) {
+      int lo = 0x7fffffff, hi = -1;
+      for (int i = ln; i < a.K; i += 32) {
+        const cplx t = tap_at<WPROJ>(a.conv, (long long)pl * a.K + i);
+        if (t.re != (acc_real)0 || t.im != (acc_real)0) {
+          lo = min(lo, i);
+          hi = max(hi, i);
+        }
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, off));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, off));
+      }
+      if (ln == 0) {
+        int2 w2 = make_int2(0, -1);  // empty window: an all-zero row
+        if (hi >= 0) {
+          w2.x = max(0, (int)ceil((double)(lo - fu_max) / a.os));
+          w2.y = min(a.W - 1, (int)floor((double)(hi - fu_min) / a.os));
+        }
+        win[pl] = w2;
+      }
+    }
+  }
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -231,14 +263,18 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
       cplx D[4];
 #pragma unroll
       for (int k = 0; k < 4; ++k) { D[k].re = 0; D[k].im = 0; }
-      // lane walks footprint cells lane, lane + 32, ... as (ju, jv) without division
-      int ju = lane % W, jv = lane / W;
-      const int sju = 32 % W, sjv = 32 / W;
-      for (; jv < W; ju += sju, jv += sjv) {
-        if (ju >= W) {
-          ju -= W;
+      // lane walks the cells lane, lane + 32, ... of the plane's nonzero window as (ju, jv) without
+      // division
+      const int2 w2 = win[plane];
+      const int ww = w2.y - w2.x + 1;
+      if (ww <= 0) continue;
+      int ju = w2.x + lane % ww, jv = w2.x + lane / ww;
+      const int sju = 32 % ww, sjv = 32 / ww, wend = w2.y + 1;
+      for (; jv < wend; ju += sju, jv += sjv) {
+        if (ju >= wend) {
+          ju -= ww;
           ++jv;
-          if (jv >= W) break;
+          if (jv >= wend) break;
         }
         const cplx tap = cmul(tap_at<WPROJ>(a.conv, fu + (long long)ju * a.os), tap_at<WPROJ>(a.conv, fv + (long long)jv * a.os));
         const cplx ct = cconj(tap);
@@ -355,7 +391,7 @@ extern "C" int bullseye_grid_adjoint(const gridding_parameters *params, const vo
   a.ra0 = (double)p.phase_centre_ra;
   a.dec0 = (double)p.phase_centre_dec;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const size_t smem = sizeof(FacetXform) * (size_t)a.nfacets;
+  const size_t smem = sizeof(FacetXform) * (size_t)a.nfacets + sizeof(int2) * (size_t)a.P;
   if (smem > 200 * 1024) return BZ_ERR_UNSUPPORTED;
   if (cudaMemsetAsync(grad_vis, 0, sizeof(vis_complex) * (size_t)a.nrows * a.nchan * 4, st) != cudaSuccess) return BZ_ERR_CUDA;
   if (a.nrows == 0) return BZ_OK;
