@@ -156,7 +156,6 @@ __global__ void bucket_kernel(const int4 *__restrict__ segs, const int *total, i
 struct Variant {
   int J;
   bool wide;
-  bool big;  // J = 8 layout compiled for at most 256 threads: up to 255 registers, no spills
   int NT, V, grid;
   size_t smem;
 };
@@ -165,23 +164,21 @@ template <int NC, bool WPROJ, bool COMP>
 using SegKernel = void (*)(const GridArgs, const int);
 
 template <int NC, bool WPROJ, bool COMP>
-SegKernel<NC, WPROJ, COMP> seg_kernel(int J, bool wide, bool big = false) {
-  if (big) return wide ? romein_segment_kernel<NC, WPROJ, 8, COMP, true, 256> : romein_segment_kernel<NC, WPROJ, 8, COMP, false, 256>;
+SegKernel<NC, WPROJ, COMP> seg_kernel(int J, bool wide) {
   if (wide) return J == 4 ? romein_segment_kernel<NC, WPROJ, 4, COMP, true> : romein_segment_kernel<NC, WPROJ, 8, COMP, true>;
   return J == 4 ? romein_segment_kernel<NC, WPROJ, 4, COMP, false> : romein_segment_kernel<NC, WPROJ, 8, COMP, false>;
 }
 
 template <int NC, bool WPROJ>
-bool make_variant(int W, int J, bool wide, bool big, Variant &v) {
+bool make_variant(int W, int J, bool wide, Variant &v) {
   const int cols = ((W + 31) / 32) * 32;
   if (wide && (cols - W) * 8 > W) return false;
   const int owners = wide ? cols * ((W + J - 1) / J) : W * ((W + J - 1) / J);
   v.J = J;
   v.wide = wide;
-  v.big = big;
   v.NT = std::max(32, ((owners + 31) / 32) * 32);
-  if (v.NT > (big ? 256 : 512)) return false;
-  v.V = grid_chunk_size<NC, WPROJ>(W, v.NT, J, big ? 256 : 128);
+  if (v.NT > 512) return false;
+  v.V = grid_chunk_size<NC, WPROJ>(W, v.NT, J);
   v.smem = grid_smem_bytes<NC, WPROJ>(v.V, W, v.NT, J);
   return true;
 }
@@ -202,7 +199,7 @@ struct BatchedState {
   DevBuf<FacetXform> facet_table;  // per-facet geometry of bullseye_grid_batched_facets
   size_t rows_cap = 0, tracks_cap = 0, segs_cap = 0;
   // tuning decisions, by (class width, NC, WPROJ, COMP)
-  std::map<std::tuple<int, int, int, int>, std::tuple<int, int, int>> tuned;  // -> (J, wide, big)
+  std::map<std::tuple<int, int, int, int>, std::pair<int, int>> tuned;
   // captured graph
   cudaGraphExec_t exec = nullptr;
   std::vector<unsigned char> key;
@@ -330,7 +327,7 @@ bool launch_class(const GridArgs &base, int k, const Variant &v, int nfacets, co
   a.segment_capacity = (long long)g_bs.segs_cap;
   a.work_count = count;
   a.work_next = next;
-  auto kern = seg_kernel<NC, WPROJ, COMP>(v.J, v.wide, v.big);
+  auto kern = seg_kernel<NC, WPROJ, COMP>(v.J, v.wide);
   if (!open_smem(kern)) {
     bz_record_error(BZ_ERR_CUDA, "batched: cudaFuncSetAttribute failed");
     return false;
@@ -344,7 +341,7 @@ bool launch_class(const GridArgs &base, int k, const Variant &v, int nfacets, co
 
 template <int NC, bool WPROJ, bool COMP>
 bool finish_variant(Variant &v) {
-  auto kern = seg_kernel<NC, WPROJ, COMP>(v.J, v.wide, v.big);
+  auto kern = seg_kernel<NC, WPROJ, COMP>(v.J, v.wide);
   if (!open_smem(kern)) return false;
   int per_sm = 0, dev = 0, sms = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, v.NT, v.smem) != cudaSuccess || per_sm < 1) return false;
@@ -365,24 +362,21 @@ bool tune_class(const GridArgs &base, int k, int nfacets, Variant &out, int host
   auto it = b.tuned.find(key);
   std::vector<Variant> cands;
   for (int J : {8, 4})
-    for (bool wide : {true, false})
-      for (bool big : {false, true}) {
-        if (big && (J != 8 || NC != 4)) continue;
-        Variant v;
-        if (make_variant<NC, WPROJ>(W, J, wide, big, v) && finish_variant<NC, WPROJ, COMP>(v)) cands.push_back(v);
-      }
+    for (bool wide : {true, false}) {
+      Variant v;
+      if (make_variant<NC, WPROJ>(W, J, wide, v) && finish_variant<NC, WPROJ, COMP>(v)) cands.push_back(v);
+    }
   if (cands.empty()) {
     bz_record_error(BZ_ERR_UNSUPPORTED, "batched: no layout for support class %d", W);
     return false;
   }
   if (it != b.tuned.end()) {
     for (auto &v : cands)
-      if (v.J == std::get<0>(it->second) && (int)v.wide == std::get<1>(it->second) &&
-          (int)v.big == std::get<2>(it->second)) { out = v; return true; }
+      if (v.J == it->second.first && (int)v.wide == it->second.second) { out = v; return true; }
   }
   if (cands.size() == 1 || host_count == 0) {
     out = cands[0];
-    b.tuned[key] = std::make_tuple(out.J, (int)out.wide, (int)out.big);
+    b.tuned[key] = {out.J, (int)out.wide};
     return true;
   }
   // Each candidate grids a quarter of the class's runs (at least 4096, when there are that many)
@@ -417,7 +411,7 @@ bool tune_class(const GridArgs &base, int k, int nfacets, Variant &out, int host
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   BZ_CUDA_TRY_RET(cudaMemsetAsync(c.scratch.ptr, 0, sizeof(vis_complex) * c.scratch.n, c.stream), false);
-  b.tuned[key] = std::make_tuple(out.J, (int)out.wide, (int)out.big);
+  b.tuned[key] = {out.J, (int)out.wide};
   return bz_error_code() == BZ_OK;
 }
 
@@ -450,7 +444,7 @@ bool launch_all(const GridArgs &base, int nfacets, bool sampling, cudaStream_t s
       cudaEventElapsedTime(&ms, e0, e1);
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
-      b.records.push_back({b.cls[k].width, NC, v.J, (int)v.wide | ((int)v.big << 1), counts ? (*counts)[k] * nfacets : 0, ms});
+      b.records.push_back({b.cls[k].width, NC, v.J, (int)v.wide, counts ? (*counts)[k] * nfacets : 0, ms});
     }
     if (!ok) return false;
   }
