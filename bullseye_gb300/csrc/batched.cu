@@ -178,7 +178,7 @@ bool make_variant(int W, int J, bool wide, Variant &v) {
   v.wide = wide;
   v.NT = std::max(32, ((owners + 31) / 32) * 32);
   if (v.NT > 512) return false;
-  v.V = grid_chunk_size<NC, WPROJ>(W, v.NT, J);
+  v.V = grid_chunk_size<NC, WPROJ>(W, v.NT, J, J == 4 ? kSegRegs<4> : kSegRegs<8>);
   v.smem = grid_smem_bytes<NC, WPROJ>(v.V, W, v.NT, J);
   return true;
 }

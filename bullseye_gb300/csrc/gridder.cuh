@@ -604,8 +604,8 @@ __host__ __device__ inline size_t grid_smem_bytes(int V, int W, int nthreads, in
 // Staged-chunk size V for a CTA of nthreads: one visibility per thread at most, and shared memory
 // small enough that the CTAs the register file allows (128 registers per thread) fit on an SM.
 template <int NC, bool WPROJ>
-__host__ inline int grid_chunk_size(int W, int nthreads, int J) {
-  const int ctas = std::max(1, std::min(8, 65536 / (nthreads * 128)));
+__host__ inline int grid_chunk_size(int W, int nthreads, int J, int regs = 128) {
+  const int ctas = std::max(1, std::min(8, 65536 / (nthreads * regs)));
   const size_t smem_sm = 227 * 1024;
   size_t budget = std::min<size_t>(200 * 1024, smem_sm / ctas - 1024);
   const size_t fixed = flush_queue_bytes<NC>((nthreads + 31) / 32) + 64 + sizeof(int) + 15;
@@ -964,6 +964,12 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
   }
 }
 
+// Register budget of the persistent segment kernel: the J = 4 layout (32 accumulator registers) is
+// capped at 80 registers per thread so that more warps stay resident (it measured faster than at 96
+// or 128); J = 8 keeps the 128 that 512 threads allow.
+template <int J>
+constexpr int kSegRegs = J == 4 ? 80 : 128;
+
 // One CTA per track: blockIdx -> (facet, baseline slot or row segment, channel).
 template <int NC, bool WPROJ, int J, bool COMP, bool WIDE>
 __global__ void __launch_bounds__(512, 1) romein_grid_kernel(const GridArgs a) {
@@ -989,7 +995,7 @@ __global__ void __launch_bounds__(512, 1) romein_grid_kernel(const GridArgs a) {
 // the facets of a segment are gridded while its rows are hot in L2.  The loop ends on the count,
 // never waits on other CTAs.
 template <int NC, bool WPROJ, int J, bool COMP, bool WIDE>
-__global__ void __launch_bounds__(512, 1) romein_segment_kernel(const GridArgs a, const int nfacets) {
+__global__ void __launch_bounds__(512, 1) __maxnreg__(kSegRegs<J>) romein_segment_kernel(const GridArgs a, const int nfacets) {
   __shared__ int s_item;
   const int count = *a.work_count;
   const long long total = (long long)count * nfacets;
