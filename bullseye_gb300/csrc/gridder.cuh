@@ -964,9 +964,10 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
   }
 }
 
-// Register budget of the persistent segment kernel: the J = 4 layout (32 accumulator registers) is
-// capped at 80 registers per thread so that more warps stay resident (it measured faster than at 96
-// or 128); J = 8 keeps the 128 that 512 threads allow.
+// Default register budget of the persistent segment kernel: the J = 4 layout (32 accumulator
+// registers) is capped at 80 registers per thread so that more warps stay resident; J = 8 keeps the
+// 128 that 512 threads allow.  The w-projection visibility launches also offer J = 4 builds at 64 and
+// 72 registers to the tuner (different support classes prefer different caps).
 template <int J>
 constexpr int kSegRegs = J == 4 ? 80 : 128;
 
@@ -994,8 +995,8 @@ __global__ void __launch_bounds__(512, 1) romein_grid_kernel(const GridArgs a) {
 // whose w planes share this launch's support class (a.W).  Items of one segment are adjacent, so
 // the facets of a segment are gridded while its rows are hot in L2.  The loop ends on the count,
 // never waits on other CTAs.
-template <int NC, bool WPROJ, int J, bool COMP, bool WIDE>
-__global__ void __launch_bounds__(512, 1) __maxnreg__(kSegRegs<J>) romein_segment_kernel(const GridArgs a, const int nfacets) {
+template <int NC, bool WPROJ, int J, bool COMP, bool WIDE, int REGS = kSegRegs<J>>
+__global__ void __launch_bounds__(512, 1) __maxnreg__(REGS) romein_segment_kernel(const GridArgs a, const int nfacets) {
   __shared__ int s_item;
   const int count = *a.work_count;
   const long long total = (long long)count * nfacets;
