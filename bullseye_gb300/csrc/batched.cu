@@ -320,7 +320,7 @@ bool plan_classes() {
   BZ_CUDA_TRY_RET(cudaMemcpy(b.plane_class.ptr, pcls.data(), sizeof(int) * P, cudaMemcpyHostToDevice), false);
   BZ_CUDA_TRY_RET(cudaMemcpy(b.plane_lo.ptr, plo.data(), sizeof(int) * P, cudaMemcpyHostToDevice), false);
   if (!b.class_count.alloc(kMaxClasses) || !b.class_off.alloc(kMaxClasses) || !b.class_cursor.alloc(kMaxClasses) ||
-      !b.work_next.alloc(2 * kMaxClasses) || !b.seg_total.alloc(1) || !b.sample_count.alloc(3 * kMaxClasses))
+      !b.work_next.alloc(2 * kMaxClasses) || !b.seg_total.alloc(1) || !b.sample_count.alloc(2 * kMaxClasses))
     return false;
   b.planned = true;
   return true;
@@ -442,52 +442,31 @@ bool tune_class(const GridArgs &base, int k, int nfacets, Variant &out, int host
   }
   // Each candidate grids a quarter of the class's runs (at least 4096, when there are that many)
   // into the scratch grid (no effect on results): smaller samples leave the persistent grid
-  // underfilled and favour the wrong layout.  A short first launch loads the variant's code.  The
-  // three fastest are then timed again on the whole class, which decides.
-  const int counts3[3] = {std::min(host_count, 64), std::min(host_count, std::max(4096, host_count / 4)), host_count};
-  BZ_CUDA_TRY_RET(cudaMemcpyAsync(b.sample_count.ptr + 3 * k, counts3, sizeof(counts3), cudaMemcpyHostToDevice, c.stream),
+  // underfilled and favour the wrong layout.  A short first launch loads the variant's code.
+  const int counts2[2] = {std::min(host_count, 64), std::min(host_count, std::max(4096, host_count / 4))};
+  BZ_CUDA_TRY_RET(cudaMemcpyAsync(b.sample_count.ptr + 2 * k, counts2, sizeof(counts2), cudaMemcpyHostToDevice, c.stream),
                   false);
   BZ_CUDA_TRY_RET(cudaStreamSynchronize(c.stream), false);
   GridArgs a = base;
   a.grid = c.scratch.ptr;
   a.grid_lo = COMP ? c.scratch.ptr : nullptr;
   a.norm = nullptr;
+  float best = 1e30f;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  auto time_one = [&](const Variant &v, int slot, float &ms) -> bool {
-    cudaEventRecord(e0, c.stream);
-    const bool ok = launch_class<NC, WPROJ, COMP>(a, k, v, nfacets, b.sample_count.ptr + 3 * k + slot, b.work_next.ptr + k,
-                                                  c.stream);
-    cudaEventRecord(e1, c.stream);
-    cudaEventSynchronize(e1);
-    cudaEventElapsedTime(&ms, e0, e1);
-    return ok;
-  };
-  std::vector<std::pair<float, int>> screen;
-  for (int i = 0; i < (int)cands.size(); ++i) {
-    float ms = 0;
-    // slot 0 (a short launch) loads the code; slot 1 is the quarter sample
-    if (!launch_class<NC, WPROJ, COMP>(a, k, cands[i], nfacets, b.sample_count.ptr + 3 * k, b.work_next.ptr + k, c.stream))
+  for (auto &v : cands) {
+    if (!launch_class<NC, WPROJ, COMP>(a, k, v, nfacets, b.sample_count.ptr + 2 * k, b.work_next.ptr + k, c.stream))
       break;
     cudaEventRecord(e0, c.stream);
-    if (!launch_class<NC, WPROJ, COMP>(a, k, cands[i], nfacets, b.sample_count.ptr + 3 * k + 1, b.work_next.ptr + k,
-                                       c.stream))
-      break;
+    launch_class<NC, WPROJ, COMP>(a, k, v, nfacets, b.sample_count.ptr + 2 * k + 1, b.work_next.ptr + k, c.stream);
     cudaEventRecord(e1, c.stream);
     cudaEventSynchronize(e1);
-    cudaEventElapsedTime(&ms, e0, e1);
-    screen.push_back({ms, i});
-  }
-  std::sort(screen.begin(), screen.end());
-  float best = 1e30f;
-  out = cands[screen.empty() ? 0 : screen[0].second];
-  for (int r = 0; r < (int)screen.size() && r < 3 && host_count > counts3[1]; ++r) {
     float ms = 0;
-    if (!time_one(cands[screen[r].second], 2, ms)) break;
+    cudaEventElapsedTime(&ms, e0, e1);
     if (ms < best) {
       best = ms;
-      out = cands[screen[r].second];
+      out = v;
     }
   }
   cudaEventDestroy(e0);
