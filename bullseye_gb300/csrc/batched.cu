@@ -156,8 +156,7 @@ __global__ void bucket_kernel(const int4 *__restrict__ segs, const int *total, i
 struct Variant {
   int J;
   bool wide;
-  int regs;    // register cap of the build
-  bool direct; // taps read from the support-window table instead of staged in shared memory
+  int regs;  // register cap of the build
   int NT, V, grid;
   size_t smem;
 };
@@ -189,19 +188,18 @@ std::vector<int> reg_caps(int J) {
 }
 
 template <int NC, bool WPROJ>
-bool make_variant(int W, int J, bool wide, int regs, bool direct, Variant &v) {
+bool make_variant(int W, int J, bool wide, int regs, Variant &v) {
   const int cols = ((W + 31) / 32) * 32;
   if (wide && (cols - W) * 8 > W) return false;
   const int owners = wide ? cols * ((W + J - 1) / J) : W * ((W + J - 1) / J);
   v.J = J;
   v.wide = wide;
   v.regs = regs;
-  v.direct = direct;
   v.NT = std::max(32, ((owners + 31) / 32) * 32);
   if (v.NT > 512) return false;
-  // direct: taps come from the support-window table, nothing staged (width 0 in the sizing)
-  v.V = grid_chunk_size<NC, WPROJ>(direct ? 0 : W, v.NT, direct ? 1 : J, regs);
-  v.smem = grid_smem_bytes<NC, WPROJ>(v.V, direct ? 0 : W, v.NT, direct ? 1 : J);
+  // taps come from the support-window table: nothing staged (width 0 in the sizing)
+  v.V = grid_chunk_size<NC, WPROJ>(0, v.NT, 1, regs);
+  v.smem = grid_smem_bytes<NC, WPROJ>(v.V, 0, v.NT, 1);
   return true;
 }
 
@@ -223,7 +221,7 @@ struct BatchedState {
   DevBuf<FacetXform> facet_table;  // per-facet geometry of bullseye_grid_batched_facets
   size_t rows_cap = 0, tracks_cap = 0, segs_cap = 0;
   // tuning decisions, by (class width, NC, WPROJ, COMP)
-  std::map<std::tuple<int, int, int, int>, std::tuple<int, int, int, int>> tuned;  // -> (J, wide, regs, direct)
+  std::map<std::tuple<int, int, int, int>, std::tuple<int, int, int>> tuned;  // -> (J, wide, regs)
   // captured graph
   cudaGraphExec_t exec = nullptr;
   std::vector<unsigned char> key;
@@ -374,8 +372,8 @@ bool launch_class(const GridArgs &base, int k, const Variant &v, int nfacets, co
   a.W = g_bs.cls[k].width;
   a.V = v.V;
   a.plane_lo = g_bs.plane_lo.ptr;
-  a.tap_win = v.direct ? g_bs.tap_win.ptr : nullptr;
-  a.tap_win_off = v.direct ? g_bs.tap_win_off.ptr : nullptr;
+  a.tap_win = g_bs.tap_win.ptr;
+  a.tap_win_off = g_bs.tap_win_off.ptr;
   a.segments = g_bs.sorted.ptr;
   a.segment_base = g_bs.class_off.ptr + k;
   a.segment_capacity = (long long)g_bs.segs_cap;
@@ -417,27 +415,24 @@ bool tune_class(const GridArgs &base, int k, int nfacets, Variant &out, int host
   std::vector<Variant> cands;
   for (int J : {8, 4})
     for (bool wide : {true, false})
-      for (int regs : reg_caps<NC, WPROJ>(J))
-        for (bool direct : {false, true}) {
-          Variant v;
-          if (make_variant<NC, WPROJ>(W, J, wide, regs, direct, v) && finish_variant<NC, WPROJ, COMP>(v))
-            cands.push_back(v);
-        }
+      for (int regs : reg_caps<NC, WPROJ>(J)) {
+        Variant v;
+        if (make_variant<NC, WPROJ>(W, J, wide, regs, v) && finish_variant<NC, WPROJ, COMP>(v)) cands.push_back(v);
+      }
   if (cands.empty()) {
     bz_record_error(BZ_ERR_UNSUPPORTED, "batched: no layout for support class %d", W);
     return false;
   }
   if (it != b.tuned.end()) {
     for (auto &v : cands)
-      if (v.J == std::get<0>(it->second) && (int)v.wide == std::get<1>(it->second) && v.regs == std::get<2>(it->second) &&
-          (int)v.direct == std::get<3>(it->second)) {
+      if (v.J == std::get<0>(it->second) && (int)v.wide == std::get<1>(it->second) && v.regs == std::get<2>(it->second)) {
         out = v;
         return true;
       }
   }
   if (cands.size() == 1 || host_count == 0) {
     out = cands[0];
-    b.tuned[key] = std::make_tuple(out.J, (int)out.wide, out.regs, (int)out.direct);
+    b.tuned[key] = std::make_tuple(out.J, (int)out.wide, out.regs);
     return true;
   }
   // Each candidate grids a quarter of the class's runs (at least 4096, when there are that many)
@@ -472,7 +467,7 @@ bool tune_class(const GridArgs &base, int k, int nfacets, Variant &out, int host
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   BZ_CUDA_TRY_RET(cudaMemsetAsync(c.scratch.ptr, 0, sizeof(vis_complex) * c.scratch.n, c.stream), false);
-  b.tuned[key] = std::make_tuple(out.J, (int)out.wide, out.regs, (int)out.direct);
+  b.tuned[key] = std::make_tuple(out.J, (int)out.wide, out.regs);
   return bz_error_code() == BZ_OK;
 }
 
@@ -505,8 +500,7 @@ bool launch_all(const GridArgs &base, int nfacets, bool sampling, cudaStream_t s
       cudaEventElapsedTime(&ms, e0, e1);
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
-      b.records.push_back({b.cls[k].width, NC, v.J, (int)v.wide | ((int)v.direct << 1) | (v.regs << 2),
-                           counts ? (*counts)[k] * nfacets : 0, ms});
+      b.records.push_back({b.cls[k].width, NC, v.J, (int)v.wide | (v.regs << 1), counts ? (*counts)[k] * nfacets : 0, ms});
     }
     if (!ok) return false;
   }
