@@ -197,9 +197,8 @@ bool make_variant(int W, int J, bool wide, int regs, Variant &v) {
   v.regs = regs;
   v.NT = std::max(32, ((owners + 31) / 32) * 32);
   if (v.NT > 512) return false;
-  // taps come from the support-window table: nothing staged (width 0 in the sizing)
-  v.V = grid_chunk_size<NC, WPROJ>(0, v.NT, 1, regs);
-  v.smem = grid_smem_bytes<NC, WPROJ>(v.V, 0, v.NT, 1);
+  v.V = grid_chunk_size<NC, WPROJ>(W, v.NT, J, regs);
+  v.smem = grid_smem_bytes<NC, WPROJ>(v.V, W, v.NT, J);
   return true;
 }
 
@@ -216,8 +215,6 @@ struct BatchedState {
   DevBuf<unsigned char> row_class;
   DevBuf<int> nseg, seg_off, seg_total, class_count, class_off, class_cursor, work_next, sample_count;
   DevBuf<int4> segs, sorted;
-  DevBuf<vis_real> tap_win;  // support-window tap table (plan_classes)
-  DevBuf<int> tap_win_off;
   DevBuf<FacetXform> facet_table;  // per-facet geometry of bullseye_grid_batched_facets
   size_t rows_cap = 0, tracks_cap = 0, segs_cap = 0;
   // tuning decisions, by (class width, NC, WPROJ, COMP)
@@ -283,34 +280,6 @@ bool plan_classes() {
   std::vector<int> pcls(P);
   for (int p = 0; p < P; ++p) pcls[p] = (int)(std::find(widths.begin(), widths.end(), pw[p]) - widths.begin());
   b.plane_width = pw;
-  {
-    // support-window tap table: for plane p (class width cw) and tap offset f, the cw window taps
-    // conv[p][f + (lo + j) os] followed by the first 7 again, so that a thread's J <= 8 owned
-    // rows read consecutive taps
-    const size_t ncomp = wproj ? 2 : 1;
-    const int F = (int)c.tap_f;
-    std::vector<int> off(P);
-    size_t total = 0;
-    for (int p = 0; p < P; ++p) {
-      off[p] = (int)total;
-      total += (size_t)F * (pw[p] + 7);
-    }
-    std::vector<vis_real> tab(ncomp * total, (vis_real)0);
-    for (int p = 0; p < P; ++p)
-      for (int f = 0; f < F; ++f) {
-        const size_t rb = (size_t)off[p] + (size_t)f * (pw[p] + 7);
-        for (int j = 0; j < pw[p] + 7; ++j) {
-          const int jj = j < pw[p] ? j : j - pw[p];
-          const long long i = f + (long long)(plo[p] + jj) * os;
-          if (i >= K) continue;
-          for (size_t q = 0; q < ncomp; ++q)
-            tab[ncomp * (rb + j) + q] = c.conv_host[ncomp * ((size_t)p * K + i) + q];
-        }
-      }
-    if (!b.tap_win.alloc(tab.size()) || !b.tap_win_off.alloc(P)) return false;
-    BZ_CUDA_TRY_RET(cudaMemcpy(b.tap_win.ptr, tab.data(), sizeof(vis_real) * tab.size(), cudaMemcpyHostToDevice), false);
-    BZ_CUDA_TRY_RET(cudaMemcpy(b.tap_win_off.ptr, off.data(), sizeof(int) * P, cudaMemcpyHostToDevice), false);
-  }
   b.ncls = (int)widths.size();
   if (b.ncls > kMaxClasses) return false;
   for (int k = 0; k < b.ncls; ++k) b.cls[k].width = widths[k];
@@ -372,8 +341,6 @@ bool launch_class(const GridArgs &base, int k, const Variant &v, int nfacets, co
   a.W = g_bs.cls[k].width;
   a.V = v.V;
   a.plane_lo = g_bs.plane_lo.ptr;
-  a.tap_win = g_bs.tap_win.ptr;
-  a.tap_win_off = g_bs.tap_win_off.ptr;
   a.segments = g_bs.sorted.ptr;
   a.segment_base = g_bs.class_off.ptr + k;
   a.segment_capacity = (long long)g_bs.segs_cap;
@@ -561,7 +528,7 @@ void bz_release_batched() {
   b.key.clear();
   b.plane_class.release(); b.plane_lo.release(); b.row_class.release(); b.nseg.release(); b.seg_off.release();
   b.seg_total.release(); b.class_count.release(); b.class_off.release(); b.class_cursor.release();
-  b.work_next.release(); b.sample_count.release(); b.segs.release(); b.sorted.release(); b.tap_win.release(); b.tap_win_off.release(); b.facet_table.release();
+  b.work_next.release(); b.sample_count.release(); b.segs.release(); b.sorted.release(); b.facet_table.release();
   b.rows_cap = b.tracks_cap = b.segs_cap = 0;
   b.planned = false;
   b.ncls = 0;

@@ -93,11 +93,6 @@ struct GridArgs {
   int tap_f;
   const void *conv_t;            // kernel regrouped by tap offset [P][tap_f][W], or null
   const uint8_t *facet_row_mask; // [facets][rows]: 0 leaves the row out of that facet, or null
-  // support-window tap table (batched launches): for plane p and tap offset f, the row of W + 7
-  // taps starting at tap_win_off[p] + f * (W + 7): the plane's window, then its first 7 taps again.
-  // When set, the multiply-add loop reads taps from it directly and nothing is staged.
-  const void *tap_win;
-  const int *tap_win_off;
   const FacetXform *facets;
   // outputs
   vis_complex *grid;             // slices [(f*groups + g)*NC + k][ny][nx]
@@ -560,12 +555,7 @@ __device__ __forceinline__ void prologue(const GridArgs &a, int f_local, int cha
     rec.fu += lo * a.os;
     rec.fv += lo * a.os;
   }
-  if (a.tap_win) {
-    // first tap of the visibility's rows in the support-window table (the window shift is in it)
-    const long long row0 = (long long)a.tap_win_off[plane];
-    rec.fu = (int)(row0 + (long long)cell.fu * (a.W + 7));
-    rec.fv = (int)(row0 + (long long)cell.fv * (a.W + 7));
-  } else if (a.conv_t) {
+  if (a.conv_t) {
     // index of the first staged tap in the regrouped table
     const int Wfull = a.W_full ? a.W_full : a.W;
     rec.fu = (int)(((long long)plane * a.tap_f + cell.fu) * Wfull + lo);
@@ -673,9 +663,8 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
   int *s_mixed = s_ng + a.V;                                                          // [V]
   int *s_runs = s_mixed + a.V;  // [V + 1]: first slot of every run of the staged chunk, then nv
   tap_t *tu = reinterpret_cast<tap_t *>(smem_raw + stage_head_bytes<NC>(a.V));
-  // row-tap stride per staged visibility (no staged taps with a support-window table)
-  const int TVS = a.tap_win ? 0 : a.W + J - 1;
-  tap_t *tv = tu + (a.tap_win ? 0 : a.V * a.W);
+  const int TVS = a.W + J - 1;  // row-tap stride per staged visibility
+  tap_t *tv = tu + a.V * a.W;
   // per-warp flush queues follow the taps
   unsigned char *qbase = reinterpret_cast<unsigned char *>(tv + a.V * TVS);
   qbase = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(qbase) + 15) & ~(uintptr_t)15);
@@ -788,7 +777,7 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
       const int per = W + TVS;
       int vi = tid / per, j = tid - vi * per;
       const int svi = (int)blockDim.x / per, sj = (int)blockDim.x - svi * per;
-      while (vi < (a.tap_win ? 0 : nv)) {
+      while (vi < nv) {
         const int4 h1 = *reinterpret_cast<const int4 *>(&recs[vi].g);  // g, valid, fu, fv
         if (h1.y) {
           const bool isv = j >= W;
@@ -918,26 +907,6 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
         // the run's visibilities share the owned cells: a branch-free multiply-add loop over
         // the J owned rows (offsets modulo W; rows of non-owning lanes stay in bounds and are
         // never flushed)
-        if (a.tap_win) {
-          const tap_t *tw = reinterpret_cast<const tap_t *>(a.tap_win);
-#pragma unroll 2
-          for (int vi = rs; vi < re; ++vi) {
-            const int4 h1 = *reinterpret_cast<const int4 *>(&recs[vi].g);
-            const tap_t tuv = tw[h1.z + ou];
-            cplx pre[NC];
-#pragma unroll
-            for (int k = 0; k < NC; ++k) pre[k] = premul(recs[vi].vis[k], tuv);
-            const tap_t *tvrow = tw + h1.w + ov0;
-#pragma unroll
-            for (int j = 0; j < J; ++j) {
-              const tap_t t = tvrow[j];
-#pragma unroll
-              for (int k = 0; k < NC; ++k) mac(acc[j][k], pre[k], t);
-            }
-          }
-          dirty = rows_mask;
-          continue;
-        }
 #pragma unroll 2
         for (int vi = rs; vi < re; ++vi) {
           const tap_t tuv = tu[vi * W + ou];
