@@ -163,7 +163,7 @@ def class_profile(lib, step, counts, plane_width):
         vis, t = taps.get(int(width[i]), (0, 0.0))
         flops = t * (N_FACETS * 8 * 4 if nc[i] == 4 else 8)
         rows.append({"width": int(width[i]), "corr": int(nc[i]), "J": int(J[i]), "wide": bool(wide[i] & 1),
-                     "registers": int(wide[i]) >> 1,
+                     "registers": (int(wide[i]) >> 1) & 255, "pipelined": bool(int(wide[i]) >> 9 & 1),
                      "work_items": int(items[i]), "vis": vis, "ms": float(ms[i]),
                      "executed_tflops": flops / (float(ms[i]) * 1e-3) / 1e12 if ms[i] > 0 else None})
     return rows

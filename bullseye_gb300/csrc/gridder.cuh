@@ -35,6 +35,7 @@
 //    Re(sum_j k_u[j] * sum_i k_v[i]).
 #pragma once
 #include <algorithm>
+#include <type_traits>
 
 #include "common.h"
 
@@ -588,30 +589,44 @@ __host__ __device__ inline size_t flush_queue_bytes(int nwarps) {
 // Row taps are stored W + J - 1 long per visibility: the first J - 1 taps are repeated after the
 // last, so a thread's J consecutive owned rows read J consecutive taps without a wrap.
 
-// Bytes before the tap arrays: V staged records, their normalisation state (partial sums, grid
-// group, mixed flag), the V + 1 run starts of the chunk; rounded up to 16.
-template <int NC>
+// Staging depth.  The plain loop stages one chunk at a time: one record buffer, one tap buffer, one
+// run list, three CTA barriers per chunk.  The pipelined loop of the persistent kernel runs the
+// prologue two chunks ahead and the tap staging one chunk ahead of the multiply-adds, all in one
+// phase with one CTA barrier per chunk: three record buffers, two tap buffers, two run lists.
+template <bool PIPE>
+struct StageDepth {
+  static constexpr int recs = PIPE ? 3 : 1;
+  static constexpr int taps = PIPE ? 2 : 1;
+};
+
+// Bytes before the tap arrays: the staged-record buffers, the normalisation state of the V staging
+// slots (partial sums, grid group, mixed flag), the run lists (V + 1 run starts each); rounded up
+// to 16.
+template <int NC, bool PIPE = false>
 __host__ __device__ inline size_t stage_head_bytes(int V) {
-  return ((sizeof(VisRec<NC>) + sizeof(double) * NC + 3 * sizeof(int)) * (size_t)V + sizeof(int) + 15) / 16 * 16;
+  constexpr int R = StageDepth<PIPE>::recs, T = StageDepth<PIPE>::taps;
+  return ((R * sizeof(VisRec<NC>) + sizeof(NormAcc) * NC + (2 + T) * sizeof(int)) * (size_t)V + T * sizeof(int) +
+          15) / 16 * 16;
 }
 
-template <int NC, bool WPROJ>
+template <int NC, bool WPROJ, bool PIPE = false>
 __host__ __device__ inline size_t grid_smem_bytes(int V, int W, int nthreads, int J) {
-  size_t taps = sizeof(typename TapT<WPROJ>::type) * (size_t)V * (2 * W + J - 1);
-  return stage_head_bytes<NC>(V) + taps + flush_queue_bytes<NC>((nthreads + 31) / 32) + 64;
+  size_t taps = StageDepth<PIPE>::taps * sizeof(typename TapT<WPROJ>::type) * (size_t)V * (2 * W + J - 1);
+  return stage_head_bytes<NC, PIPE>(V) + taps + flush_queue_bytes<NC>((nthreads + 31) / 32) + 64;
 }
 
 // Staged-chunk size V for a CTA of nthreads: one visibility per thread at most, and shared memory
-// small enough that the CTAs the register file allows (128 registers per thread) fit on an SM.
-template <int NC, bool WPROJ>
+// small enough that the CTAs the register file allows (regs registers per thread) fit on an SM.
+template <int NC, bool WPROJ, bool PIPE = false>
 __host__ inline int grid_chunk_size(int W, int nthreads, int J, int regs = 128) {
+  constexpr int R = StageDepth<PIPE>::recs, T = StageDepth<PIPE>::taps;
   const int ctas = std::max(1, std::min(8, 65536 / (nthreads * regs)));
   const size_t smem_sm = 227 * 1024;
   size_t budget = std::min<size_t>(200 * 1024, smem_sm / ctas - 1024);
-  const size_t fixed = flush_queue_bytes<NC>((nthreads + 31) / 32) + 64 + sizeof(int) + 15;
+  const size_t fixed = flush_queue_bytes<NC>((nthreads + 31) / 32) + 64 + T * sizeof(int) + 15;
   budget = budget > fixed ? budget - fixed : 0;
-  const size_t per = sizeof(VisRec<NC>) + sizeof(double) * NC + 3 * sizeof(int) +
-                     sizeof(typename TapT<WPROJ>::type) * (2 * (size_t)W + J - 1);
+  const size_t per = R * sizeof(VisRec<NC>) + sizeof(NormAcc) * NC + (2 + T) * sizeof(int) +
+                     T * sizeof(typename TapT<WPROJ>::type) * (2 * (size_t)W + J - 1);
   return std::max(1, (int)std::min<size_t>(nthreads, budget / per));
 }
 
@@ -652,31 +667,305 @@ __device__ __forceinline__ void owner_map(int tid, int W, int J, int &du, int &s
   }
 }
 
-template <int NC, bool WPROJ, int J, bool COMP, bool WIDE>
+// Register state of a Romein owner thread: the accumulators of its J cells and the footprint they
+// belong to.  For the last footprint corner (pu0, pv0) the owned cells are
+// (pu0 + ou, pv0 + wrap(ov0 + j)), wrap(i) = i - W when i >= W.
+template <int NC, int J>
+struct OwnerState {
+  cplx acc[J][NC];
+  unsigned dirty;
+  int cg, pu0, pv0, ou, ov0;
+};
+
+// Prologue of one staging slot: the visibility of `row` staged into recs[slot] and, with the
+// precomputed row sums, its normalisation term added to the slot's running sums (which go to the
+// global normalisation when the slot's grid group changes).
+template <int NC, bool WPROJ>
+__device__ __forceinline__ void stage_slot(const GridArgs &a, int f_local, int chan, long long row, bool in_range,
+                                           int slot, VisRec<NC> *recs, NormAcc *s_nacc, int *s_ng, int *s_mixed,
+                                           long long fslice, ChanCache &cc, double plane_scale) {
+  VisRec<NC> rec;
+  prologue<NC, WPROJ>(a, f_local, chan, row, in_range, rec, cc, plane_scale);
+  recs[slot] = rec;
+  if (a.norm && a.tap_sums && rec.valid) {
+    const double *su = a.tap_sums + 2 * ((long long)rec.plane * a.tap_f + rec.fu0);
+    const double *sv = a.tap_sums + 2 * ((long long)rec.plane * a.tap_f + rec.fv0);
+    const NormTerm nt = (NormTerm)(su[0] * sv[0] - su[1] * sv[1]);
+    NormAcc *na = s_nacc + slot * NC;
+    if (s_ng[slot] != rec.g) {
+      if (s_ng[slot] >= 0) {
+        s_mixed[slot] = 1;
+#pragma unroll
+        for (int k = 0; k < NC; ++k)
+          if (norm_value(na[k]) != 0.0) atomicAdd(&a.norm[(fslice + s_ng[slot]) * NC + k], norm_value(na[k]));
+      }
+#pragma unroll
+      for (int k = 0; k < NC; ++k) norm_zero(na[k]);
+      s_ng[slot] = rec.g;
+    }
+#pragma unroll
+    for (int k = 0; k < NC; ++k) norm_add(na[k], (NormTerm)rec.cw[k] * nt);
+  }
+}
+
+// Runs of a staged chunk, found by one warp: maximal stretches of valid staged visibilities with
+// one footprint corner and grid group (a Romein thread keeps its cells across a run); an invalid
+// slot is a run of its own.  runs[0..n) are the first slots of the runs, runs[n] = nv.
+template <int NC>
+__device__ __forceinline__ void find_runs(const VisRec<NC> *recs, int nv, int *runs, int *nruns) {
+  const int lane = threadIdx.x & 31;
+  int count = 0;
+  for (int b = 0; b < nv; b += 32) {
+    const int t = b + lane;
+    bool start = false;
+    if (t < nv) {
+      const int4 c0 = *reinterpret_cast<const int4 *>(&recs[t].u0);
+      const int4 c1 = *reinterpret_cast<const int4 *>(&recs[t].g);
+      start = !c1.y || t == 0;
+      if (!start) {
+        const int4 p0 = *reinterpret_cast<const int4 *>(&recs[t - 1].u0);
+        const int4 p1 = *reinterpret_cast<const int4 *>(&recs[t - 1].g);
+        start = !p1.y || p0.x != c0.x || p0.y != c0.y || p1.x != c1.x;
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, start);
+    if (start) runs[count + __popc(m & ((1u << lane) - 1u))] = t;
+    count += __popc(m);
+  }
+  if (lane == 0) {
+    runs[count] = nv;
+    *nruns = count;
+  }
+}
+
+// Asynchronous global -> shared copy of one tap (cp.async: no register staging, so a thread has its
+// whole share of a chunk's taps in flight at once).  Kernel tables are stored in the working
+// precision, so a tap is copied as it is (4, 8 or 16 bytes, aligned to its size).
+template <int BYTES>
+__device__ __forceinline__ void copy_tap_async(void *dst_smem, const void *src) {
+  static_assert(BYTES == 4 || BYTES == 8 || BYTES == 16, "cp.async copies 4, 8 or 16 bytes");
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(d), "l"(src), "n"(BYTES) : "memory");
+}
+// Waits for this thread's outstanding tap copies; a CTA barrier then publishes them.
+__device__ __forceinline__ void wait_taps() { asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory"); }
+
+// Taps of every valid staged visibility: W column taps, then W + J - 1 row taps, issued as
+// asynchronous copies (the caller runs wait_taps() before the barrier that publishes them).  Thread
+// tid walks (visibility, tap) pairs with a stride of blockDim.x pairs, stepped without division.
+template <int NC, bool WPROJ>
+__device__ __forceinline__ void stage_taps(const GridArgs &a, const VisRec<NC> *recs, int nv, int TVS,
+                                           typename TapT<WPROJ>::type *tu, typename TapT<WPROJ>::type *tv) {
+  typedef typename TapT<WPROJ>::type tap_t;
+  typedef typename std::conditional<WPROJ, vis_complex, vis_real>::type stored_t;
+  static_assert(sizeof(stored_t) == sizeof(tap_t), "kernel tables are stored in the working precision");
+  const stored_t *table = reinterpret_cast<const stored_t *>(a.conv_t ? a.conv_t : a.conv);
+  // a caller-owned table (the allocation-free entries) may be only element-part aligned: such a
+  // table is read through registers
+  const bool aligned = (reinterpret_cast<uintptr_t>(table) & (sizeof(tap_t) - 1)) == 0;
+  const int W = a.W;
+  const int per = W + TVS;
+  const int tid = threadIdx.x;
+  int vi = tid / per, j = tid - vi * per;
+  const int svi = (int)blockDim.x / per, sj = (int)blockDim.x - svi * per;
+  while (vi < nv) {
+    const int4 h1 = *reinterpret_cast<const int4 *>(&recs[vi].g);  // g, valid, fu, fv
+    if (h1.y) {
+      const bool isv = j >= W;
+      const int js = isv ? j - W : j;  // slot in the staged row
+      int jj = js >= W ? js - W : js;  // repeated leading row taps
+      if (jj >= W) jj = W - 1;
+      const long long idx = a.conv_t ? (long long)(isv ? h1.w : h1.z) + jj
+                                     : (long long)recs[vi].plane * a.K + (isv ? h1.w : h1.z) + (long long)jj * a.os;
+      tap_t *dst = isv ? &tv[vi * TVS + js] : &tu[vi * W + js];
+      if (aligned) {
+        copy_tap_async<sizeof(tap_t)>(dst, table + idx);
+      } else {
+        load_tap(table, idx, *dst);
+      }
+    }
+    vi += svi;
+    j += sj;
+    if (j >= per) {
+      j -= per;
+      ++vi;
+    }
+  }
+}
+
+// Normalisation without precomputed row sums (the allocation-free entry), four lanes per staged
+// visibility: Re(sum_u k_u * sum_v k_v) x weight x flag (loop bounds are warp-uniform so the
+// shuffles always see full warps); lane 4i owns the running sums of staged slot i.
+template <int NC, bool WPROJ>
+__device__ __forceinline__ void norm_from_taps(const GridArgs &a, const VisRec<NC> *recs, int nv, int TVS,
+                                               const typename TapT<WPROJ>::type *tu,
+                                               const typename TapT<WPROJ>::type *tv, NormAcc *s_nacc, int *s_ng,
+                                               int *s_mixed, long long fslice) {
+  const int W = a.W;
+  const int tid = threadIdx.x;
+  for (int b4 = tid & ~31; b4 < 4 * nv; b4 += blockDim.x) {
+    const int q = b4 + (tid & 31);
+    const int vi = q >> 2, part = q & 3;
+    const bool act = vi < nv;
+    // tap sums in the library's working precision (FP64 units are scarce on this GPU)
+    acc_real sur = 0, sui = 0, svr = 0, svi = 0;
+    if (act) {
+      if (WPROJ) {
+        const cplx *pu = reinterpret_cast<const cplx *>(tu) + vi * W;
+        const cplx *pv = reinterpret_cast<const cplx *>(tv) + vi * TVS;
+        for (int j = part; j < W; j += 4) { sur += pu[j].re; sui += pu[j].im; svr += pv[j].re; svi += pv[j].im; }
+      } else {
+        const acc_real *pu = reinterpret_cast<const acc_real *>(tu) + vi * W;
+        const acc_real *pv = reinterpret_cast<const acc_real *>(tv) + vi * TVS;
+        for (int j = part; j < W; j += 4) { sur += pu[j]; svr += pv[j]; }
+      }
+    }
+#pragma unroll
+    for (int off = 1; off < 4; off <<= 1) {
+      sur += __shfl_xor_sync(0xffffffffu, sur, off);
+      sui += __shfl_xor_sync(0xffffffffu, sui, off);
+      svr += __shfl_xor_sync(0xffffffffu, svr, off);
+      svi += __shfl_xor_sync(0xffffffffu, svi, off);
+    }
+    if (act && part == 0 && recs[vi].valid) {
+      const VisRec<NC> &r = recs[vi];
+      const NormTerm nt = (NormTerm)sur * (NormTerm)svr - (NormTerm)sui * (NormTerm)svi;
+      NormAcc *na = s_nacc + vi * NC;
+      if (s_ng[vi] != r.g) {
+        if (s_ng[vi] >= 0) {
+          s_mixed[vi] = 1;
+#pragma unroll
+          for (int k = 0; k < NC; ++k)
+            if (norm_value(na[k]) != 0.0) atomicAdd(&a.norm[(fslice + s_ng[vi]) * NC + k], norm_value(na[k]));
+        }
+#pragma unroll
+        for (int k = 0; k < NC; ++k) norm_zero(na[k]);
+        s_ng[vi] = r.g;
+      }
+#pragma unroll
+      for (int k = 0; k < NC; ++k) norm_add(na[k], (NormTerm)r.cw[k] * nt);
+    }
+  }
+}
+
+// Multiply-adds of a staged chunk's runs into an owner thread's cells.  When the footprint moves,
+// the owned cells are recomputed and those that changed are flushed (queued for the warp's
+// compensated flush in single precision).  Every lane of a warp with any owned cell calls this, so
+// the queue drains are warp-uniform.
+template <int NC, bool WPROJ, int J, bool COMP>
+__device__ __forceinline__ void grid_runs(const GridArgs &a, const VisRec<NC> *recs,
+                                          const typename TapT<WPROJ>::type *tu,
+                                          const typename TapT<WPROJ>::type *tv, const int *runs, int nruns,
+                                          int TVS, int du, int strip, unsigned rows_mask, long long fbase,
+                                          long long nxy, int gnx, FlushRec<NC> *fq, int *fqn,
+                                          OwnerState<NC, J> &st) {
+  typedef typename TapT<WPROJ>::type tap_t;
+  const int W = a.W;
+  for (int ri = 0; ri < nruns; ++ri) {
+    const int rs = runs[ri], re = runs[ri + 1];
+    const int4 h0 = *reinterpret_cast<const int4 *>(&recs[rs].u0);
+    const int4 h1 = *reinterpret_cast<const int4 *>(&recs[rs].g);
+    if (!h1.y) continue;
+    if (h0.x != st.pu0 || h0.y != st.pv0 || h1.x != st.cg) {
+      // footprint moved: recompute the owned cells, flush those that changed
+      int o = du - h0.z;
+      o += (o < 0) ? W : 0;
+      int nov0 = strip * J - h0.w;
+      nov0 += (nov0 < 0) ? W : 0;
+      if (h0.x + o != st.pu0 + st.ou || h1.x != st.cg) {
+        if (st.dirty) {
+#pragma unroll
+          for (int j = 0; j < J; ++j)
+            if (st.dirty & (1u << j)) {
+              const int oy = st.ov0 + j >= W ? st.ov0 + j - W : st.ov0 + j;
+              if (COMP)
+                queue_cell<NC>(a, fbase + (long long)st.cg * NC * nxy, nxy, gnx, st.pu0 + st.ou, st.pv0 + oy,
+                               st.acc[j], fq, fqn);
+              else
+                flush_cell<NC, false>(a, fbase + (long long)st.cg * NC * nxy, nxy, gnx, st.pu0 + st.ou,
+                                      st.pv0 + oy, st.acc[j]);
+            }
+          st.dirty = 0;
+        }
+        st.cg = h1.x;
+      }
+      if (st.dirty) {
+#pragma unroll
+        for (int j = 0; j < J; ++j) {
+          const int oy = st.ov0 + j >= W ? st.ov0 + j - W : st.ov0 + j;
+          const int ny = nov0 + j >= W ? nov0 + j - W : nov0 + j;
+          if ((st.dirty & (1u << j)) && h0.y + ny != st.pv0 + oy) {
+            if (COMP)
+              queue_cell<NC>(a, fbase + (long long)st.cg * NC * nxy, nxy, gnx, st.pu0 + st.ou, st.pv0 + oy,
+                             st.acc[j], fq, fqn);
+            else
+              flush_cell<NC, false>(a, fbase + (long long)st.cg * NC * nxy, nxy, gnx, st.pu0 + st.ou, st.pv0 + oy,
+                                    st.acc[j]);
+            st.dirty &= ~(1u << j);
+          }
+        }
+      }
+      // columns beyond W (padding lanes) read in-bounds taps and are never flushed
+      st.ou = o < W ? o : W - 1;
+      st.ov0 = nov0 < W ? nov0 : 0;  // lanes past the last strip own nothing: keep their reads in bounds
+      st.pu0 = h0.x;
+      st.pv0 = h0.y;
+      if (COMP) {  // the queue only grows here; the branch is uniform over the warp
+        __syncwarp();
+        if (*fqn >= kDrainAt) drain_queue<NC>(a, nxy, fq, fqn);
+      }
+    }
+    // the run's visibilities share the owned cells: a branch-free multiply-add loop over the J
+    // owned rows (offsets modulo W; rows of non-owning lanes stay in bounds and are never flushed)
+#pragma unroll 2
+    for (int vi = rs; vi < re; ++vi) {
+      const tap_t tuv = tu[vi * W + st.ou];
+      cplx pre[NC];
+#pragma unroll
+      for (int k = 0; k < NC; ++k) pre[k] = premul(recs[vi].vis[k], tuv);
+      const tap_t *tvrow = tv + vi * TVS + st.ov0;
+#pragma unroll
+      for (int j = 0; j < J; ++j) {
+        const tap_t t = tvrow[j];
+#pragma unroll
+        for (int k = 0; k < NC; ++k) mac(st.acc[j][k], pre[k], t);
+      }
+    }
+    st.dirty = rows_mask;
+  }
+  if (COMP) drain_queue<NC>(a, nxy, fq, fqn);
+}
+
+// One track (facet, channel, rows [r0, r1)) of one CTA: the rows are staged V at a time (prologue,
+// runs, taps) and gridded by the Romein owner threads.  PIPE selects the pipelined loop: the
+// prologue of chunk k + 2 (on the last V threads) and the tap staging of chunk k + 1 run in the same
+// phase as the multiply-adds of chunk k, with one CTA barrier per chunk.
+template <int NC, bool WPROJ, int J, bool COMP, bool WIDE, bool PIPE = false>
 __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local, const int chan, long long r0,
                                            long long r1) {
   typedef typename TapT<WPROJ>::type tap_t;
+  constexpr int R = StageDepth<PIPE>::recs, T = StageDepth<PIPE>::taps;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  VisRec<NC> *recs = reinterpret_cast<VisRec<NC> *>(smem_raw);
-  NormAcc *s_nacc = reinterpret_cast<NormAcc *>(smem_raw + sizeof(VisRec<NC>) * a.V);  // [V][NC]
-  int *s_ng = reinterpret_cast<int *>(s_nacc + (size_t)a.V * NC);                    // [V]
-  int *s_mixed = s_ng + a.V;                                                          // [V]
-  int *s_runs = s_mixed + a.V;  // [V + 1]: first slot of every run of the staged chunk, then nv
-  tap_t *tu = reinterpret_cast<tap_t *>(smem_raw + stage_head_bytes<NC>(a.V));
-  const int TVS = a.W + J - 1;  // row-tap stride per staged visibility
-  tap_t *tv = tu + a.V * a.W;
+  const int V = a.V, W = a.W;
+  const int TVS = W + J - 1;  // row-tap stride per staged visibility
+  VisRec<NC> *recs = reinterpret_cast<VisRec<NC> *>(smem_raw);                                // [R][V]
+  NormAcc *s_nacc = reinterpret_cast<NormAcc *>(smem_raw + sizeof(VisRec<NC>) * R * (size_t)V);  // [V][NC]
+  int *s_ng = reinterpret_cast<int *>(s_nacc + (size_t)V * NC);                                   // [V]
+  int *s_mixed = s_ng + V;                                                                        // [V]
+  int *s_runs = s_mixed + V;                                                                      // [T][V + 1]
+  tap_t *tu = reinterpret_cast<tap_t *>(smem_raw + stage_head_bytes<NC, PIPE>(V));               // [T][V][W]
+  tap_t *tv = tu + T * V * W;                                                                     // [T][V][TVS]
   // per-warp flush queues follow the taps
-  unsigned char *qbase = reinterpret_cast<unsigned char *>(tv + a.V * TVS);
+  unsigned char *qbase = reinterpret_cast<unsigned char *>(tv + T * V * TVS);
   qbase = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(qbase) + 15) & ~(uintptr_t)15);
   const int warp_id = threadIdx.x >> 5, nwarps = (blockDim.x + 31) >> 5;
   FlushRec<NC> *fq = reinterpret_cast<FlushRec<NC> *>(qbase) + warp_id * kFlushQueueCap;
   int *fqn = reinterpret_cast<int *>(qbase + nwarps * sizeof(FlushRec<NC>) * kFlushQueueCap) + warp_id * 4;
   if (COMP && (threadIdx.x & 31) == 0) *fqn = 0;
   __shared__ int s_same_g;
-  __shared__ int s_nruns;
+  __shared__ int s_nruns[T];
   __shared__ double s_norm[NC];
 
-  const int W = a.W;
   const FacetXform &fxt = a.facets[f_local];
   const int gnx = fxt.nx;
   const long long nxy = (long long)fxt.nx * fxt.ny;
@@ -685,6 +974,10 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
   if (r0 >= r1) return;
 
   const int tid = threadIdx.x;
+  // staging slot whose prologue this thread runs (none when outside [0, V)): the first V threads
+  // in the plain loop, the last V in the pipelined one (warp 0 finds the runs)
+  const int pslot = PIPE ? tid - ((int)blockDim.x - V) : tid;
+  const bool stager = pslot >= 0 && pslot < V;
   int du, strip;
   bool owner;
   owner_map<WIDE>(tid, W, J, du, strip, owner);
@@ -693,260 +986,111 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
   for (int j = 0; j < J; ++j)
     if (strip * J + j < W) rows_mask |= 1u << j;
   if (!owner) rows_mask = 0;
+  const bool grids = __any_sync(0xffffffffu, rows_mask != 0);
   const long long fslice = (long long)(a.facet_base + f_local) * a.groups;
   const bool want_norm = a.norm != nullptr;
-  if (want_norm && tid < a.V) {
+  if (want_norm && stager) {
 #pragma unroll
-    for (int k = 0; k < NC; ++k) norm_zero(s_nacc[tid * NC + k]);
-    s_ng[tid] = -1;
-    s_mixed[tid] = 0;
+    for (int k = 0; k < NC; ++k) norm_zero(s_nacc[pslot * NC + k]);
+    s_ng[pslot] = -1;
+    s_mixed[pslot] = 0;
   }
 
-  // Register state: accumulators of the J owned cells and the footprint they belong to.  For
-  // the last footprint corner (pu0, pv0) the owned cells are (pu0 + ou, pv0 + wrap(ov0 + j)),
-  // wrap(i) = i - W when i >= W.
-  cplx acc[J][NC];
+  OwnerState<NC, J> st;
 #pragma unroll
   for (int j = 0; j < J; ++j) {
 #pragma unroll
-    for (int k = 0; k < NC; ++k) { acc[j][k].re = 0; acc[j][k].im = 0; }
+    for (int k = 0; k < NC; ++k) { st.acc[j][k].re = 0; st.acc[j][k].im = 0; }
   }
-  unsigned dirty = 0;
-  int cg = -1, pu0 = -1, pv0 = -1, ou = 0, ov0 = 0;
+  st.dirty = 0;
+  st.cg = -1;
+  st.pu0 = -1;
+  st.pv0 = -1;
+  st.ou = 0;
+  st.ov0 = 0;
   ChanCache cc;
   const double plane_scale = WPROJ ? (double)(a.P - 1) / a.wmax : 0.0;
 
-  for (long long base = r0; base < r1; base += a.V) {
-    const int nv = (int)min((long long)a.V, r1 - base);
-    if (tid < a.V) {
-      VisRec<NC> rec;
-      prologue<NC, WPROJ>(a, f_local, chan, base + tid, tid < nv, rec, cc, plane_scale);
-      recs[tid] = rec;
-      // normalisation from the precomputed row sums: the staging thread owns slot tid's sums
-      if (want_norm && a.tap_sums && rec.valid) {
-        const double *su = a.tap_sums + 2 * ((long long)rec.plane * a.tap_f + rec.fu0);
-        const double *sv = a.tap_sums + 2 * ((long long)rec.plane * a.tap_f + rec.fv0);
-        const NormTerm nt = (NormTerm)(su[0] * sv[0] - su[1] * sv[1]);
-        NormAcc *na = s_nacc + tid * NC;
-        if (s_ng[tid] != rec.g) {
-          if (s_ng[tid] >= 0) {
-            s_mixed[tid] = 1;
-#pragma unroll
-            for (int k = 0; k < NC; ++k)
-              if (norm_value(na[k]) != 0.0) atomicAdd(&a.norm[(fslice + s_ng[tid]) * NC + k], norm_value(na[k]));
-          }
-#pragma unroll
-          for (int k = 0; k < NC; ++k) norm_zero(na[k]);
-          s_ng[tid] = rec.g;
-        }
-#pragma unroll
-        for (int k = 0; k < NC; ++k) norm_add(na[k], (NormTerm)rec.cw[k] * nt);
-      }
+  if (!PIPE) {
+    for (long long base = r0; base < r1; base += V) {
+      const int nv = (int)min((long long)V, r1 - base);
+      if (stager)
+        stage_slot<NC, WPROJ>(a, f_local, chan, base + pslot, pslot < nv, pslot, recs, s_nacc, s_ng, s_mixed, fslice,
+                              cc, plane_scale);
+      __syncthreads();
+      if (warp_id == 0) find_runs<NC>(recs, nv, s_runs, &s_nruns[0]);
+      stage_taps<NC, WPROJ>(a, recs, nv, TVS, tu, tv);
+      wait_taps();
+      __syncthreads();
+      if (want_norm && !a.tap_sums)
+        norm_from_taps<NC, WPROJ>(a, recs, nv, TVS, tu, tv, s_nacc, s_ng, s_mixed, fslice);
+      if (grids)
+        grid_runs<NC, WPROJ, J, COMP>(a, recs, tu, tv, s_runs, s_nruns[0], TVS, du, strip, rows_mask, fbase, nxy, gnx,
+                                      fq, fqn, st);
+      __syncthreads();
     }
+  } else {
+    // chunk k covers rows [r0 + k V, min(r1, r0 + (k + 1) V)); its records live in buffer k mod 3,
+    // its taps and runs in buffer k mod 2.  Within one phase the buffers written (records of
+    // k + 2, taps and runs of k + 1) are the ones chunk k - 1 read before the last barrier.
+    const long long nchunks = (r1 - r0 + V - 1) / V;
+    int rb = 0;  // record buffer of chunk k
+    auto chunk_nv = [&](long long k) { return (int)min((long long)V, r1 - r0 - k * V); };
+    auto prologue_chunk = [&](long long k, int buf) {
+      if (stager)
+        stage_slot<NC, WPROJ>(a, f_local, chan, r0 + k * V + pslot, pslot < chunk_nv(k), pslot, recs + buf * V,
+                              s_nacc, s_ng, s_mixed, fslice, cc, plane_scale);
+    };
+    auto taps_chunk = [&](long long k, int buf) {
+      const int tb = (int)(k & 1);
+      const VisRec<NC> *rk = recs + buf * V;
+      if (warp_id == 0) find_runs<NC>(rk, chunk_nv(k), s_runs + tb * (V + 1), &s_nruns[tb]);
+      stage_taps<NC, WPROJ>(a, rk, chunk_nv(k), TVS, tu + tb * V * W, tv + tb * V * TVS);
+    };
+    prologue_chunk(0, 0);
     __syncthreads();
-    // runs: maximal stretches of valid staged visibilities with one footprint corner and grid
-    // group (a Romein thread keeps its cells across a run); an invalid slot is a run of its own
-    if (warp_id == 0) {
-      const int lane = tid & 31;
-      int count = 0;
-      for (int b = 0; b < nv; b += 32) {
-        const int t = b + lane;
-        bool start = false;
-        if (t < nv) {
-          const int4 c0 = *reinterpret_cast<const int4 *>(&recs[t].u0);
-          const int4 c1 = *reinterpret_cast<const int4 *>(&recs[t].g);
-          start = !c1.y || t == 0;
-          if (!start) {
-            const int4 p0 = *reinterpret_cast<const int4 *>(&recs[t - 1].u0);
-            const int4 p1 = *reinterpret_cast<const int4 *>(&recs[t - 1].g);
-            start = !p1.y || p0.x != c0.x || p0.y != c0.y || p1.x != c1.x;
-          }
-        }
-        const unsigned m = __ballot_sync(0xffffffffu, start);
-        if (start) s_runs[count + __popc(m & ((1u << lane) - 1u))] = t;
-        count += __popc(m);
-      }
-      if (lane == 0) {
-        s_runs[count] = nv;
-        s_nruns = count;
-      }
-    }
-    // gather the taps of every staged visibility: W column taps, then W + J - 1 row taps.  Thread
-    // tid walks (visibility, tap) pairs with a stride of blockDim.x pairs, stepped without division.
-    {
-      const int per = W + TVS;
-      int vi = tid / per, j = tid - vi * per;
-      const int svi = (int)blockDim.x / per, sj = (int)blockDim.x - svi * per;
-      while (vi < nv) {
-        const int4 h1 = *reinterpret_cast<const int4 *>(&recs[vi].g);  // g, valid, fu, fv
-        if (h1.y) {
-          const bool isv = j >= W;
-          const int js = isv ? j - W : j;  // slot in the staged row
-          int jj = js >= W ? js - W : js;  // repeated leading row taps
-          if (jj >= W) jj = W - 1;
-          tap_t t;
-          if (a.conv_t) {
-            load_tap(a.conv_t, (long long)(isv ? h1.w : h1.z) + jj, t);
-          } else {
-            load_tap(a.conv, (long long)recs[vi].plane * a.K + (isv ? h1.w : h1.z) + (long long)jj * a.os, t);
-          }
-          if (isv) tv[vi * TVS + js] = t;
-          else tu[vi * W + js] = t;
-        }
-        vi += svi;
-        j += sj;
-        if (j >= per) {
-          j -= per;
-          ++vi;
-        }
-      }
-    }
+    taps_chunk(0, 0);
+    if (nchunks > 1) prologue_chunk(1, 1);
+    wait_taps();
     __syncthreads();
-    // normalisation without precomputed row sums (the allocation-free entry), four lanes per
-    // staged visibility: Re(sum_u k_u * sum_v k_v) x weight x flag (loop bounds are warp-uniform
-    // so the shuffles always see full warps); lane 4i owns the running sums of staged slot i
-    if (want_norm && !a.tap_sums) {
-      for (int b4 = tid & ~31; b4 < 4 * nv; b4 += blockDim.x) {
-        const int q = b4 + (tid & 31);
-        const int vi = q >> 2, part = q & 3;
-        const bool act = vi < nv;
-        // tap sums in the library's working precision (FP64 units are scarce on this GPU)
-        acc_real sur = 0, sui = 0, svr = 0, svi = 0;
-        if (act) {
-          if (WPROJ) {
-            const cplx *pu = reinterpret_cast<const cplx *>(tu) + vi * W;
-            const cplx *pv = reinterpret_cast<const cplx *>(tv) + vi * TVS;
-            for (int j = part; j < W; j += 4) { sur += pu[j].re; sui += pu[j].im; svr += pv[j].re; svi += pv[j].im; }
-          } else {
-            const acc_real *pu = reinterpret_cast<const acc_real *>(tu) + vi * W;
-            const acc_real *pv = reinterpret_cast<const acc_real *>(tv) + vi * TVS;
-            for (int j = part; j < W; j += 4) { sur += pu[j]; svr += pv[j]; }
-          }
-        }
-#pragma unroll
-        for (int off = 1; off < 4; off <<= 1) {
-          sur += __shfl_xor_sync(0xffffffffu, sur, off);
-          sui += __shfl_xor_sync(0xffffffffu, sui, off);
-          svr += __shfl_xor_sync(0xffffffffu, svr, off);
-          svi += __shfl_xor_sync(0xffffffffu, svi, off);
-        }
-        if (act && part == 0 && recs[vi].valid) {
-          const VisRec<NC> &r = recs[vi];
-          const NormTerm nt = (NormTerm)sur * (NormTerm)svr - (NormTerm)sui * (NormTerm)svi;
-          NormAcc *na = s_nacc + vi * NC;
-          if (s_ng[vi] != r.g) {
-            if (s_ng[vi] >= 0) {
-              s_mixed[vi] = 1;
-#pragma unroll
-              for (int k = 0; k < NC; ++k)
-                if (norm_value(na[k]) != 0.0) atomicAdd(&a.norm[(fslice + s_ng[vi]) * NC + k], norm_value(na[k]));
-            }
-#pragma unroll
-            for (int k = 0; k < NC; ++k) norm_zero(na[k]);
-            s_ng[vi] = r.g;
-          }
-#pragma unroll
-          for (int k = 0; k < NC; ++k) norm_add(na[k], (NormTerm)r.cw[k] * nt);
-        }
-      }
+    for (long long k = 0; k < nchunks; ++k) {
+      const int rb1 = rb == 2 ? 0 : rb + 1, rb2 = rb1 == 2 ? 0 : rb1 + 1;
+      if (k + 1 < nchunks) taps_chunk(k + 1, rb1);
+      if (k + 2 < nchunks) prologue_chunk(k + 2, rb2);
+      const int tb = (int)(k & 1);
+      const VisRec<NC> *rk = recs + rb * V;
+      const tap_t *tuk = tu + tb * V * W, *tvk = tv + tb * V * TVS;
+      if (want_norm && !a.tap_sums)
+        norm_from_taps<NC, WPROJ>(a, rk, chunk_nv(k), TVS, tuk, tvk, s_nacc, s_ng, s_mixed, fslice);
+      if (grids)
+        grid_runs<NC, WPROJ, J, COMP>(a, rk, tuk, tvk, s_runs + tb * (V + 1), s_nruns[tb], TVS, du, strip, rows_mask,
+                                      fbase, nxy, gnx, fq, fqn, st);
+      wait_taps();  // the taps of chunk k + 1 were in flight under the multiply-adds
+      __syncthreads();
+      rb = rb1;
     }
-    // grid the staged chunk (every lane of a warp with any owned cell takes part, so the
-    // queue drains below are warp-uniform)
-    if (__any_sync(0xffffffffu, rows_mask != 0)) {
-      const int nruns = s_nruns;
-      for (int ri = 0; ri < nruns; ++ri) {
-        const int rs = s_runs[ri], re = s_runs[ri + 1];
-        const int4 h0 = *reinterpret_cast<const int4 *>(&recs[rs].u0);
-        const int4 h1 = *reinterpret_cast<const int4 *>(&recs[rs].g);
-        if (!h1.y) continue;
-        if (h0.x != pu0 || h0.y != pv0 || h1.x != cg) {
-          // footprint moved: recompute the owned cells, flush those that changed
-          int o = du - h0.z;
-          o += (o < 0) ? W : 0;
-          int nov0 = strip * J - h0.w;
-          nov0 += (nov0 < 0) ? W : 0;
-          if (h0.x + o != pu0 + ou || h1.x != cg) {
-            if (dirty) {
-#pragma unroll
-              for (int j = 0; j < J; ++j)
-                if (dirty & (1u << j)) {
-                  const int oy = ov0 + j >= W ? ov0 + j - W : ov0 + j;
-                  if (COMP)
-                    queue_cell<NC>(a, fbase + (long long)cg * NC * nxy, nxy, gnx, pu0 + ou, pv0 + oy, acc[j], fq, fqn);
-                  else
-                    flush_cell<NC, false>(a, fbase + (long long)cg * NC * nxy, nxy, gnx, pu0 + ou, pv0 + oy, acc[j]);
-                }
-              dirty = 0;
-            }
-            cg = h1.x;
-          }
-          if (dirty) {
-#pragma unroll
-            for (int j = 0; j < J; ++j) {
-              const int oy = ov0 + j >= W ? ov0 + j - W : ov0 + j;
-              const int ny = nov0 + j >= W ? nov0 + j - W : nov0 + j;
-              if ((dirty & (1u << j)) && h0.y + ny != pv0 + oy) {
-                if (COMP)
-                  queue_cell<NC>(a, fbase + (long long)cg * NC * nxy, nxy, gnx, pu0 + ou, pv0 + oy, acc[j], fq, fqn);
-                else
-                  flush_cell<NC, false>(a, fbase + (long long)cg * NC * nxy, nxy, gnx, pu0 + ou, pv0 + oy, acc[j]);
-                dirty &= ~(1u << j);
-              }
-            }
-          }
-          // columns beyond W (padding lanes) read in-bounds taps and are never flushed
-          ou = o < W ? o : W - 1;
-          ov0 = nov0 < W ? nov0 : 0;  // lanes past the last strip own nothing: keep their reads in bounds
-          pu0 = h0.x;
-          pv0 = h0.y;
-          if (COMP) {  // the queue only grows here; the branch is uniform over the CTA
-            __syncwarp();
-            if (*fqn >= kDrainAt) drain_queue<NC>(a, nxy, fq, fqn);
-          }
-        }
-        // the run's visibilities share the owned cells: a branch-free multiply-add loop over
-        // the J owned rows (offsets modulo W; rows of non-owning lanes stay in bounds and are
-        // never flushed)
-#pragma unroll 2
-        for (int vi = rs; vi < re; ++vi) {
-          const tap_t tuv = tu[vi * W + ou];
-          cplx pre[NC];
-#pragma unroll
-          for (int k = 0; k < NC; ++k) pre[k] = premul(recs[vi].vis[k], tuv);
-          const tap_t *tvrow = tv + vi * TVS + ov0;
-#pragma unroll
-          for (int j = 0; j < J; ++j) {
-            const tap_t t = tvrow[j];
-#pragma unroll
-            for (int k = 0; k < NC; ++k) mac(acc[j][k], pre[k], t);
-          }
-        }
-        dirty = rows_mask;
-      }
-      if (COMP) drain_queue<NC>(a, nxy, fq, fqn);
-    }
-    __syncthreads();
   }
   // final flush of owned cells
-  if (dirty) {
+  if (st.dirty) {
 #pragma unroll
     for (int j = 0; j < J; ++j) {
-      const int oy = ov0 + j >= W ? ov0 + j - W : ov0 + j;
-      if (dirty & (1u << j)) flush_cell<NC, COMP>(a, fbase + (long long)cg * NC * nxy, nxy, gnx, pu0 + ou, pv0 + oy, acc[j]);
+      const int oy = st.ov0 + j >= W ? st.ov0 + j - W : st.ov0 + j;
+      if (st.dirty & (1u << j))
+        flush_cell<NC, COMP>(a, fbase + (long long)st.cg * NC * nxy, nxy, gnx, st.pu0 + st.ou, st.pv0 + oy, st.acc[j]);
     }
   }
-  // normalisation: one reduction per CTA when every staged slot saw a single grid group
+  // normalisation: one reduction per CTA when every staging slot saw a single grid group
   if (want_norm) {
     if (tid == 0) s_same_g = -1;
     if (tid < NC) s_norm[tid] = 0.0;
     __syncthreads();
-    const int my_g = tid < a.V ? s_ng[tid] : -1;
+    const int my_g = tid < V ? s_ng[tid] : -1;
     if (my_g >= 0) atomicMax(&s_same_g, my_g);
     __syncthreads();
     const int gmax = s_same_g;
-    const bool uniform_here = tid >= a.V || (!s_mixed[tid] && (my_g < 0 || my_g == gmax));
+    const bool uniform_here = tid >= V || (!s_mixed[tid] && (my_g < 0 || my_g == gmax));
     const int all_uniform = __syncthreads_and(uniform_here ? 1 : 0);
-    if (tid < a.V && my_g >= 0) {
+    if (tid < V && my_g >= 0) {
       const NormAcc *na = s_nacc + tid * NC;
       if (all_uniform) {
 #pragma unroll
@@ -995,7 +1139,7 @@ __global__ void __launch_bounds__(512, 1) romein_grid_kernel(const GridArgs a) {
 // whose w planes share this launch's support class (a.W).  Items of one segment are adjacent, so
 // the facets of a segment are gridded while its rows are hot in L2.  The loop ends on the count,
 // never waits on other CTAs.
-template <int NC, bool WPROJ, int J, bool COMP, bool WIDE, int REGS = kSegRegs<J>>
+template <int NC, bool WPROJ, int J, bool COMP, bool WIDE, int REGS = kSegRegs<J>, bool PIPE = false>
 __global__ void __launch_bounds__(512, 1) __maxnreg__(REGS) romein_segment_kernel(const GridArgs a, const int nfacets) {
   __shared__ int s_item;
   const int count = *a.work_count;
@@ -1018,7 +1162,7 @@ __global__ void __launch_bounds__(512, 1) __maxnreg__(REGS) romein_segment_kerne
       if (threadIdx.x == 0) atomicOr(a.error, DEV_ERR_GRID_INDEX);
       continue;
     }
-    grid_track<NC, WPROJ, J, COMP, WIDE>(a, f_local, sg.z, sg.x, sg.y);
+    grid_track<NC, WPROJ, J, COMP, WIDE, PIPE>(a, f_local, sg.z, sg.x, sg.y);
   }
 }
 
