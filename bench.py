@@ -163,7 +163,7 @@ def class_profile(lib, step, counts, plane_width):
         vis, t = taps.get(int(width[i]), (0, 0.0))
         flops = t * (N_FACETS * 8 * 4 if nc[i] == 4 else 8)
         rows.append({"width": int(width[i]), "corr": int(nc[i]), "J": int(J[i]), "wide": bool(wide[i] & 1),
-                     "registers": (int(wide[i]) >> 1) & 255, "pipelined": bool(int(wide[i]) >> 9 & 1),
+                     "registers": int(wide[i]) >> 1,
                      "work_items": int(items[i]), "vis": vis, "ms": float(ms[i]),
                      "executed_tflops": flops / (float(ms[i]) * 1e-3) / 1e12 if ms[i] > 0 else None})
     return rows
@@ -903,28 +903,41 @@ def main():
         torch.cuda.empty_cache()
         P = ctypes.c_void_p
 
+        parts = {}
+
         def e2e_step():
+            marks = [time.perf_counter()]
             tab2 = Tables(geo, conv)
             s2 = gridding_parameters_type("single")()
             tab2.fill(s2, geo, R)
             lib.initLibrary(ctypes.byref(s2))
             set_rows(s2, hnp, lambda a: a.ctypes.data_as(P))
             s2.is_final_data_chunk = True
+            marks.append(time.perf_counter())
             if args.form == "plain":
                 lib.facet_4_cor_corrections(ctypes.byref(s2))
                 lib.facet_sampling_function(ctypes.byref(s2))
             else:
                 lib.bullseye_grid_batched(ctypes.byref(s2), 0, 1)
             lib.gridding_barrier()
+            marks.append(time.perf_counter())
             lib.weight_uniformly(ctypes.byref(s2))
+            marks.append(time.perf_counter())
             lib.normalize(ctypes.byref(s2))
+            marks.append(time.perf_counter())
             lib.finalize(ctypes.byref(s2))
             img = float(tab2.grid.view(np.float32).reshape(-1)[0])
+            marks.append(time.perf_counter())
             lib.releaseLibrary()
             check(lib)
+            marks.append(time.perf_counter())
+            for name, t0_, t1_ in zip(("init", "grid", "weight_uniformly", "normalize", "finalize", "release"),
+                                      marks[:-1], marks[1:]):
+                parts[name] = parts.get(name, 0.0) + (t1_ - t0_) * 1e3
             return img
 
         e2e_step()
+        parts.clear()
         t0 = time.perf_counter()
         n_e2e = max(1, min(args.steps, 3))
         for _ in range(n_e2e):
@@ -937,6 +950,7 @@ def main():
         d2h = tab.grid.nbytes + tab.sf.nbytes + N_FACETS * NX * NX * (8 + 4)
         e2e = {"value": pairs_per_step / dt / 1e6, "unit": "Mvis/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "s_per_step": dt,
+               "ms_by_call": {k: round(v / n_e2e, 1) for k, v in parts.items()},
                "calls": ("initLibrary, " + ("facet_4_cor_corrections, facet_sampling_function"
                                              if args.form == "plain" else "bullseye_grid_batched(call 0, sampling)") +
                          ", weight_uniformly, normalize, finalize, releaseLibrary (host pinned buffers)")}

@@ -156,8 +156,7 @@ __global__ void bucket_kernel(const int4 *__restrict__ segs, const int *total, i
 struct Variant {
   int J;
   bool wide;
-  int regs;   // register cap of the build
-  bool pipe;  // pipelined staging (prologue two chunks ahead, taps one chunk ahead)
+  int regs;  // register cap of the build
   int NT, V, grid;
   size_t smem;
 };
@@ -165,21 +164,19 @@ struct Variant {
 template <int NC, bool WPROJ, bool COMP>
 using SegKernel = void (*)(const GridArgs, const int);
 
-template <int NC, bool WPROJ, bool COMP, bool WIDE, bool PIPE>
+template <int NC, bool WPROJ, bool COMP, bool WIDE>
 SegKernel<NC, WPROJ, COMP> seg_kernel_of(int J, int regs) {
-  if (J == 8) return romein_segment_kernel<NC, WPROJ, 8, COMP, WIDE, kSegRegs<8>, PIPE>;
+  if (J == 8) return romein_segment_kernel<NC, WPROJ, 8, COMP, WIDE>;
   if constexpr (NC == 4 && WPROJ) {
-    if (regs == 64) return romein_segment_kernel<NC, WPROJ, 4, COMP, WIDE, 64, PIPE>;
-    if (regs == 72) return romein_segment_kernel<NC, WPROJ, 4, COMP, WIDE, 72, PIPE>;
+    if (regs == 64) return romein_segment_kernel<NC, WPROJ, 4, COMP, WIDE, 64>;
+    if (regs == 72) return romein_segment_kernel<NC, WPROJ, 4, COMP, WIDE, 72>;
   }
-  return romein_segment_kernel<NC, WPROJ, 4, COMP, WIDE, kSegRegs<4>, PIPE>;
+  return romein_segment_kernel<NC, WPROJ, 4, COMP, WIDE>;
 }
 
 template <int NC, bool WPROJ, bool COMP>
-SegKernel<NC, WPROJ, COMP> seg_kernel(int J, bool wide, int regs, bool pipe) {
-  if (pipe)
-    return wide ? seg_kernel_of<NC, WPROJ, COMP, true, true>(J, regs) : seg_kernel_of<NC, WPROJ, COMP, false, true>(J, regs);
-  return wide ? seg_kernel_of<NC, WPROJ, COMP, true, false>(J, regs) : seg_kernel_of<NC, WPROJ, COMP, false, false>(J, regs);
+SegKernel<NC, WPROJ, COMP> seg_kernel(int J, bool wide, int regs) {
+  return wide ? seg_kernel_of<NC, WPROJ, COMP, true>(J, regs) : seg_kernel_of<NC, WPROJ, COMP, false>(J, regs);
 }
 
 // Register caps the tuner tries for a layout.
@@ -191,23 +188,17 @@ std::vector<int> reg_caps(int J) {
 }
 
 template <int NC, bool WPROJ>
-bool make_variant(int W, int J, bool wide, int regs, bool pipe, Variant &v) {
+bool make_variant(int W, int J, bool wide, int regs, Variant &v) {
   const int cols = ((W + 31) / 32) * 32;
   if (wide && (cols - W) * 8 > W) return false;
   const int owners = wide ? cols * ((W + J - 1) / J) : W * ((W + J - 1) / J);
   v.J = J;
   v.wide = wide;
   v.regs = regs;
-  v.pipe = pipe;
   v.NT = std::max(32, ((owners + 31) / 32) * 32);
   if (v.NT > 512) return false;
-  if (pipe) {
-    v.V = grid_chunk_size<NC, WPROJ, true>(W, v.NT, J, regs);
-    v.smem = grid_smem_bytes<NC, WPROJ, true>(v.V, W, v.NT, J);
-  } else {
-    v.V = grid_chunk_size<NC, WPROJ>(W, v.NT, J, regs);
-    v.smem = grid_smem_bytes<NC, WPROJ>(v.V, W, v.NT, J);
-  }
+  v.V = grid_chunk_size<NC, WPROJ>(W, v.NT, J, regs);
+  v.smem = grid_smem_bytes<NC, WPROJ>(v.V, W, v.NT, J);
   return true;
 }
 
@@ -227,7 +218,7 @@ struct BatchedState {
   DevBuf<FacetXform> facet_table;  // per-facet geometry of bullseye_grid_batched_facets
   size_t rows_cap = 0, tracks_cap = 0, segs_cap = 0;
   // tuning decisions, by (class width, NC, WPROJ, COMP)
-  std::map<std::tuple<int, int, int, int>, std::tuple<int, int, int, int>> tuned;  // -> (J, wide, regs, pipe)
+  std::map<std::tuple<int, int, int, int>, std::tuple<int, int, int>> tuned;  // -> (J, wide, regs)
   // captured graph
   cudaGraphExec_t exec = nullptr;
   std::vector<unsigned char> key;
@@ -355,7 +346,7 @@ bool launch_class(const GridArgs &base, int k, const Variant &v, int nfacets, co
   a.segment_capacity = (long long)g_bs.segs_cap;
   a.work_count = count;
   a.work_next = next;
-  auto kern = seg_kernel<NC, WPROJ, COMP>(v.J, v.wide, v.regs, v.pipe);
+  auto kern = seg_kernel<NC, WPROJ, COMP>(v.J, v.wide, v.regs);
   if (!open_smem(kern)) {
     bz_record_error(BZ_ERR_CUDA, "batched: cudaFuncSetAttribute failed");
     return false;
@@ -369,7 +360,7 @@ bool launch_class(const GridArgs &base, int k, const Variant &v, int nfacets, co
 
 template <int NC, bool WPROJ, bool COMP>
 bool finish_variant(Variant &v) {
-  auto kern = seg_kernel<NC, WPROJ, COMP>(v.J, v.wide, v.regs, v.pipe);
+  auto kern = seg_kernel<NC, WPROJ, COMP>(v.J, v.wide, v.regs);
   if (!open_smem(kern)) return false;
   int per_sm = 0, dev = 0, sms = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, v.NT, v.smem) != cudaSuccess || per_sm < 1) return false;
@@ -391,27 +382,24 @@ bool tune_class(const GridArgs &base, int k, int nfacets, Variant &out, int host
   std::vector<Variant> cands;
   for (int J : {8, 4})
     for (bool wide : {true, false})
-      for (int regs : reg_caps<NC, WPROJ>(J))
-        for (bool pipe : {false, true}) {
-          Variant v;
-          if (make_variant<NC, WPROJ>(W, J, wide, regs, pipe, v) && finish_variant<NC, WPROJ, COMP>(v))
-            cands.push_back(v);
-        }
+      for (int regs : reg_caps<NC, WPROJ>(J)) {
+        Variant v;
+        if (make_variant<NC, WPROJ>(W, J, wide, regs, v) && finish_variant<NC, WPROJ, COMP>(v)) cands.push_back(v);
+      }
   if (cands.empty()) {
     bz_record_error(BZ_ERR_UNSUPPORTED, "batched: no layout for support class %d", W);
     return false;
   }
   if (it != b.tuned.end()) {
     for (auto &v : cands)
-      if (v.J == std::get<0>(it->second) && (int)v.wide == std::get<1>(it->second) && v.regs == std::get<2>(it->second) &&
-          (int)v.pipe == std::get<3>(it->second)) {
+      if (v.J == std::get<0>(it->second) && (int)v.wide == std::get<1>(it->second) && v.regs == std::get<2>(it->second)) {
         out = v;
         return true;
       }
   }
   if (cands.size() == 1 || host_count == 0) {
     out = cands[0];
-    b.tuned[key] = std::make_tuple(out.J, (int)out.wide, out.regs, (int)out.pipe);
+    b.tuned[key] = std::make_tuple(out.J, (int)out.wide, out.regs);
     return true;
   }
   // Each candidate grids a quarter of the class's runs (at least 4096, when there are that many)
@@ -446,7 +434,7 @@ bool tune_class(const GridArgs &base, int k, int nfacets, Variant &out, int host
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   BZ_CUDA_TRY_RET(cudaMemsetAsync(c.scratch.ptr, 0, sizeof(vis_complex) * c.scratch.n, c.stream), false);
-  b.tuned[key] = std::make_tuple(out.J, (int)out.wide, out.regs, (int)out.pipe);
+  b.tuned[key] = std::make_tuple(out.J, (int)out.wide, out.regs);
   return bz_error_code() == BZ_OK;
 }
 
@@ -479,7 +467,7 @@ bool launch_all(const GridArgs &base, int nfacets, bool sampling, cudaStream_t s
       cudaEventElapsedTime(&ms, e0, e1);
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
-      b.records.push_back({b.cls[k].width, NC, v.J, (int)v.wide | (v.regs << 1) | ((int)v.pipe << 9), counts ? (*counts)[k] * nfacets : 0, ms});
+      b.records.push_back({b.cls[k].width, NC, v.J, (int)v.wide | (v.regs << 1), counts ? (*counts)[k] * nfacets : 0, ms});
     }
     if (!ok) return false;
   }
@@ -666,7 +654,9 @@ extern "C" int bullseye_grid_batched(gridding_parameters *pp, int call, int with
   GridArgs va, sa;
   int nslots = 0, nslots_sf = 0;
   if (!bz_prepare_grid_args(p, 4, mode, faceting, va, nslots, "bullseye_grid_batched")) return bz_error_code();
-  if (sf && !bz_prepare_grid_args(p, 1, CORR_SAMPLING, faceting, sa, nslots_sf, "bullseye_grid_batched")) return bz_error_code();
+  // the sampling function reads the rows the visibility prepare just uploaded
+  if (sf && !bz_prepare_grid_args(p, 1, CORR_SAMPLING, faceting, sa, nslots_sf, "bullseye_grid_batched", false))
+    return bz_error_code();
   if (p.row_count == 0) {
     bz_timer_stop();
     return BZ_OK;

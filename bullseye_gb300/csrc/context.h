@@ -102,5 +102,6 @@ void bz_copy_back_grids(gridding_parameters &p, bool sampling);
 FacetXform bz_facet_xform(double ra0, double dec0, double ra, double dec, bool phase, bool uvx);
 void bz_timer_start();
 void bz_timer_stop();
+// upload = false reuses the rows a preceding prepare of the same call already uploaded.
 bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool faceting, GridArgs &a,
-                          int &nslots, const char *name);
+                          int &nslots, const char *name, bool upload = true);

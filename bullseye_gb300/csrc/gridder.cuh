@@ -589,44 +589,30 @@ __host__ __device__ inline size_t flush_queue_bytes(int nwarps) {
 // Row taps are stored W + J - 1 long per visibility: the first J - 1 taps are repeated after the
 // last, so a thread's J consecutive owned rows read J consecutive taps without a wrap.
 
-// Staging depth.  The plain loop stages one chunk at a time: one record buffer, one tap buffer, one
-// run list, three CTA barriers per chunk.  The pipelined loop of the persistent kernel runs the
-// prologue two chunks ahead and the tap staging one chunk ahead of the multiply-adds, all in one
-// phase with one CTA barrier per chunk: three record buffers, two tap buffers, two run lists.
-template <bool PIPE>
-struct StageDepth {
-  static constexpr int recs = PIPE ? 3 : 1;
-  static constexpr int taps = PIPE ? 2 : 1;
-};
-
-// Bytes before the tap arrays: the staged-record buffers, the normalisation state of the V staging
-// slots (partial sums, grid group, mixed flag), the run lists (V + 1 run starts each); rounded up
-// to 16.
-template <int NC, bool PIPE = false>
+// Bytes before the tap arrays: V staged records, their normalisation state (partial sums, grid
+// group, mixed flag), the V + 1 run starts of the chunk; rounded up to 16.
+template <int NC>
 __host__ __device__ inline size_t stage_head_bytes(int V) {
-  constexpr int R = StageDepth<PIPE>::recs, T = StageDepth<PIPE>::taps;
-  return ((R * sizeof(VisRec<NC>) + sizeof(NormAcc) * NC + (2 + T) * sizeof(int)) * (size_t)V + T * sizeof(int) +
-          15) / 16 * 16;
+  return ((sizeof(VisRec<NC>) + sizeof(NormAcc) * NC + 3 * sizeof(int)) * (size_t)V + sizeof(int) + 15) / 16 * 16;
 }
 
-template <int NC, bool WPROJ, bool PIPE = false>
+template <int NC, bool WPROJ>
 __host__ __device__ inline size_t grid_smem_bytes(int V, int W, int nthreads, int J) {
-  size_t taps = StageDepth<PIPE>::taps * sizeof(typename TapT<WPROJ>::type) * (size_t)V * (2 * W + J - 1);
-  return stage_head_bytes<NC, PIPE>(V) + taps + flush_queue_bytes<NC>((nthreads + 31) / 32) + 64;
+  size_t taps = sizeof(typename TapT<WPROJ>::type) * (size_t)V * (2 * W + J - 1);
+  return stage_head_bytes<NC>(V) + taps + flush_queue_bytes<NC>((nthreads + 31) / 32) + 64;
 }
 
 // Staged-chunk size V for a CTA of nthreads: one visibility per thread at most, and shared memory
 // small enough that the CTAs the register file allows (regs registers per thread) fit on an SM.
-template <int NC, bool WPROJ, bool PIPE = false>
+template <int NC, bool WPROJ>
 __host__ inline int grid_chunk_size(int W, int nthreads, int J, int regs = 128) {
-  constexpr int R = StageDepth<PIPE>::recs, T = StageDepth<PIPE>::taps;
   const int ctas = std::max(1, std::min(8, 65536 / (nthreads * regs)));
   const size_t smem_sm = 227 * 1024;
   size_t budget = std::min<size_t>(200 * 1024, smem_sm / ctas - 1024);
-  const size_t fixed = flush_queue_bytes<NC>((nthreads + 31) / 32) + 64 + T * sizeof(int) + 15;
+  const size_t fixed = flush_queue_bytes<NC>((nthreads + 31) / 32) + 64 + sizeof(int) + 15;
   budget = budget > fixed ? budget - fixed : 0;
-  const size_t per = R * sizeof(VisRec<NC>) + sizeof(NormAcc) * NC + (2 + T) * sizeof(int) +
-                     T * sizeof(typename TapT<WPROJ>::type) * (2 * (size_t)W + J - 1);
+  const size_t per = sizeof(VisRec<NC>) + sizeof(NormAcc) * NC + 3 * sizeof(int) +
+                     sizeof(typename TapT<WPROJ>::type) * (2 * (size_t)W + J - 1);
   return std::max(1, (int)std::min<size_t>(nthreads, budget / per));
 }
 
@@ -937,33 +923,30 @@ __device__ __forceinline__ void grid_runs(const GridArgs &a, const VisRec<NC> *r
 }
 
 // One track (facet, channel, rows [r0, r1)) of one CTA: the rows are staged V at a time (prologue,
-// runs, taps) and gridded by the Romein owner threads.  PIPE selects the pipelined loop: the
-// prologue of chunk k + 2 (on the last V threads) and the tap staging of chunk k + 1 run in the same
-// phase as the multiply-adds of chunk k, with one CTA barrier per chunk.
-template <int NC, bool WPROJ, int J, bool COMP, bool WIDE, bool PIPE = false>
+// runs, taps) and gridded by the Romein owner threads.
+template <int NC, bool WPROJ, int J, bool COMP, bool WIDE>
 __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local, const int chan, long long r0,
                                            long long r1) {
   typedef typename TapT<WPROJ>::type tap_t;
-  constexpr int R = StageDepth<PIPE>::recs, T = StageDepth<PIPE>::taps;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int V = a.V, W = a.W;
   const int TVS = W + J - 1;  // row-tap stride per staged visibility
-  VisRec<NC> *recs = reinterpret_cast<VisRec<NC> *>(smem_raw);                                // [R][V]
-  NormAcc *s_nacc = reinterpret_cast<NormAcc *>(smem_raw + sizeof(VisRec<NC>) * R * (size_t)V);  // [V][NC]
-  int *s_ng = reinterpret_cast<int *>(s_nacc + (size_t)V * NC);                                   // [V]
-  int *s_mixed = s_ng + V;                                                                        // [V]
-  int *s_runs = s_mixed + V;                                                                      // [T][V + 1]
-  tap_t *tu = reinterpret_cast<tap_t *>(smem_raw + stage_head_bytes<NC, PIPE>(V));               // [T][V][W]
-  tap_t *tv = tu + T * V * W;                                                                     // [T][V][TVS]
+  VisRec<NC> *recs = reinterpret_cast<VisRec<NC> *>(smem_raw);                          // [V]
+  NormAcc *s_nacc = reinterpret_cast<NormAcc *>(smem_raw + sizeof(VisRec<NC>) * (size_t)V);  // [V][NC]
+  int *s_ng = reinterpret_cast<int *>(s_nacc + (size_t)V * NC);                             // [V]
+  int *s_mixed = s_ng + V;                                                                  // [V]
+  int *s_runs = s_mixed + V;                                                                // [V + 1]
+  tap_t *tu = reinterpret_cast<tap_t *>(smem_raw + stage_head_bytes<NC>(V));               // [V][W]
+  tap_t *tv = tu + V * W;                                                                   // [V][TVS]
   // per-warp flush queues follow the taps
-  unsigned char *qbase = reinterpret_cast<unsigned char *>(tv + T * V * TVS);
+  unsigned char *qbase = reinterpret_cast<unsigned char *>(tv + V * TVS);
   qbase = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(qbase) + 15) & ~(uintptr_t)15);
   const int warp_id = threadIdx.x >> 5, nwarps = (blockDim.x + 31) >> 5;
   FlushRec<NC> *fq = reinterpret_cast<FlushRec<NC> *>(qbase) + warp_id * kFlushQueueCap;
   int *fqn = reinterpret_cast<int *>(qbase + nwarps * sizeof(FlushRec<NC>) * kFlushQueueCap) + warp_id * 4;
   if (COMP && (threadIdx.x & 31) == 0) *fqn = 0;
   __shared__ int s_same_g;
-  __shared__ int s_nruns[T];
+  __shared__ int s_nruns;
   __shared__ double s_norm[NC];
 
   const FacetXform &fxt = a.facets[f_local];
@@ -974,10 +957,6 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
   if (r0 >= r1) return;
 
   const int tid = threadIdx.x;
-  // staging slot whose prologue this thread runs (none when outside [0, V)): the first V threads
-  // in the plain loop, the last V in the pipelined one (warp 0 finds the runs)
-  const int pslot = PIPE ? tid - ((int)blockDim.x - V) : tid;
-  const bool stager = pslot >= 0 && pslot < V;
   int du, strip;
   bool owner;
   owner_map<WIDE>(tid, W, J, du, strip, owner);
@@ -989,11 +968,11 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
   const bool grids = __any_sync(0xffffffffu, rows_mask != 0);
   const long long fslice = (long long)(a.facet_base + f_local) * a.groups;
   const bool want_norm = a.norm != nullptr;
-  if (want_norm && stager) {
+  if (want_norm && tid < V) {
 #pragma unroll
-    for (int k = 0; k < NC; ++k) norm_zero(s_nacc[pslot * NC + k]);
-    s_ng[pslot] = -1;
-    s_mixed[pslot] = 0;
+    for (int k = 0; k < NC; ++k) norm_zero(s_nacc[tid * NC + k]);
+    s_ng[tid] = -1;
+    s_mixed[tid] = 0;
   }
 
   OwnerState<NC, J> st;
@@ -1011,64 +990,21 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
   ChanCache cc;
   const double plane_scale = WPROJ ? (double)(a.P - 1) / a.wmax : 0.0;
 
-  if (!PIPE) {
-    for (long long base = r0; base < r1; base += V) {
-      const int nv = (int)min((long long)V, r1 - base);
-      if (stager)
-        stage_slot<NC, WPROJ>(a, f_local, chan, base + pslot, pslot < nv, pslot, recs, s_nacc, s_ng, s_mixed, fslice,
-                              cc, plane_scale);
-      __syncthreads();
-      if (warp_id == 0) find_runs<NC>(recs, nv, s_runs, &s_nruns[0]);
-      stage_taps<NC, WPROJ>(a, recs, nv, TVS, tu, tv);
-      wait_taps();
-      __syncthreads();
-      if (want_norm && !a.tap_sums)
-        norm_from_taps<NC, WPROJ>(a, recs, nv, TVS, tu, tv, s_nacc, s_ng, s_mixed, fslice);
-      if (grids)
-        grid_runs<NC, WPROJ, J, COMP>(a, recs, tu, tv, s_runs, s_nruns[0], TVS, du, strip, rows_mask, fbase, nxy, gnx,
-                                      fq, fqn, st);
-      __syncthreads();
-    }
-  } else {
-    // chunk k covers rows [r0 + k V, min(r1, r0 + (k + 1) V)); its records live in buffer k mod 3,
-    // its taps and runs in buffer k mod 2.  Within one phase the buffers written (records of
-    // k + 2, taps and runs of k + 1) are the ones chunk k - 1 read before the last barrier.
-    const long long nchunks = (r1 - r0 + V - 1) / V;
-    int rb = 0;  // record buffer of chunk k
-    auto chunk_nv = [&](long long k) { return (int)min((long long)V, r1 - r0 - k * V); };
-    auto prologue_chunk = [&](long long k, int buf) {
-      if (stager)
-        stage_slot<NC, WPROJ>(a, f_local, chan, r0 + k * V + pslot, pslot < chunk_nv(k), pslot, recs + buf * V,
-                              s_nacc, s_ng, s_mixed, fslice, cc, plane_scale);
-    };
-    auto taps_chunk = [&](long long k, int buf) {
-      const int tb = (int)(k & 1);
-      const VisRec<NC> *rk = recs + buf * V;
-      if (warp_id == 0) find_runs<NC>(rk, chunk_nv(k), s_runs + tb * (V + 1), &s_nruns[tb]);
-      stage_taps<NC, WPROJ>(a, rk, chunk_nv(k), TVS, tu + tb * V * W, tv + tb * V * TVS);
-    };
-    prologue_chunk(0, 0);
+  for (long long base = r0; base < r1; base += V) {
+    const int nv = (int)min((long long)V, r1 - base);
+    if (tid < V)
+      stage_slot<NC, WPROJ>(a, f_local, chan, base + tid, tid < nv, tid, recs, s_nacc, s_ng, s_mixed, fslice, cc,
+                            plane_scale);
     __syncthreads();
-    taps_chunk(0, 0);
-    if (nchunks > 1) prologue_chunk(1, 1);
+    if (warp_id == 0) find_runs<NC>(recs, nv, s_runs, &s_nruns);
+    stage_taps<NC, WPROJ>(a, recs, nv, TVS, tu, tv);
     wait_taps();
     __syncthreads();
-    for (long long k = 0; k < nchunks; ++k) {
-      const int rb1 = rb == 2 ? 0 : rb + 1, rb2 = rb1 == 2 ? 0 : rb1 + 1;
-      if (k + 1 < nchunks) taps_chunk(k + 1, rb1);
-      if (k + 2 < nchunks) prologue_chunk(k + 2, rb2);
-      const int tb = (int)(k & 1);
-      const VisRec<NC> *rk = recs + rb * V;
-      const tap_t *tuk = tu + tb * V * W, *tvk = tv + tb * V * TVS;
-      if (want_norm && !a.tap_sums)
-        norm_from_taps<NC, WPROJ>(a, rk, chunk_nv(k), TVS, tuk, tvk, s_nacc, s_ng, s_mixed, fslice);
-      if (grids)
-        grid_runs<NC, WPROJ, J, COMP>(a, rk, tuk, tvk, s_runs + tb * (V + 1), s_nruns[tb], TVS, du, strip, rows_mask,
-                                      fbase, nxy, gnx, fq, fqn, st);
-      wait_taps();  // the taps of chunk k + 1 were in flight under the multiply-adds
-      __syncthreads();
-      rb = rb1;
-    }
+    if (want_norm && !a.tap_sums) norm_from_taps<NC, WPROJ>(a, recs, nv, TVS, tu, tv, s_nacc, s_ng, s_mixed, fslice);
+    if (grids)
+      grid_runs<NC, WPROJ, J, COMP>(a, recs, tu, tv, s_runs, s_nruns, TVS, du, strip, rows_mask, fbase, nxy, gnx, fq,
+                                    fqn, st);
+    __syncthreads();
   }
   // final flush of owned cells
   if (st.dirty) {
@@ -1139,7 +1075,7 @@ __global__ void __launch_bounds__(512, 1) romein_grid_kernel(const GridArgs a) {
 // whose w planes share this launch's support class (a.W).  Items of one segment are adjacent, so
 // the facets of a segment are gridded while its rows are hot in L2.  The loop ends on the count,
 // never waits on other CTAs.
-template <int NC, bool WPROJ, int J, bool COMP, bool WIDE, int REGS = kSegRegs<J>, bool PIPE = false>
+template <int NC, bool WPROJ, int J, bool COMP, bool WIDE, int REGS = kSegRegs<J>>
 __global__ void __launch_bounds__(512, 1) __maxnreg__(REGS) romein_segment_kernel(const GridArgs a, const int nfacets) {
   __shared__ int s_item;
   const int count = *a.work_count;
@@ -1162,7 +1098,7 @@ __global__ void __launch_bounds__(512, 1) __maxnreg__(REGS) romein_segment_kerne
       if (threadIdx.x == 0) atomicOr(a.error, DEV_ERR_GRID_INDEX);
       continue;
     }
-    grid_track<NC, WPROJ, J, COMP, WIDE, PIPE>(a, f_local, sg.z, sg.x, sg.y);
+    grid_track<NC, WPROJ, J, COMP, WIDE>(a, f_local, sg.z, sg.x, sg.y);
   }
 }
 

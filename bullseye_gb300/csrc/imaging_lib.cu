@@ -674,7 +674,7 @@ static void copy_back_grids(gridding_parameters &p, bool sampling) {
 // Validation, uploads, Jones inversion, track setup and the per-facet transforms of one gridding
 // call; fills the kernel arguments.  Shared by the per-call and the batched paths.
 bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool faceting, GridArgs &a, int &nslots,
-                          const char *name) {
+                          const char *name, bool upload) {
   Context &c = g_ctx;
   const bool sampling = mode == CORR_SAMPLING;
   if (sampling && !c.want_sf) {
@@ -694,7 +694,7 @@ bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool f
     return false;
   }
   const bool jones = mode == CORR_QUAD_JONES;
-  if (!upload_rows(p, jones, jones)) return false;
+  if (upload && !upload_rows(p, jones, jones)) return false;
   if (jones) {
     const size_t nj = p.no_timestamps_read * p.antenna_count * c.F * c.nspw * c.nchan;
     if (!p.jones_terms || nj == 0) {

@@ -139,8 +139,8 @@ int bullseye_grid_batched_facets(gridding_parameters *params, const bullseye_fac
  * graph) with a CUDA event pair around every support-class launch, synchronising after each. */
 void bullseye_set_batched_profiling(int on);
 /* The last profiled call's class launches: support width, correlations (4 visibilities, 1
- * sampling function), layout (J rows per thread; `wide` bit 0 = WIDE, bits 1-8 = the build's register
- * cap, bit 9 = pipelined staging), (track run, facet) work items and
+ * sampling function), layout (J rows per thread; `wide` bit 0 = WIDE, bits 1.. = the build's register
+ * cap), (track run, facet) work items and
  * milliseconds, up to max entries; returns the number of launches recorded. */
 int bullseye_batched_profile(int *width, int *nc, int *J, int *wide, int *items, float *ms, int max);
 /* Support-class width the batched gridder uses for every w plane (the plane's nonzero window,
