@@ -590,10 +590,10 @@ __host__ __device__ inline size_t flush_queue_bytes(int nwarps) {
 // last, so a thread's J consecutive owned rows read J consecutive taps without a wrap.
 
 // Bytes before the tap arrays: V staged records, their normalisation state (partial sums, grid
-// group, mixed flag), the V + 1 run starts of the chunk; rounded up to 16.
+// group), the V + 1 run starts of the chunk; rounded up to 16.
 template <int NC>
 __host__ __device__ inline size_t stage_head_bytes(int V) {
-  return ((sizeof(VisRec<NC>) + sizeof(NormAcc) * NC + 3 * sizeof(int)) * (size_t)V + sizeof(int) + 15) / 16 * 16;
+  return ((sizeof(VisRec<NC>) + sizeof(NormAcc) * NC + 2 * sizeof(int)) * (size_t)V + sizeof(int) + 15) / 16 * 16;
 }
 
 template <int NC, bool WPROJ>
@@ -611,7 +611,7 @@ __host__ inline int grid_chunk_size(int W, int nthreads, int J, int regs = 128) 
   size_t budget = std::min<size_t>(200 * 1024, smem_sm / ctas - 1024);
   const size_t fixed = flush_queue_bytes<NC>((nthreads + 31) / 32) + 64 + sizeof(int) + 15;
   budget = budget > fixed ? budget - fixed : 0;
-  const size_t per = sizeof(VisRec<NC>) + sizeof(NormAcc) * NC + 3 * sizeof(int) +
+  const size_t per = sizeof(VisRec<NC>) + sizeof(NormAcc) * NC + 2 * sizeof(int) +
                      sizeof(typename TapT<WPROJ>::type) * (2 * (size_t)W + J - 1);
   return std::max(1, (int)std::min<size_t>(nthreads, budget / per));
 }
@@ -663,35 +663,39 @@ struct OwnerState {
   int cg, pu0, pv0, ou, ov0;
 };
 
-// Prologue of one staging slot: the visibility of `row` staged into recs[slot] and, with the
-// precomputed row sums, its normalisation term added to the slot's running sums (which go to the
-// global normalisation when the slot's grid group changes).
+// Prologue of one staging slot: the visibility of `row` staged into recs[slot].
 template <int NC, bool WPROJ>
 __device__ __forceinline__ void stage_slot(const GridArgs &a, int f_local, int chan, long long row, bool in_range,
-                                           int slot, VisRec<NC> *recs, NormAcc *s_nacc, int *s_ng, int *s_mixed,
-                                           long long fslice, ChanCache &cc, double plane_scale) {
+                                           int slot, VisRec<NC> *recs, ChanCache &cc, double plane_scale) {
   VisRec<NC> rec;
   prologue<NC, WPROJ>(a, f_local, chan, row, in_range, rec, cc, plane_scale);
   recs[slot] = rec;
-  if (a.norm && a.tap_sums && rec.valid) {
-    const double *su = a.tap_sums + 2 * ((long long)rec.plane * a.tap_f + rec.fu0);
-    const double *sv = a.tap_sums + 2 * ((long long)rec.plane * a.tap_f + rec.fv0);
-    const NormTerm nt = (NormTerm)(su[0] * sv[0] - su[1] * sv[1]);
-    NormAcc *na = s_nacc + slot * NC;
-    if (s_ng[slot] != rec.g) {
-      if (s_ng[slot] >= 0) {
-        s_mixed[slot] = 1;
+}
+
+// Normalisation term of a staged visibility from the precomputed kernel row sums, added to its
+// slot's running sums (which go to the global normalisation when the slot's grid group changes).
+// Runs after the chunk's records are published, so its table loads overlap the tap copies instead
+// of lengthening the prologue.
+template <int NC>
+__device__ __forceinline__ void norm_slot(const GridArgs &a, const VisRec<NC> &rec, int slot, NormAcc *s_nacc,
+                                          int *s_ng, long long fslice) {
+  if (!rec.valid) return;
+  const double *su = a.tap_sums + 2 * ((long long)rec.plane * a.tap_f + rec.fu0);
+  const double *sv = a.tap_sums + 2 * ((long long)rec.plane * a.tap_f + rec.fv0);
+  const NormTerm nt = (NormTerm)(su[0] * sv[0] - su[1] * sv[1]);
+  NormAcc *na = s_nacc + slot * NC;
+  if (s_ng[slot] != rec.g) {
+    if (s_ng[slot] >= 0) {
 #pragma unroll
-        for (int k = 0; k < NC; ++k)
-          if (norm_value(na[k]) != 0.0) atomicAdd(&a.norm[(fslice + s_ng[slot]) * NC + k], norm_value(na[k]));
-      }
-#pragma unroll
-      for (int k = 0; k < NC; ++k) norm_zero(na[k]);
-      s_ng[slot] = rec.g;
+      for (int k = 0; k < NC; ++k)
+        if (norm_value(na[k]) != 0.0) atomicAdd(&a.norm[(fslice + s_ng[slot]) * NC + k], norm_value(na[k]));
     }
 #pragma unroll
-    for (int k = 0; k < NC; ++k) norm_add(na[k], (NormTerm)rec.cw[k] * nt);
+    for (int k = 0; k < NC; ++k) norm_zero(na[k]);
+    s_ng[slot] = rec.g;
   }
+#pragma unroll
+  for (int k = 0; k < NC; ++k) norm_add(na[k], (NormTerm)rec.cw[k] * nt);
 }
 
 // Runs of a staged chunk, found by one warp: maximal stretches of valid staged visibilities with
@@ -786,7 +790,7 @@ template <int NC, bool WPROJ>
 __device__ __forceinline__ void norm_from_taps(const GridArgs &a, const VisRec<NC> *recs, int nv, int TVS,
                                                const typename TapT<WPROJ>::type *tu,
                                                const typename TapT<WPROJ>::type *tv, NormAcc *s_nacc, int *s_ng,
-                                               int *s_mixed, long long fslice) {
+                                               long long fslice) {
   const int W = a.W;
   const int tid = threadIdx.x;
   for (int b4 = tid & ~31; b4 < 4 * nv; b4 += blockDim.x) {
@@ -819,7 +823,6 @@ __device__ __forceinline__ void norm_from_taps(const GridArgs &a, const VisRec<N
       NormAcc *na = s_nacc + vi * NC;
       if (s_ng[vi] != r.g) {
         if (s_ng[vi] >= 0) {
-          s_mixed[vi] = 1;
 #pragma unroll
           for (int k = 0; k < NC; ++k)
             if (norm_value(na[k]) != 0.0) atomicAdd(&a.norm[(fslice + s_ng[vi]) * NC + k], norm_value(na[k]));
@@ -836,8 +839,9 @@ __device__ __forceinline__ void norm_from_taps(const GridArgs &a, const VisRec<N
 
 // Multiply-adds of a staged chunk's runs into an owner thread's cells.  When the footprint moves,
 // the owned cells are recomputed and those that changed are flushed (queued for the warp's
-// compensated flush in single precision).  Every lane of a warp with any owned cell calls this, so
-// the queue drains are warp-uniform.
+// compensated flush in single precision; the queue is drained when it fills and at the end of the
+// track).  Every lane of a warp with any owned cell calls this, so the queue drains are
+// warp-uniform.
 template <int NC, bool WPROJ, int J, bool COMP>
 __device__ __forceinline__ void grid_runs(const GridArgs &a, const VisRec<NC> *recs,
                                           const typename TapT<WPROJ>::type *tu,
@@ -919,7 +923,6 @@ __device__ __forceinline__ void grid_runs(const GridArgs &a, const VisRec<NC> *r
     }
     st.dirty = rows_mask;
   }
-  if (COMP) drain_queue<NC>(a, nxy, fq, fqn);
 }
 
 // One track (facet, channel, rows [r0, r1)) of one CTA: the rows are staged V at a time (prologue,
@@ -934,8 +937,7 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
   VisRec<NC> *recs = reinterpret_cast<VisRec<NC> *>(smem_raw);                          // [V]
   NormAcc *s_nacc = reinterpret_cast<NormAcc *>(smem_raw + sizeof(VisRec<NC>) * (size_t)V);  // [V][NC]
   int *s_ng = reinterpret_cast<int *>(s_nacc + (size_t)V * NC);                             // [V]
-  int *s_mixed = s_ng + V;                                                                  // [V]
-  int *s_runs = s_mixed + V;                                                                // [V + 1]
+  int *s_runs = s_ng + V;                                                                   // [V + 1]
   tap_t *tu = reinterpret_cast<tap_t *>(smem_raw + stage_head_bytes<NC>(V));               // [V][W]
   tap_t *tv = tu + V * W;                                                                   // [V][TVS]
   // per-warp flush queues follow the taps
@@ -945,9 +947,7 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
   FlushRec<NC> *fq = reinterpret_cast<FlushRec<NC> *>(qbase) + warp_id * kFlushQueueCap;
   int *fqn = reinterpret_cast<int *>(qbase + nwarps * sizeof(FlushRec<NC>) * kFlushQueueCap) + warp_id * 4;
   if (COMP && (threadIdx.x & 31) == 0) *fqn = 0;
-  __shared__ int s_same_g;
   __shared__ int s_nruns;
-  __shared__ double s_norm[NC];
 
   const FacetXform &fxt = a.facets[f_local];
   const int gnx = fxt.nx;
@@ -972,7 +972,6 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
 #pragma unroll
     for (int k = 0; k < NC; ++k) norm_zero(s_nacc[tid * NC + k]);
     s_ng[tid] = -1;
-    s_mixed[tid] = 0;
   }
 
   OwnerState<NC, J> st;
@@ -992,20 +991,21 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
 
   for (long long base = r0; base < r1; base += V) {
     const int nv = (int)min((long long)V, r1 - base);
-    if (tid < V)
-      stage_slot<NC, WPROJ>(a, f_local, chan, base + tid, tid < nv, tid, recs, s_nacc, s_ng, s_mixed, fslice, cc,
-                            plane_scale);
+    if (tid < V) stage_slot<NC, WPROJ>(a, f_local, chan, base + tid, tid < nv, tid, recs, cc, plane_scale);
     __syncthreads();
     if (warp_id == 0) find_runs<NC>(recs, nv, s_runs, &s_nruns);
     stage_taps<NC, WPROJ>(a, recs, nv, TVS, tu, tv);
+    if (want_norm && a.tap_sums && tid < nv) norm_slot<NC>(a, recs[tid], tid, s_nacc, s_ng, fslice);
     wait_taps();
     __syncthreads();
-    if (want_norm && !a.tap_sums) norm_from_taps<NC, WPROJ>(a, recs, nv, TVS, tu, tv, s_nacc, s_ng, s_mixed, fslice);
+    if (want_norm && !a.tap_sums) norm_from_taps<NC, WPROJ>(a, recs, nv, TVS, tu, tv, s_nacc, s_ng, fslice);
     if (grids)
       grid_runs<NC, WPROJ, J, COMP>(a, recs, tu, tv, s_runs, s_nruns, TVS, du, strip, rows_mask, fbase, nxy, gnx, fq,
                                     fqn, st);
     __syncthreads();
   }
+  // the flush queues carry over from chunk to chunk; empty them before the final flush
+  if (COMP && grids) drain_queue<NC>(a, nxy, fq, fqn);
   // final flush of owned cells
   if (st.dirty) {
 #pragma unroll
@@ -1015,32 +1015,31 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
         flush_cell<NC, COMP>(a, fbase + (long long)st.cg * NC * nxy, nxy, gnx, st.pu0 + st.ou, st.pv0 + oy, st.acc[j]);
     }
   }
-  // normalisation: one reduction per CTA when every staging slot saw a single grid group
+  // normalisation: the slots' current partial sums (earlier grid groups went out when the group
+  // changed), summed over each warp by shuffles when its slots share one group (one atomic per
+  // correlation and warp), added slot by slot otherwise.  The slots' state was last written before
+  // the chunk loop's final barrier.
   if (want_norm) {
-    if (tid == 0) s_same_g = -1;
-    if (tid < NC) s_norm[tid] = 0.0;
-    __syncthreads();
-    const int my_g = tid < V ? s_ng[tid] : -1;
-    if (my_g >= 0) atomicMax(&s_same_g, my_g);
-    __syncthreads();
-    const int gmax = s_same_g;
-    const bool uniform_here = tid >= V || (!s_mixed[tid] && (my_g < 0 || my_g == gmax));
-    const int all_uniform = __syncthreads_and(uniform_here ? 1 : 0);
-    if (tid < V && my_g >= 0) {
-      const NormAcc *na = s_nacc + tid * NC;
-      if (all_uniform) {
+    const bool has = tid < V && s_ng[tid] >= 0;
+    const int my_g = has ? s_ng[tid] : -1;
+    const unsigned m = __ballot_sync(0xffffffffu, has);
+    if (m) {
+      const int g0 = __shfl_sync(0xffffffffu, my_g, __ffs(m) - 1);
+      const NormAcc *na = s_nacc + (has ? tid : 0) * NC;
+      if (__all_sync(0xffffffffu, !has || my_g == g0)) {
 #pragma unroll
-        for (int k = 0; k < NC; ++k)
-          if (norm_value(na[k]) != 0.0) atomicAdd(&s_norm[k], norm_value(na[k]));
-      } else {
+        for (int k = 0; k < NC; ++k) {
+          double v = has ? norm_value(na[k]) : 0.0;
+#pragma unroll
+          for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+          if ((tid & 31) == 0 && v != 0.0) atomicAdd(&a.norm[(fslice + g0) * NC + k], v);
+        }
+      } else if (has) {
 #pragma unroll
         for (int k = 0; k < NC; ++k)
           if (norm_value(na[k]) != 0.0) atomicAdd(&a.norm[(fslice + my_g) * NC + k], norm_value(na[k]));
       }
     }
-    __syncthreads();
-    if (all_uniform && tid < NC && gmax >= 0 && s_norm[tid] != 0.0)
-      atomicAdd(&a.norm[(fslice + gmax) * NC + tid], s_norm[tid]);
   }
 }
 
