@@ -216,6 +216,8 @@ struct BatchedState {
   DevBuf<int> nseg, seg_off, seg_total, class_count, class_off, class_cursor, work_next, sample_count;
   DevBuf<int4> segs, sorted;
   DevBuf<FacetXform> facet_table;  // per-facet geometry of bullseye_grid_batched_facets
+  DevBuf<vis_real> conv_w;         // support-window table [P][tap_f][conv_w_stride] (plan_classes)
+  int conv_w_stride = 0;
   size_t rows_cap = 0, tracks_cap = 0, segs_cap = 0;
   // tuning decisions, by (class width, NC, WPROJ, COMP)
   std::map<std::tuple<int, int, int, int>, std::tuple<int, int, int>> tuned;  // -> (J, wide, regs)
@@ -279,6 +281,32 @@ bool plan_classes() {
     if (std::find(pw.begin(), pw.end(), w) != pw.end()) widths.push_back(w);
   std::vector<int> pcls(P);
   for (int p = 0; p < P; ++p) pcls[p] = (int)(std::find(widths.begin(), widths.end(), pw[p]) - widths.begin());
+  // Support-window table: row (plane p, tap offset f) holds the taps s = plo[p] + j,
+  // j < pw[p] (conv[p][f + s os]), then its first 7 taps again (the J - 1 <= 7 repeated leading
+  // row taps of a Romein strip), zero-padded to a multiple of 16 bytes.  A staged tap row is then
+  // one 16-byte aligned bulk copy from the row start.
+  {
+    const size_t ncomp = wproj ? 2 : 1;
+    const int E = (int)(16 / (ncomp * sizeof(vis_real)));
+    const int pwmax = *std::max_element(pw.begin(), pw.end());
+    const int L = (pwmax + 7 + E - 1) / E * E;
+    const size_t tf = c.tap_f;
+    std::vector<vis_real> tab(ncomp * (size_t)P * tf * L, (vis_real)0);
+    for (int p = 0; p < P; ++p)
+      for (size_t f = 0; f < tf; ++f) {
+        vis_real *row = tab.data() + ncomp * (((size_t)p * tf + f) * L);
+        for (int j = 0; j < pw[p]; ++j) {
+          const size_t i = f + (size_t)(plo[p] + j) * os;
+          if (i >= (size_t)K) break;
+          for (size_t q = 0; q < ncomp; ++q) row[ncomp * j + q] = c.conv_host[ncomp * ((size_t)p * K + i) + q];
+        }
+        for (int j = pw[p]; j < pw[p] + 7; ++j)
+          for (size_t q = 0; q < ncomp; ++q) row[ncomp * j + q] = row[ncomp * (j - pw[p]) + q];
+      }
+    if (!b.conv_w.alloc(tab.size())) return false;
+    BZ_CUDA_TRY_RET(cudaMemcpy(b.conv_w.ptr, tab.data(), sizeof(vis_real) * tab.size(), cudaMemcpyHostToDevice), false);
+    b.conv_w_stride = L;
+  }
   b.plane_width = pw;
   b.ncls = (int)widths.size();
   if (b.ncls > kMaxClasses) return false;
@@ -341,6 +369,8 @@ bool launch_class(const GridArgs &base, int k, const Variant &v, int nfacets, co
   a.W = g_bs.cls[k].width;
   a.V = v.V;
   a.plane_lo = g_bs.plane_lo.ptr;
+  a.conv_w = g_bs.conv_w.ptr;
+  a.conv_w_stride = g_bs.conv_w_stride;
   a.segments = g_bs.sorted.ptr;
   a.segment_base = g_bs.class_off.ptr + k;
   a.segment_capacity = (long long)g_bs.segs_cap;
@@ -529,6 +559,8 @@ void bz_release_batched() {
   b.plane_class.release(); b.plane_lo.release(); b.row_class.release(); b.nseg.release(); b.seg_off.release();
   b.seg_total.release(); b.class_count.release(); b.class_off.release(); b.class_cursor.release();
   b.work_next.release(); b.sample_count.release(); b.segs.release(); b.sorted.release(); b.facet_table.release();
+  b.conv_w.release();
+  b.conv_w_stride = 0;
   b.rows_cap = b.tracks_cap = b.segs_cap = 0;
   b.planned = false;
   b.ncls = 0;

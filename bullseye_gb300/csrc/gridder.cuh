@@ -93,6 +93,9 @@ struct GridArgs {
   const double *tap_sums;        // FP64 complex [P][tap_f] row sums of the kernel, or null
   int tap_f;
   const void *conv_t;            // kernel regrouped by tap offset [P][tap_f][W], or null
+  const void *conv_w;            // support-window rows [P][tap_f][conv_w_stride], or null (see
+                                 // the batched planner): a staged tap row is one bulk copy
+  int conv_w_stride;
   const uint8_t *facet_row_mask; // [facets][rows]: 0 leaves the row out of that facet, or null
   const FacetXform *facets;
   // outputs
@@ -123,7 +126,13 @@ struct GridArgs {
 };
 
 // Error bits written to GridArgs::error (host decodes them)
-enum DeviceError { DEV_ERR_GRID_INDEX = 1, DEV_ERR_JONES_INDEX = 2, DEV_ERR_SINGULAR = 4, DEV_ERR_POL_INDEX = 8 };
+enum DeviceError {
+  DEV_ERR_GRID_INDEX = 1,
+  DEV_ERR_JONES_INDEX = 2,
+  DEV_ERR_SINGULAR = 4,
+  DEV_ERR_POL_INDEX = 8,
+  DEV_ERR_WAIT_TIMEOUT = 16  // a bounded wait on the tap-copy barrier ran out
+};
 
 template <bool WPROJ>
 struct TapT;
@@ -556,7 +565,11 @@ __device__ __forceinline__ void prologue(const GridArgs &a, int f_local, int cha
     rec.fu += lo * a.os;
     rec.fv += lo * a.os;
   }
-  if (a.conv_t) {
+  if (a.conv_w) {
+    // start of the (plane, tap offset) row of the support-window table (window start included)
+    rec.fu = (int)(((long long)plane * a.tap_f + cell.fu) * a.conv_w_stride);
+    rec.fv = (int)(((long long)plane * a.tap_f + cell.fv) * a.conv_w_stride);
+  } else if (a.conv_t) {
     // index of the first staged tap in the regrouped table
     const int Wfull = a.W_full ? a.W_full : a.W;
     rec.fu = (int)(((long long)plane * a.tap_f + cell.fu) * Wfull + lo);
@@ -589,6 +602,19 @@ __host__ __device__ inline size_t flush_queue_bytes(int nwarps) {
 // Row taps are stored W + J - 1 long per visibility: the first J - 1 taps are repeated after the
 // last, so a thread's J consecutive owned rows read J consecutive taps without a wrap.
 
+// Staged tap rows per visibility: W column taps, then W + J - 1 row taps (the first J - 1 repeated
+// after the last), each row padded to a multiple of 16 bytes so that it can be one bulk copy.
+template <bool WPROJ>
+__host__ __device__ inline int tap_row_u(int W) {
+  constexpr int E = (int)(16 / sizeof(typename TapT<WPROJ>::type));
+  return (W + E - 1) / E * E;
+}
+template <bool WPROJ>
+__host__ __device__ inline int tap_row_v(int W, int J) {
+  constexpr int E = (int)(16 / sizeof(typename TapT<WPROJ>::type));
+  return (W + J - 1 + E - 1) / E * E;
+}
+
 // Bytes before the tap arrays: V staged records, their normalisation state (partial sums, grid
 // group), the V + 1 run starts of the chunk; rounded up to 16.
 template <int NC>
@@ -598,7 +624,7 @@ __host__ __device__ inline size_t stage_head_bytes(int V) {
 
 template <int NC, bool WPROJ>
 __host__ __device__ inline size_t grid_smem_bytes(int V, int W, int nthreads, int J) {
-  size_t taps = sizeof(typename TapT<WPROJ>::type) * (size_t)V * (2 * W + J - 1);
+  size_t taps = sizeof(typename TapT<WPROJ>::type) * (size_t)V * (tap_row_u<WPROJ>(W) + tap_row_v<WPROJ>(W, J));
   return stage_head_bytes<NC>(V) + taps + flush_queue_bytes<NC>((nthreads + 31) / 32) + 64;
 }
 
@@ -612,7 +638,7 @@ __host__ inline int grid_chunk_size(int W, int nthreads, int J, int regs = 128) 
   const size_t fixed = flush_queue_bytes<NC>((nthreads + 31) / 32) + 64 + sizeof(int) + 15;
   budget = budget > fixed ? budget - fixed : 0;
   const size_t per = sizeof(VisRec<NC>) + sizeof(NormAcc) * NC + 2 * sizeof(int) +
-                     sizeof(typename TapT<WPROJ>::type) * (2 * (size_t)W + J - 1);
+                     sizeof(typename TapT<WPROJ>::type) * (size_t)(tap_row_u<WPROJ>(W) + tap_row_v<WPROJ>(W, J));
   return std::max(1, (int)std::min<size_t>(nthreads, budget / per));
 }
 
@@ -743,8 +769,9 @@ __device__ __forceinline__ void wait_taps() { asm volatile("cp.async.commit_grou
 // Taps of every valid staged visibility: W column taps, then W + J - 1 row taps, issued as
 // asynchronous copies (the caller runs wait_taps() before the barrier that publishes them).  Thread
 // tid walks (visibility, tap) pairs with a stride of blockDim.x pairs, stepped without division.
+// Rows are stored with strides TUS and TVS (padded to 16 bytes).
 template <int NC, bool WPROJ>
-__device__ __forceinline__ void stage_taps(const GridArgs &a, const VisRec<NC> *recs, int nv, int TVS,
+__device__ __forceinline__ void stage_taps(const GridArgs &a, const VisRec<NC> *recs, int nv, int J, int TUS, int TVS,
                                            typename TapT<WPROJ>::type *tu, typename TapT<WPROJ>::type *tv) {
   typedef typename TapT<WPROJ>::type tap_t;
   typedef typename std::conditional<WPROJ, vis_complex, vis_real>::type stored_t;
@@ -754,7 +781,7 @@ __device__ __forceinline__ void stage_taps(const GridArgs &a, const VisRec<NC> *
   // table is read through registers
   const bool aligned = (reinterpret_cast<uintptr_t>(table) & (sizeof(tap_t) - 1)) == 0;
   const int W = a.W;
-  const int per = W + TVS;
+  const int per = 2 * W + J - 1;
   const int tid = threadIdx.x;
   int vi = tid / per, j = tid - vi * per;
   const int svi = (int)blockDim.x / per, sj = (int)blockDim.x - svi * per;
@@ -767,7 +794,7 @@ __device__ __forceinline__ void stage_taps(const GridArgs &a, const VisRec<NC> *
       if (jj >= W) jj = W - 1;
       const long long idx = a.conv_t ? (long long)(isv ? h1.w : h1.z) + jj
                                      : (long long)recs[vi].plane * a.K + (isv ? h1.w : h1.z) + (long long)jj * a.os;
-      tap_t *dst = isv ? &tv[vi * TVS + js] : &tu[vi * W + js];
+      tap_t *dst = isv ? &tv[vi * TVS + js] : &tu[vi * TUS + js];
       if (aligned) {
         copy_tap_async<sizeof(tap_t)>(dst, table + idx);
       } else {
@@ -783,11 +810,76 @@ __device__ __forceinline__ void stage_taps(const GridArgs &a, const VisRec<NC> *
   }
 }
 
+// Tap-copy barrier (mbarrier) of the bulk-copy staging: V arrivals per chunk, one per staging
+// slot, each announcing the bytes of its two row copies.  Waits are bounded.
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void bar_init(unsigned long long *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+__device__ __forceinline__ void bar_arrive(unsigned long long *bar) {
+  asm volatile("{\n.reg .b64 st;\nmbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void bar_arrive_tx(unsigned long long *bar, unsigned bytes) {
+  asm volatile("{\n.reg .b64 st;\nmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}\n" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// Non-blocking test of the phase of the given parity.
+__device__ __forceinline__ bool bar_test(unsigned long long *bar, unsigned parity) {
+  unsigned done;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// Bounded wait for the phase of the given parity (polls, then polls with short sleeps: about 0.2 s
+// at most); false when the bound ran out.
+__device__ __forceinline__ bool bar_wait(unsigned long long *bar, unsigned parity) {
+  for (int i = 0; i < (1 << 22); ++i) {
+    if (bar_test(bar, parity)) return true;
+    if (i >= 64) __nanosleep(32);
+  }
+  return false;
+}
+// One bulk (TMA) copy global -> shared of `bytes` (16-byte aligned addresses, a multiple of 16
+// bytes) that completes its bytes on the barrier.
+__device__ __forceinline__ void bulk_copy(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
+// Bulk-copy staging of a chunk's taps from the support-window table: staging slot tid copies its
+// visibility's column row (TUS taps) and row row (TVS taps, the repeated leading taps included) as
+// two bulk copies and arrives on the barrier with their bytes; an empty slot arrives without bytes.
+template <int NC, bool WPROJ>
+__device__ __forceinline__ void stage_taps_bulk(const GridArgs &a, const VisRec<NC> *recs, int nv, int TUS, int TVS,
+                                                typename TapT<WPROJ>::type *tu, typename TapT<WPROJ>::type *tv,
+                                                unsigned long long *bar) {
+  typedef typename TapT<WPROJ>::type tap_t;
+  const int tid = threadIdx.x;
+  if (tid >= a.V) return;
+  const int4 h1 = *reinterpret_cast<const int4 *>(&recs[tid].g);  // g, valid, fu, fv
+  if (tid < nv && h1.y) {
+    const tap_t *table = reinterpret_cast<const tap_t *>(a.conv_w);
+    const unsigned bu = (unsigned)(sizeof(tap_t) * TUS), bv = (unsigned)(sizeof(tap_t) * TVS);
+    bar_arrive_tx(bar, bu + bv);
+    bulk_copy(tu + tid * TUS, table + h1.z, bu, bar);
+    bulk_copy(tv + tid * TVS, table + h1.w, bv, bar);
+  } else {
+    bar_arrive(bar);
+  }
+}
+
 // Normalisation without precomputed row sums (the allocation-free entry), four lanes per staged
 // visibility: Re(sum_u k_u * sum_v k_v) x weight x flag (loop bounds are warp-uniform so the
 // shuffles always see full warps); lane 4i owns the running sums of staged slot i.
 template <int NC, bool WPROJ>
-__device__ __forceinline__ void norm_from_taps(const GridArgs &a, const VisRec<NC> *recs, int nv, int TVS,
+__device__ __forceinline__ void norm_from_taps(const GridArgs &a, const VisRec<NC> *recs, int nv, int TUS, int TVS,
                                                const typename TapT<WPROJ>::type *tu,
                                                const typename TapT<WPROJ>::type *tv, NormAcc *s_nacc, int *s_ng,
                                                long long fslice) {
@@ -801,11 +893,11 @@ __device__ __forceinline__ void norm_from_taps(const GridArgs &a, const VisRec<N
     acc_real sur = 0, sui = 0, svr = 0, svi = 0;
     if (act) {
       if (WPROJ) {
-        const cplx *pu = reinterpret_cast<const cplx *>(tu) + vi * W;
+        const cplx *pu = reinterpret_cast<const cplx *>(tu) + vi * TUS;
         const cplx *pv = reinterpret_cast<const cplx *>(tv) + vi * TVS;
         for (int j = part; j < W; j += 4) { sur += pu[j].re; sui += pu[j].im; svr += pv[j].re; svi += pv[j].im; }
       } else {
-        const acc_real *pu = reinterpret_cast<const acc_real *>(tu) + vi * W;
+        const acc_real *pu = reinterpret_cast<const acc_real *>(tu) + vi * TUS;
         const acc_real *pv = reinterpret_cast<const acc_real *>(tv) + vi * TVS;
         for (int j = part; j < W; j += 4) { sur += pu[j]; svr += pv[j]; }
       }
@@ -846,7 +938,7 @@ template <int NC, bool WPROJ, int J, bool COMP>
 __device__ __forceinline__ void grid_runs(const GridArgs &a, const VisRec<NC> *recs,
                                           const typename TapT<WPROJ>::type *tu,
                                           const typename TapT<WPROJ>::type *tv, const int *runs, int nruns,
-                                          int TVS, int du, int strip, unsigned rows_mask, long long fbase,
+                                          int TUS, int TVS, int du, int strip, unsigned rows_mask, long long fbase,
                                           long long nxy, int gnx, FlushRec<NC> *fq, int *fqn,
                                           OwnerState<NC, J> &st) {
   typedef typename TapT<WPROJ>::type tap_t;
@@ -909,7 +1001,7 @@ __device__ __forceinline__ void grid_runs(const GridArgs &a, const VisRec<NC> *r
     // owned rows (offsets modulo W; rows of non-owning lanes stay in bounds and are never flushed)
 #pragma unroll 2
     for (int vi = rs; vi < re; ++vi) {
-      const tap_t tuv = tu[vi * W + st.ou];
+      const tap_t tuv = tu[vi * TUS + st.ou];
       cplx pre[NC];
 #pragma unroll
       for (int k = 0; k < NC; ++k) pre[k] = premul(recs[vi].vis[k], tuv);
@@ -926,20 +1018,23 @@ __device__ __forceinline__ void grid_runs(const GridArgs &a, const VisRec<NC> *r
 }
 
 // One track (facet, channel, rows [r0, r1)) of one CTA: the rows are staged V at a time (prologue,
-// runs, taps) and gridded by the Romein owner threads.
+// runs, taps) and gridded by the Romein owner threads.  With a tap-copy barrier (`bar`, whose
+// phase parity `phase` carries over from track to track) and the support-window table, a staged
+// visibility's tap rows are two bulk copies; otherwise per-tap asynchronous copies.
 template <int NC, bool WPROJ, int J, bool COMP, bool WIDE>
 __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local, const int chan, long long r0,
-                                           long long r1) {
+                                           long long r1, unsigned long long *bar, unsigned &phase) {
   typedef typename TapT<WPROJ>::type tap_t;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int V = a.V, W = a.W;
-  const int TVS = W + J - 1;  // row-tap stride per staged visibility
+  const int TUS = tap_row_u<WPROJ>(W), TVS = tap_row_v<WPROJ>(W, J);  // staged row strides
+  const bool bulk = bar != nullptr && a.conv_w != nullptr;
   VisRec<NC> *recs = reinterpret_cast<VisRec<NC> *>(smem_raw);                          // [V]
   NormAcc *s_nacc = reinterpret_cast<NormAcc *>(smem_raw + sizeof(VisRec<NC>) * (size_t)V);  // [V][NC]
   int *s_ng = reinterpret_cast<int *>(s_nacc + (size_t)V * NC);                             // [V]
   int *s_runs = s_ng + V;                                                                   // [V + 1]
-  tap_t *tu = reinterpret_cast<tap_t *>(smem_raw + stage_head_bytes<NC>(V));               // [V][W]
-  tap_t *tv = tu + V * W;                                                                   // [V][TVS]
+  tap_t *tu = reinterpret_cast<tap_t *>(smem_raw + stage_head_bytes<NC>(V));               // [V][TUS]
+  tap_t *tv = tu + V * TUS;                                                                 // [V][TVS]
   // per-warp flush queues follow the taps
   unsigned char *qbase = reinterpret_cast<unsigned char *>(tv + V * TVS);
   qbase = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(qbase) + 15) & ~(uintptr_t)15);
@@ -993,15 +1088,28 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
     const int nv = (int)min((long long)V, r1 - base);
     if (tid < V) stage_slot<NC, WPROJ>(a, f_local, chan, base + tid, tid < nv, tid, recs, cc, plane_scale);
     __syncthreads();
+    if (bulk)
+      stage_taps_bulk<NC, WPROJ>(a, recs, nv, TUS, TVS, tu, tv, bar);
+    else
+      stage_taps<NC, WPROJ>(a, recs, nv, J, TUS, TVS, tu, tv);
     if (warp_id == 0) find_runs<NC>(recs, nv, s_runs, &s_nruns);
-    stage_taps<NC, WPROJ>(a, recs, nv, TVS, tu, tv);
     if (want_norm && a.tap_sums && tid < nv) norm_slot<NC>(a, recs[tid], tid, s_nacc, s_ng, fslice);
-    wait_taps();
+    if (bulk) {
+      // every thread observes the phase (the copies' data is visible to the threads that do);
+      // a wait that runs out is recorded, then waited for once more before the data is used
+      if (!bar_wait(bar, phase)) {
+        atomicOr(a.error, DEV_ERR_WAIT_TIMEOUT);
+        bar_wait(bar, phase);
+      }
+      phase ^= 1u;
+    } else {
+      wait_taps();
+    }
     __syncthreads();
-    if (want_norm && !a.tap_sums) norm_from_taps<NC, WPROJ>(a, recs, nv, TVS, tu, tv, s_nacc, s_ng, fslice);
+    if (want_norm && !a.tap_sums) norm_from_taps<NC, WPROJ>(a, recs, nv, TUS, TVS, tu, tv, s_nacc, s_ng, fslice);
     if (grids)
-      grid_runs<NC, WPROJ, J, COMP>(a, recs, tu, tv, s_runs, s_nruns, TVS, du, strip, rows_mask, fbase, nxy, gnx, fq,
-                                    fqn, st);
+      grid_runs<NC, WPROJ, J, COMP>(a, recs, tu, tv, s_runs, s_nruns, TUS, TVS, du, strip, rows_mask, fbase, nxy, gnx,
+                                    fq, fqn, st);
     __syncthreads();
   }
   // the flush queues carry over from chunk to chunk; empty them before the final flush
@@ -1066,17 +1174,21 @@ __global__ void __launch_bounds__(512, 1) romein_grid_kernel(const GridArgs a) {
     r0 = (long long)slot * a.seg;
     r1 = min(a.nrows, r0 + a.seg);
   }
-  grid_track<NC, WPROJ, J, COMP, WIDE>(a, f_local, chan, r0, r1);
+  unsigned phase = 0;
+  grid_track<NC, WPROJ, J, COMP, WIDE>(a, f_local, chan, r0, r1, nullptr, phase);
 }
 
 // Persistent form: a fixed grid of CTAs takes (segment, facet) work items from a device counter
 // until the device-side item count is exhausted; every segment is a run of one track's rows
 // whose w planes share this launch's support class (a.W).  Items of one segment are adjacent, so
 // the facets of a segment are gridded while its rows are hot in L2.  The loop ends on the count,
-// never waits on other CTAs.
+// never waits on other CTAs.  The tap-copy barrier is set up once (V arrivals per phase).
 template <int NC, bool WPROJ, int J, bool COMP, bool WIDE, int REGS = kSegRegs<J>>
 __global__ void __launch_bounds__(512, 1) __maxnreg__(REGS) romein_segment_kernel(const GridArgs a, const int nfacets) {
   __shared__ int s_item;
+  __shared__ __align__(8) unsigned long long s_tap_bar;
+  unsigned phase = 0;
+  if (threadIdx.x == 0) bar_init(&s_tap_bar, (unsigned)a.V);
   const int count = *a.work_count;
   const long long total = (long long)count * nfacets;
   for (;;) {
@@ -1097,7 +1209,7 @@ __global__ void __launch_bounds__(512, 1) __maxnreg__(REGS) romein_segment_kerne
       if (threadIdx.x == 0) atomicOr(a.error, DEV_ERR_GRID_INDEX);
       continue;
     }
-    grid_track<NC, WPROJ, J, COMP, WIDE>(a, f_local, sg.z, sg.x, sg.y);
+    grid_track<NC, WPROJ, J, COMP, WIDE>(a, f_local, sg.z, sg.x, sg.y, &s_tap_bar, phase);
   }
 }
 

@@ -90,6 +90,7 @@ static void drain_device_error() {
     if (h & DEV_ERR_SINGULAR) bz_record_error(BZ_ERR_SINGULAR_JONES, "Jones matrix set contains singular matrices");
     if (h & DEV_ERR_GRID_INDEX) bz_record_error(BZ_ERR_INVALID_ARGUMENT, "channel grid index out of range of the cube");
     if (h & DEV_ERR_JONES_INDEX) bz_record_error(BZ_ERR_INVALID_ARGUMENT, "timestamp or antenna id out of range of the Jones terms");
+    if (h & DEV_ERR_WAIT_TIMEOUT) bz_record_error(BZ_ERR_CUDA, "gridder: a bounded wait for staged kernel taps ran out");
     int z = 0;
     cudaMemcpy(g_ctx.dev_error.ptr, &z, sizeof(int), cudaMemcpyHostToDevice);
   }
