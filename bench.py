@@ -283,19 +283,20 @@ def set_rows(st, d, ptr):
 
 # ----------------------------------------------------------------------------- clocks
 class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples every 200 ms between start() and stop(); the raw
+    samples are also written to `path` when one is given."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, path):
+    def __init__(self, path=None):
         self.path = path
         self.proc = None
 
     def start(self):
         try:
-            self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                                          "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
 
@@ -304,13 +305,15 @@ class ClockSampler:
             return None
         self.proc.terminate()
         try:
-            self.proc.wait(timeout=5)
+            out = self.proc.communicate(timeout=5)[0] or ""
         except Exception:
             self.proc.kill()
-        self.fh.close()
+            out = ""
+        if self.path:
+            with open(self.path, "w") as fh:
+                fh.write(out)
         sm, mx, reasons = [], [], set()
-        dev = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]
-        for line in open(self.path):
+        for line in out.splitlines():
             parts = [x.strip() for x in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -327,6 +330,12 @@ class ClockSampler:
             return None
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def clocks_path(name):
+    """Where the raw clock samples go: gpurun_out/ when it exists, else nowhere."""
+    d = os.path.join(REPO, "gpurun_out")
+    return os.path.join(d, name) if os.path.isdir(d) else None
 
 
 # ----------------------------------------------------------------------------- CPU (oracle port)
@@ -515,8 +524,7 @@ def uneven_main(args):
     torch.cuda.synchronize()
     check(lib)
     lib.bullseye_reset_counters()
-    clocks = ClockSampler(os.path.join(REPO, "gpurun_out", "clocks.csv") if os.path.isdir(os.path.join(REPO, "gpurun_out"))
-                          else "/tmp/bullseye_clocks.csv")
+    clocks = ClockSampler(clocks_path("clocks.csv"))
     clocks.start()
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
@@ -830,8 +838,7 @@ def main():
     torch.cuda.synchronize()
     check(lib)
     lib.bullseye_reset_counters()
-    clocks = ClockSampler(os.path.join(REPO, "gpurun_out", "clocks.csv") if os.path.isdir(os.path.join(REPO, "gpurun_out"))
-                          else "/tmp/bullseye_clocks.csv")
+    clocks = ClockSampler(clocks_path("clocks.csv"))
     clocks.start()
     if world > 1:
         torch.distributed.barrier()
@@ -938,11 +945,14 @@ def main():
 
         e2e_step()
         parts.clear()
+        e2e_clocks = ClockSampler(clocks_path("clocks_e2e.csv"))
+        e2e_clocks.start()
         t0 = time.perf_counter()
         n_e2e = max(1, min(args.steps, 3))
         for _ in range(n_e2e):
             e2e_step()
         dt = (time.perf_counter() - t0) / n_e2e
+        e2e_clk = e2e_clocks.stop()
         h2d = sum(hnp[k].nbytes for k in ("vis", "weights", "flags", "uvw", "flagged_rows", "field", "spw", "a1",
                                           "a2", "tid", "jones", "starts"))
         h2d += tab.conv.nbytes + tab.grid.nbytes + tab.sf.nbytes  # tables and initial grids (initLibrary)
@@ -950,7 +960,7 @@ def main():
         d2h = tab.grid.nbytes + tab.sf.nbytes + N_FACETS * NX * NX * (8 + 4)
         e2e = {"value": pairs_per_step / dt / 1e6, "unit": "Mvis/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "s_per_step": dt,
-               "ms_by_call": {k: round(v / n_e2e, 1) for k, v in parts.items()},
+               "ms_by_call": {k: round(v / n_e2e, 1) for k, v in parts.items()}, "clocks": e2e_clk,
                "calls": ("initLibrary, " + ("facet_4_cor_corrections, facet_sampling_function"
                                              if args.form == "plain" else "bullseye_grid_batched(call 0, sampling)") +
                          ", weight_uniformly, normalize, finalize, releaseLibrary (host pinned buffers)")}
