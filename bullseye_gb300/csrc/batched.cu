@@ -569,6 +569,33 @@ void bz_release_batched() {
 // See include/bullseye_gb300.h.
 extern "C" void bullseye_set_batched_profiling(int on) { g_bs.profile = on != 0; }
 
+namespace {
+// Self-test of the bounded tap-barrier wait: the barrier expects two arrivals and gets one, so
+// every thread's wait must run out (about 0.2 s) and record DEV_ERR_WAIT_TIMEOUT.  No copy is in
+// flight, so nothing is left pending when the CTA exits.
+__global__ void bounded_wait_selftest_kernel(int *err) {
+  __shared__ __align__(8) unsigned long long bar;
+  if (threadIdx.x == 0) bar_init(&bar, 2);
+  __syncthreads();
+  if (threadIdx.x == 0) bar_arrive(&bar);
+  if (!bar_wait(&bar, 0) && threadIdx.x == 0) atomicOr(err, DEV_ERR_WAIT_TIMEOUT);
+}
+}  // namespace
+
+// See include/bullseye_gb300.h.
+extern "C" int bullseye_selftest_bounded_wait(void) {
+  int *d = nullptr, h = 0;
+  if (cudaMalloc(&d, sizeof(int)) != cudaSuccess) return -1;
+  bool ok = cudaMemset(d, 0, sizeof(int)) == cudaSuccess;
+  if (ok) {
+    bounded_wait_selftest_kernel<<<1, 32>>>(d);
+    ok = cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess &&
+         cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess;
+  }
+  cudaFree(d);
+  return ok ? h : -1;
+}
+
 // See include/bullseye_gb300.h.
 extern "C" int bullseye_batched_plane_classes(int *width, int max) {
   const auto &w = g_bs.plane_width;

@@ -147,6 +147,10 @@ int bullseye_batched_profile(int *width, int *nc, int *J, int *wide, int *items,
  * rounded up to a class width), up to max planes; returns the plane count (0 before the first
  * batched call after initLibrary). */
 int bullseye_batched_plane_classes(int *width, int max);
+/* Self-test of the batched gridder's bounded waits: runs one CTA whose tap-copy barrier never
+ * completes and returns the device error bits it recorded (16 = the wait ran out, as expected),
+ * or -1 on a CUDA error.  Takes about 0.2 s; touches no library state. */
+int bullseye_selftest_bounded_wait(void);
 
 /* Allocation-free facet_4_cor_corrections, for callers that cannot allocate device memory while
  * they grid (a fixed device arena with no further cudaMalloc/cudaFree, or code where a device

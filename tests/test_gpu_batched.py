@@ -114,3 +114,15 @@ def test_batched_graph_replay_is_stable(libs):
     two = _run(lib, p2, "facet_4_cor", chunks=2)
     assert rel(two.raw_grid, 2 * one.raw_grid) <= 1e-12
     assert rel(two.normalization, 2 * one.normalization) <= 1e-12
+
+
+@pytest.mark.parametrize("precision", ["single", "double"])
+def test_bounded_wait_runs_out_and_reports(precision, gpu_required, built_libraries):
+    """The tap-copy barrier's wait is bounded: a barrier that never completes (one arrival of two)
+    makes the wait run out and record the timeout bit, and the context stays usable."""
+    import torch
+    from bullseye_gb300.library import load_library
+    lib = load_library("GPU", precision)
+    assert lib.bullseye_selftest_bounded_wait() == 16
+    x = torch.ones(1024, device="cuda")
+    assert float(x.sum()) == 1024.0  # the device still runs work afterwards
