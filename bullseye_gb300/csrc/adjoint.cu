@@ -180,18 +180,36 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
   const long long nxy = (long long)a.nx * a.ny;
   const double plane_scale = WPROJ ? (double)(a.P - 1) / a.wmax : 0.0;
 
-  for (long long item = warp; item < a.nrows * a.nchan; item += nwarps) {
-    const long long row = item / a.nchan;
-    const int c = (int)(item - row * a.nchan);
-    const unsigned spw = a.spw[row];
-    if (spw >= (unsigned)a.nspw) continue;
-    const long long sc = (long long)spw * a.nchan + c;
-    if (!a.enabled[sc]) continue;
-    const size_t g = a.cgi[sc];
-    if (g >= (size_t)a.cube) continue;
-    ChanCache cc;  // used by lane 0 only
+  // Each warp takes 32 consecutive (row, channel) items at a time.  Lane i does the scalar work
+  // of item i: its loads, the FP64 geometry, the Jones inverses and the chain rule.  FP64 and the
+  // 2x2 algebra therefore run 32 items per instruction, not one (GB300 issues FP64 at 1/64 of
+  // FP32).  The warp then gathers the footprints one item at a time with every lane, and each
+  // item's sums land in its own lane.
+  const long long total = a.nrows * a.nchan;
+  for (long long base0 = warp * 32; base0 < total; base0 += nwarps * 32) {
+    const long long item = base0 + lane;
+    bool live = item < total;
+    long long row = 0, sc = 0;
+    int c = 0;
+    unsigned spw = 0;
+    size_t g = 0;
+    if (live) {
+      row = item / a.nchan;
+      c = (int)(item - row * a.nchan);
+      spw = a.spw[row];
+      live = spw < (unsigned)a.nspw;
+    }
+    if (live) {
+      sc = (long long)spw * a.nchan + c;
+      live = a.enabled[sc] != 0;
+    }
+    if (live) {
+      g = a.cgi[sc];
+      live = g < (size_t)a.cube;
+    }
+    ChanCache cc;
     double um = 0, vm = 0, wm = 0;
-    if (lane == 0) {
+    if (live) {
       cc.spw = spw;
       cc.inv = 1.0 / (double)a.wavelengths[sc];
       cc.su = cc.inv * a.u_scale;
@@ -201,25 +219,14 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
       vm = (double)a.uvw[3 * row + 1];
       wm = (double)a.uvw[3 * row + 2];
     }
-    const bool row_ok = !a.flagged_rows[row] && a.field[row] == a.imaging_field;
     const long long base = (row * a.nchan + c) * 4;
-    acc_real cw[4];
-    cplx V[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const bool keep = row_ok && !a.flags[base + k];
-      cw[k] = keep ? (acc_real)a.weights[base + k] : (acc_real)0;
-      V[k].re = a.vis[base + k].re;
-      V[k].im = a.vis[base + k].im;
-    }
     cplx gV[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) { gV[k].re = 0; gV[k].im = 0; }
 
     for (int f = 0; f < a.nfacets; ++f) {
-      // lane 0 resolves the Jones inverses and the geometry (FP64 is scarce on this GPU: no lane
-      // repeats it); the lanes share the footprint through shuffles
-      cplx Pm[4], Qm[4];
+      // this lane's item: Jones indices and the geometry (the gridder's own cell choice: same
+      // cells, taps, plane and phase)
       long long i1 = 0, i2 = 0;
       CellChoice cell;
       cell.du = cell.dv = cell.fu = cell.fv = cell.plane = 0;
@@ -227,82 +234,99 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
       cplx ph;
       ph.re = 1;
       ph.im = 0;
-      int ok = 0;
-      if (lane == 0) {
-        ok = 1;
-        if (a.jones) {
-          const long long t = (long long)a.time_ids[row];
-          const unsigned a1 = a.ant1[row], a2 = a.ant2[row];
-          if (t < 0 || t >= a.ntimes || a1 >= (unsigned)a.nant || a2 >= (unsigned)a.nant) {
-            ok = 0;
-          } else {
-            i1 = ((((t * a.nant + a1) * a.nfacets + f) * a.nspw + spw) * a.nchan + c) * 4;
-            i2 = ((((t * a.nant + a2) * a.nfacets + f) * a.nspw + spw) * a.nchan + c) * 4;
+      bool ok = live;
+      if (ok && a.jones) {
+        const long long t = (long long)a.time_ids[row];
+        const unsigned a1 = a.ant1[row], a2 = a.ant2[row];
+        if (t < 0 || t >= a.ntimes || a1 >= (unsigned)a.nant || a2 >= (unsigned)a.nant) {
+          ok = false;
+        } else {
+          i1 = ((((t * a.nant + a1) * a.nfacets + f) * a.nspw + spw) * a.nchan + c) * 4;
+          i2 = ((((t * a.nant + a2) * a.nfacets + f) * a.nspw + spw) * a.nchan + c) * 4;
+        }
+      }
+      if (ok)
+        ok = choose_cells<WPROJ>(um, vm, wm, cc, fx[f], a.faceting != 0, a.faceting != 0, a.u_scale, a.v_scale,
+                                 plane_scale, a.gcx, a.gcy, a.nx, a.ny, W, a.P, a.os, ph, cell);
+      // gather, item by item: D_k = sum over the footprint of g_G conj(tap)
+      cplx myD[4];
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-              Pm[k].re = a.jones[i1 + k].re; Pm[k].im = a.jones[i1 + k].im;
-              Qm[k].re = a.jones[i2 + k].re; Qm[k].im = a.jones[i2 + k].im;
-            }
-            ok = inv2(Pm) && inv2(Qm);
+      for (int k = 0; k < 4; ++k) { myD[k].re = 0; myD[k].im = 0; }
+      unsigned todo = __ballot_sync(0xffffffffu, ok);
+      while (todo) {
+        const int it = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const int u0 = __shfl_sync(0xffffffffu, cell.du, it), v0 = __shfl_sync(0xffffffffu, cell.dv, it);
+        const int plane = __shfl_sync(0xffffffffu, cell.plane, it);
+        const long long fu = (long long)plane * a.K + __shfl_sync(0xffffffffu, cell.fu, it);
+        const long long fv = (long long)plane * a.K + __shfl_sync(0xffffffffu, cell.fv, it);
+        const long long git = __shfl_sync(0xffffffffu, (long long)g, it);
+        const long long slice0 = ((long long)f * a.cube + git) * 4;
+        // lane walks the cells lane, lane + 32, ... of the plane's nonzero window as (ju, jv)
+        // without division
+        const int2 w2 = win[plane];
+        const int ww = w2.y - w2.x + 1;
+        if (ww <= 0) continue;  // an all-zero kernel row: the item's sums stay zero
+        cplx D[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) { D[k].re = 0; D[k].im = 0; }
+        int ju = w2.x + lane % ww, jv = w2.x + lane / ww;
+        const int sju = 32 % ww, sjv = 32 / ww, wend = w2.y + 1;
+        for (; jv < wend; ju += sju, jv += sjv) {
+          if (ju >= wend) {
+            ju -= ww;
+            ++jv;
+            if (jv >= wend) break;
+          }
+          const cplx tap =
+              cmul(tap_at<WPROJ>(a.conv, fu + (long long)ju * a.os), tap_at<WPROJ>(a.conv, fv + (long long)jv * a.os));
+          const cplx ct = cconj(tap);
+          const long long cidx = (long long)(v0 + jv) * a.nx + (u0 + ju);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const vis_complex gg = a.grad_grid[(slice0 + k) * nxy + cidx];
+            cplx gc;
+            gc.re = gg.re;
+            gc.im = gg.im;
+            D[k] = cadd(D[k], cmul(gc, ct));
           }
         }
-        // geometry: the gridder's own cell choice (same cells, taps, plane and phase)
-        if (ok)
-          ok = choose_cells<WPROJ>(um, vm, wm, cc, fx[f], a.faceting != 0, a.faceting != 0, a.u_scale, a.v_scale,
-                                   plane_scale, a.gcx, a.gcy, a.nx, a.ny, W, a.P, a.os, ph, cell) ? 1 : 0;
-      }
-      ok = __shfl_sync(0xffffffffu, ok, 0);
-      if (!ok) continue;
-      const bool flip = cell.flip;
-      const int u0 = __shfl_sync(0xffffffffu, cell.du, 0), v0 = __shfl_sync(0xffffffffu, cell.dv, 0);
-      const int plane = __shfl_sync(0xffffffffu, cell.plane, 0);
-      const long long fu = (long long)plane * a.K + __shfl_sync(0xffffffffu, cell.fu, 0);
-      const long long fv = (long long)plane * a.K + __shfl_sync(0xffffffffu, cell.fv, 0);
-      const long long slice0 = ((long long)f * a.cube + (long long)g) * 4;
-      // gather: D_k = sum over the footprint of g_G conj(tap)
-      cplx D[4];
-#pragma unroll
-      for (int k = 0; k < 4; ++k) { D[k].re = 0; D[k].im = 0; }
-      // lane walks the cells lane, lane + 32, ... of the plane's nonzero window as (ju, jv) without
-      // division
-      const int2 w2 = win[plane];
-      const int ww = w2.y - w2.x + 1;
-      if (ww <= 0) continue;
-      int ju = w2.x + lane % ww, jv = w2.x + lane / ww;
-      const int sju = 32 % ww, sjv = 32 / ww, wend = w2.y + 1;
-      for (; jv < wend; ju += sju, jv += sjv) {
-        if (ju >= wend) {
-          ju -= ww;
-          ++jv;
-          if (jv >= wend) break;
-        }
-        const cplx tap = cmul(tap_at<WPROJ>(a.conv, fu + (long long)ju * a.os), tap_at<WPROJ>(a.conv, fv + (long long)jv * a.os));
-        const cplx ct = cconj(tap);
-        const long long cell = (long long)(v0 + jv) * a.nx + (u0 + ju);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          const vis_complex gg = a.grad_grid[(slice0 + k) * nxy + cell];
-          cplx gc;
-          gc.re = gg.re;
-          gc.im = gg.im;
-          D[k] = cadd(D[k], cmul(gc, ct));
+#pragma unroll
+          for (int off = 16; off > 0; off >>= 1) {
+            D[k].re += __shfl_xor_sync(0xffffffffu, D[k].re, off);
+            D[k].im += __shfl_xor_sync(0xffffffffu, D[k].im, off);
+          }
+        }
+        if (lane == it) {
+#pragma unroll
+          for (int k = 0; k < 4; ++k) myD[k] = D[k];
         }
       }
+      if (!ok) continue;
+      // chain rule back to V (and the Jones terms), each lane for its own item
+      cplx Pm[4], Qm[4];
+      if (a.jones) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          Pm[k].re = a.jones[i1 + k].re; Pm[k].im = a.jones[i1 + k].im;
+          Qm[k].re = a.jones[i2 + k].re; Qm[k].im = a.jones[i2 + k].im;
+        }
+        if (!inv2(Pm) || !inv2(Qm)) continue;  // a singular term: no gradient through it
+      }
+      const bool row_ok = !a.flagged_rows[row] && a.field[row] == a.imaging_field;
+      acc_real cw[4];
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-          D[k].re += __shfl_xor_sync(0xffffffffu, D[k].re, off);
-          D[k].im += __shfl_xor_sync(0xffffffffu, D[k].im, off);
-        }
+        const bool keep = row_ok && !a.flags[base + k];
+        cw[k] = keep ? (acc_real)a.weights[base + k] : (acc_real)0;
       }
-      // chain rule back to V (and the Jones terms), in lane 0
-      if (lane != 0) continue;
       cplx gM[4];
       const cplx cph = cconj(ph);
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
-        const cplx gvp = flip ? cconj(D[k]) : D[k];
+        const cplx gvp = cell.flip ? cconj(myD[k]) : myD[k];
         cplx t = cmul(cph, gvp);
         t.re *= cw[k];
         t.im *= cw[k];
@@ -315,6 +339,12 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
 #pragma unroll
         for (int k = 0; k < 4; ++k) gV[k] = cadd(gV[k], G1[k]);
         if (a.grad_jones) {
+          cplx V[4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            V[k].re = a.vis[base + k].re;
+            V[k].im = a.vis[base + k].im;
+          }
           cplx VQ[4], M[4], gp[4], gq[4];
           mat2(V, false, Qm, true, VQ);  // V Q^H
           mat2(Pm, false, VQ, false, M);  // M = P V Q^H
@@ -335,7 +365,7 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
         for (int k = 0; k < 4; ++k) gV[k] = cadd(gV[k], gM[k]);
       }
     }
-    if (lane == 0) {
+    if (live) {
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         vis_complex o;
@@ -398,7 +428,7 @@ extern "C" int bullseye_grid_adjoint(const gridding_parameters *params, const vo
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const long long warps_needed = a.nrows * a.nchan;
+  const long long warps_needed = (a.nrows * a.nchan + 31) / 32;  // 32 items per warp pass
   const long long blocks = std::min<long long>((warps_needed + 7) / 8, (long long)sms * 16);
   if (p.wplanes > 1) {
     if (smem > 48 * 1024 && cudaFuncSetAttribute(degrid_adjoint_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
