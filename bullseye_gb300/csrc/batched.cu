@@ -221,9 +221,23 @@ struct BatchedState {
   size_t rows_cap = 0, tracks_cap = 0, segs_cap = 0;
   // tuning decisions, by (class width, NC, WPROJ, COMP)
   std::map<std::tuple<int, int, int, int>, std::tuple<int, int, int>> tuned;  // -> (J, wide, regs)
-  // captured graph
-  cudaGraphExec_t exec = nullptr;
-  std::vector<unsigned char> key;
+  // captured graphs, by launch arguments (two slots: the reference's exports alternate between
+  // the visibilities and the sampling function); least recently used is replaced
+  struct GraphSlot {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<unsigned char> key;
+    unsigned long long used = 0;
+  };
+  GraphSlot graphs[2];
+  unsigned long long graph_clock = 0;
+  void drop_graphs() {
+    for (auto &g : graphs) {
+      if (g.exec) cudaGraphExecDestroy(g.exec);
+      g.exec = nullptr;
+      g.key.clear();
+      g.used = 0;
+    }
+  }
   // eager, per-class timed mode (bullseye_set_batched_profiling)
   bool profile = false;
   struct ClassRecord {
@@ -341,10 +355,7 @@ bool ensure_capacity(size_t rows, size_t tracks) {
     if (!b.segs.alloc(maxseg) || !b.sorted.alloc(maxseg)) return false;
     b.segs_cap = maxseg;
   }
-  if (before[0] != b.row_class.ptr || before[1] != b.nseg.ptr || before[2] != b.segs.ptr) {
-    if (b.exec) cudaGraphExecDestroy(b.exec);
-    b.exec = nullptr;
-  }
+  if (before[0] != b.row_class.ptr || before[1] != b.nseg.ptr || before[2] != b.segs.ptr) b.drop_graphs();
   return true;
 }
 
@@ -504,28 +515,33 @@ bool launch_all(const GridArgs &base, int nfacets, bool sampling, cudaStream_t s
   return true;
 }
 
+// vis = false launches (and tunes) only the sampling function's classes; va then only feeds the
+// schedule.
 template <bool WPROJ, bool COMP>
 bool dispatch(const GridArgs &va, const GridArgs *sa, int nfacets, bool tune, const std::vector<int> &counts,
-              cudaStream_t st) {
+              cudaStream_t st, bool vis) {
   if (tune) {
-    if (!tune_all<4, WPROJ, COMP>(va, nfacets, false, counts)) return false;
+    if (vis && !tune_all<4, WPROJ, COMP>(va, nfacets, false, counts)) return false;
     if (sa && !tune_all<1, WPROJ, COMP>(*sa, 1, true, counts)) return false;
     return true;
   }
-  if (!launch_all<4, WPROJ, COMP>(va, nfacets, false, st, &counts)) return false;
+  if (vis && !launch_all<4, WPROJ, COMP>(va, nfacets, false, st, &counts)) return false;
   if (sa && !launch_all<1, WPROJ, COMP>(*sa, 1, true, st, &counts)) return false;
   return true;
 }
 
 bool run_dispatch(const GridArgs &va, const GridArgs *sa, bool wproj, bool comp, bool tune, const std::vector<int> &counts,
-                  cudaStream_t st, int nfacets = -1) {
+                  cudaStream_t st, int nfacets, bool vis) {
   const int F = nfacets > 0 ? nfacets : (int)g_ctx.F;
 #if defined(BULLSEYE_SINGLE)
-  if (comp) return wproj ? dispatch<true, true>(va, sa, F, tune, counts, st) : dispatch<false, true>(va, sa, F, tune, counts, st);
+  if (comp)
+    return wproj ? dispatch<true, true>(va, sa, F, tune, counts, st, vis)
+                 : dispatch<false, true>(va, sa, F, tune, counts, st, vis);
 #else
   (void)comp;
 #endif
-  return wproj ? dispatch<true, false>(va, sa, F, tune, counts, st) : dispatch<false, false>(va, sa, F, tune, counts, st);
+  return wproj ? dispatch<true, false>(va, sa, F, tune, counts, st, vis)
+               : dispatch<false, false>(va, sa, F, tune, counts, st, vis);
 }
 
 // The schedule-building kernels (everything before the per-class launches).
@@ -553,9 +569,7 @@ bool enqueue_schedule(const GridArgs &va, cudaStream_t st) {
 
 void bz_release_batched() {
   BatchedState &b = g_bs;
-  if (b.exec) cudaGraphExecDestroy(b.exec);
-  b.exec = nullptr;
-  b.key.clear();
+  b.drop_graphs();
   b.plane_class.release(); b.plane_lo.release(); b.row_class.release(); b.nseg.release(); b.seg_off.release();
   b.seg_total.release(); b.class_count.release(); b.class_off.release(); b.class_cursor.release();
   b.work_next.release(); b.sample_count.release(); b.segs.release(); b.sorted.release(); b.facet_table.release();
@@ -623,9 +637,10 @@ namespace {
 // Runs one batched call: builds the schedule on the device, on first use tunes every support class
 // (tuning launches use `ta` over `tune_facets` facets and grid into the library's scratch grid),
 // then replays the call as a CUDA graph keyed on the launch arguments; eager with per-class events
-// in profiling mode.
+// in profiling mode.  vis = false grids only the sampling function (sa), with va feeding the
+// schedule.
 int run_batched(const GridArgs &va, const GridArgs *sa, int nfacets, const GridArgs &ta, int tune_facets, bool wproj,
-                bool comp, const char *name) {
+                bool comp, const char *name, bool vis = true) {
   Context &c = g_ctx;
   BatchedState &b = g_bs;
   const bool sf = sa != nullptr;
@@ -635,6 +650,7 @@ int run_batched(const GridArgs &va, const GridArgs *sa, int nfacets, const GridA
   if (sf) std::memcpy(key.data() + sizeof(GridArgs), sa, sizeof(GridArgs));
   key[sizeof(GridArgs) * 2] = (unsigned char)sf;
   key[sizeof(GridArgs) * 2 + 1] = (unsigned char)comp;
+  key[sizeof(GridArgs) * 2 + 2] = (unsigned char)vis;
   std::memcpy(key.data() + sizeof(GridArgs) * 2 + 4, &nfacets, sizeof(int));
 
   auto schedule_counts = [&](std::vector<int> &counts) -> bool {
@@ -647,38 +663,48 @@ int run_batched(const GridArgs &va, const GridArgs *sa, int nfacets, const GridA
   if (b.profile) {
     std::vector<int> counts(kMaxClasses, 0);
     if (!schedule_counts(counts)) return bz_error_code() ? bz_error_code() : BZ_ERR_CUDA;
-    if (!run_dispatch(ta, sa, wproj, comp, true, counts, c.stream, tune_facets)) return bz_error_code();
+    if (!run_dispatch(ta, sa, wproj, comp, true, counts, c.stream, tune_facets, vis)) return bz_error_code();
     b.records.clear();
-    if (!run_dispatch(va, sa, wproj, comp, false, counts, c.stream, nfacets)) return bz_error_code();
+    if (!run_dispatch(va, sa, wproj, comp, false, counts, c.stream, nfacets, vis)) return bz_error_code();
     return BZ_OK;
   }
-  if (!b.exec || key != b.key) {
+  BatchedState::GraphSlot *slot = nullptr;
+  for (auto &g : b.graphs)
+    if (g.exec && g.key == key) slot = &g;
+  if (!slot) {
     // first run of this configuration: build the schedule eagerly, tune each class, then capture
+    // into the least recently used slot
+    slot = &b.graphs[0];
+    for (auto &g : b.graphs)
+      if (g.used < slot->used) slot = &g;
     std::vector<int> counts(kMaxClasses, 0);
     if (!schedule_counts(counts)) return bz_error_code() ? bz_error_code() : BZ_ERR_CUDA;
-    if (!run_dispatch(ta, sa, wproj, comp, true, counts, c.stream, tune_facets)) return bz_error_code();
-    if (b.exec) cudaGraphExecDestroy(b.exec);
-    b.exec = nullptr;
+    if (!run_dispatch(ta, sa, wproj, comp, true, counts, c.stream, tune_facets, vis)) return bz_error_code();
+    if (slot->exec) cudaGraphExecDestroy(slot->exec);
+    slot->exec = nullptr;
+    slot->key.clear();
     cudaGraph_t graph;
     BZ_CUDA_TRY_RET(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal), BZ_ERR_CUDA);
     const long long launches0 = c.launches;
-    bool ok = enqueue_schedule(va, c.stream) && run_dispatch(va, sa, wproj, comp, false, counts, c.stream, nfacets);
+    bool ok = enqueue_schedule(va, c.stream) && run_dispatch(va, sa, wproj, comp, false, counts, c.stream, nfacets, vis);
     cudaError_t ce = cudaStreamEndCapture(c.stream, &graph);
     if (!ok || ce != cudaSuccess) {
       bz_record_error(BZ_ERR_CUDA, "%s: graph capture failed (%s)", name, cudaGetErrorString(ce));
       return BZ_ERR_CUDA;
     }
     c.launches = launches0;  // counted again when the graph is launched
-    ce = cudaGraphInstantiate(&b.exec, graph, 0);
+    ce = cudaGraphInstantiate(&slot->exec, graph, 0);
     cudaGraphDestroy(graph);
     if (ce != cudaSuccess) {
+      slot->exec = nullptr;
       bz_record_error(BZ_ERR_CUDA, "%s: graph instantiation failed (%s)", name, cudaGetErrorString(ce));
       return BZ_ERR_CUDA;
     }
-    b.key = key;
+    slot->key = key;
   }
-  BZ_CUDA_TRY_RET(cudaGraphLaunch(b.exec, c.stream), BZ_ERR_CUDA);
-  c.launches += 6 + (long long)b.ncls * (sf ? 2 : 1);
+  slot->used = ++b.graph_clock;
+  BZ_CUDA_TRY_RET(cudaGraphLaunch(slot->exec, c.stream), BZ_ERR_CUDA);
+  c.launches += 6 + (long long)b.ncls * ((vis ? 1 : 0) + (sf ? 1 : 0));
   return BZ_OK;
 }
 
@@ -694,6 +720,27 @@ bool call_mode(int call, int &mode, bool &faceting, const char *name) {
 }
 
 }  // namespace
+
+// The batched gridder behind the reference's 4-correlation and sampling-function exports (one
+// kind of grid per call; the two graph slots keep both captured).
+bool bz_grid_batched_call(gridding_parameters &p, int mode, bool faceting, const char *name) {
+  Context &c = g_ctx;
+  BatchedState &b = g_bs;
+  const bool sampling = mode == CORR_SAMPLING;
+  GridArgs a;
+  int nslots = 0;
+  if (!bz_prepare_grid_args(p, sampling ? 1 : 4, mode, faceting, a, nslots, name)) return false;
+  if (p.row_count == 0) return true;
+  if (!b.planned && !plan_classes()) {
+    if (!bz_error_code()) bz_record_error(BZ_ERR_CUDA, "%s: support-class planning failed", name);
+    return false;
+  }
+  if (!ensure_capacity(p.row_count, (size_t)nslots * c.nchan)) return false;
+  const bool wproj = p.wplanes > 1, comp = a.grid_lo != nullptr;
+  const int rc = sampling ? run_batched(a, &a, 1, a, 1, wproj, comp, name, false)
+                          : run_batched(a, nullptr, (int)c.F, a, (int)c.F, wproj, comp, name, true);
+  return rc == BZ_OK;
+}
 
 // See include/bullseye_gb300.h.
 extern "C" int bullseye_grid_batched(gridding_parameters *pp, int call, int with_sampling) {

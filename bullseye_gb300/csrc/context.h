@@ -46,6 +46,7 @@ struct Context {
   double grid_seconds = 0.0, inv_seconds = 0.0;
   bool compensated = true;  // FP32: compensated (hi/lo) grid accumulation
   bool device_inputs = false;  // row arrays, Jones terms and baseline starts are device pointers
+  bool batched_calls = true;   // 4-correlation and sampling-function exports run the batched gridder
   long long launches = 0;      // kernels launched by this library since initLibrary
   cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;  // around the last gridder launch
   bool kernel_timing_pending = false;
@@ -102,6 +103,10 @@ void bz_copy_back_grids(gridding_parameters &p, bool sampling);
 FacetXform bz_facet_xform(double ra0, double dec0, double ra, double dec, bool phase, bool uvx);
 void bz_timer_start();
 void bz_timer_stop();
+// The batched (support-aware, persistent per-class) gridder behind one reference export: grids
+// the visibilities (mode != CORR_SAMPLING, 4 correlations) or the sampling function; false on
+// error (recorded).
+bool bz_grid_batched_call(gridding_parameters &p, int mode, bool faceting, const char *name);
 // upload = false reuses the rows a preceding prepare of the same call already uploaded.
 bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool faceting, GridArgs &a,
                           int &nslots, const char *name, bool upload = true);

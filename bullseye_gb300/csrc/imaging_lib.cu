@@ -122,6 +122,9 @@ extern "C" int bullseye_precision_bits() { return BZ_PRECISION_BITS; }
 
 extern "C" void bullseye_set_compensated(int on) { g_ctx.compensated = on != 0; }
 
+// See include/bullseye_gb300.h.
+extern "C" void bullseye_set_batched_calls(int on) { g_ctx.batched_calls = on != 0; }
+
 // Device-resident inputs: when on, the row arrays (visibilities, weights, flags, uvw, flagged
 // rows, field, spw, antenna and timestamp ids), jones_terms and baseline_starting_indexes in
 // gridding_parameters are device pointers already in baseline-major order; the gridding calls
@@ -580,7 +583,9 @@ static bool ensure_row_buffers() {
          c.time_ids.alloc(R) && c.starts.alloc(c.baselines + 2);
 }
 
-static bool upload_rows(const gridding_parameters &p, bool need_ants, bool need_time) {
+// need_vis = false (the sampling function) leaves out the visibilities, weights and flags, which
+// that gridding does not read.
+static bool upload_rows(const gridding_parameters &p, bool need_ants, bool need_time, bool need_vis = true) {
   Context &c = g_ctx;
   const size_t R = p.row_count;
   if (c.device_inputs) return true;
@@ -592,9 +597,12 @@ static bool upload_rows(const gridding_parameters &p, bool need_ants, bool need_
   if (R == 0) return true;
   const size_t RC = R * c.nchan * c.npol;
   cudaStream_t s = c.stream;
-  BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.vis.ptr, p.visibilities, sizeof(vis_complex) * RC, cudaMemcpyHostToDevice, s), false);
-  BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.weights.ptr, p.visibility_weights, sizeof(vis_real) * RC, cudaMemcpyHostToDevice, s), false);
-  BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.flags.ptr, p.flags, RC, cudaMemcpyHostToDevice, s), false);
+  if (need_vis) {
+    BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.vis.ptr, p.visibilities, sizeof(vis_complex) * RC, cudaMemcpyHostToDevice, s), false);
+    BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.weights.ptr, p.visibility_weights, sizeof(vis_real) * RC, cudaMemcpyHostToDevice, s),
+                    false);
+    BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.flags.ptr, p.flags, RC, cudaMemcpyHostToDevice, s), false);
+  }
   BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.uvw.ptr, p.uvw_coords, sizeof(vis_real) * 3 * R, cudaMemcpyHostToDevice, s), false);
   BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.flagged_rows.ptr, p.flagged_rows, R, cudaMemcpyHostToDevice, s), false);
   BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.field.ptr, p.field_array, sizeof(unsigned) * R, cudaMemcpyHostToDevice, s), false);
@@ -695,7 +703,7 @@ bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool f
     return false;
   }
   const bool jones = mode == CORR_QUAD_JONES;
-  if (upload && !upload_rows(p, jones, jones)) return false;
+  if (upload && !upload_rows(p, jones, jones, !sampling)) return false;
   if (jones) {
     const size_t nj = p.no_timestamps_read * p.antenna_count * c.F * c.nspw * c.nchan;
     if (!p.jones_terms || nj == 0) {
@@ -797,6 +805,19 @@ static void grid_common(gridding_parameters *pp, int nc, int mode, bool faceting
   Context &c = g_ctx;
   const bool sampling = mode == CORR_SAMPLING;
   timer_start();
+  if (c.batched_calls && c.C == 4 && (sampling || nc == 4)) {
+    // the support-aware batched gridder (same results; see batched.cu)
+    settle_kernel_timing();
+    cudaEventRecord(c.ev_k0, c.stream);
+    if (!bz_grid_batched_call(p, mode, faceting, name)) return;
+    cudaEventRecord(c.ev_k1, c.stream);
+    c.kernel_timing_pending = true;
+    c.kernel_timing_kind = sampling ? 1 : 0;
+    c.kernel_count[c.kernel_timing_kind]++;
+    if (p.is_final_data_chunk) copy_back_grids(p, sampling);
+    timer_stop();
+    return;
+  }
   GridArgs a;
   int nslots = 0;
   if (!bz_prepare_grid_args(p, nc, mode, faceting, a, nslots, name)) return;

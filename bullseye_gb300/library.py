@@ -52,6 +52,7 @@ EXTENSIONS = {
     "bullseye_batched_profile": (ctypes.c_int, [ctypes.c_void_p] * 6 + [ctypes.c_int]),
     "bullseye_batched_plane_classes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "bullseye_selftest_bounded_wait": (ctypes.c_int, []),
+    "bullseye_set_batched_calls": (None, [ctypes.c_int]),
     "bullseye_grid_batched_facets": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     "bullseye_facet_4_cor_corrections_ws_bytes": (ctypes.c_size_t, [ctypes.c_void_p]),

@@ -147,6 +147,13 @@ int bullseye_batched_profile(int *width, int *nc, int *J, int *wide, int *items,
  * rounded up to a class width), up to max planes; returns the plane count (0 before the first
  * batched call after initLibrary). */
 int bullseye_batched_plane_classes(int *width, int max);
+/* The reference's 4-correlation gridding exports (grid_4_cor, facet_4_cor,
+ * facet_4_cor_corrections) and sampling-function exports run the batched, support-aware gridder
+ * (the same grids: each w plane's taps outside its nonzero window are exactly zero) when this is
+ * on (the default, when the library is initialised for 4 correlations); off selects the plain
+ * per-track kernels, which grid the full padded support.  Single and dual polarisation calls
+ * always use the plain kernels. */
+void bullseye_set_batched_calls(int on);
 /* Self-test of the batched gridder's bounded waits: runs one CTA whose tap-copy barrier never
  * completes and returns the device error bits it recorded (16 = the wait ran out, as expected),
  * or -1 on a CUDA error.  Takes about 0.2 s; touches no library state. */

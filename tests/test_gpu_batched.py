@@ -89,7 +89,11 @@ def test_batched_wproj_fp32_within_1e5(chunks, libs, oracles):
 def test_batched_aa_matches_per_call(libs):
     from bullseye_gb300.library import check
     p = synth.small_problem("single", nx=96, n_ant=8, n_times=10, n_chan=2, s=3, os=63)
-    per_call = run_imaging(libs["single"], p, "grid_4_cor", repack=True, keep_raw=True, psf=True, norm_bins=49)
+    libs["single"].bullseye_set_batched_calls(0)  # the plain per-track kernels as the reference
+    try:
+        per_call = run_imaging(libs["single"], p, "grid_4_cor", repack=True, keep_raw=True, psf=True, norm_bins=49)
+    finally:
+        libs["single"].bullseye_set_batched_calls(1)
     check(libs["single"])
     res = _run(libs["single"], p, "grid_4_cor")
     assert rel(res.raw_grid, per_call.raw_grid) <= 1e-6

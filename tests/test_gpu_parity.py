@@ -41,6 +41,17 @@ def oracle_libs(oracle_built):
     return {p: load_oracle(p) for p in PRECISIONS}
 
 
+@pytest.fixture(params=["batched", "plain"])
+def form(request, gpu_libs):
+    """The 4-correlation and sampling-function exports through the batched, support-aware gridder
+    (the default) or the plain per-track kernels."""
+    for lib in gpu_libs.values():
+        lib.bullseye_set_batched_calls(1 if request.param == "batched" else 0)
+    yield request.param
+    for lib in gpu_libs.values():
+        lib.bullseye_set_batched_calls(1)
+
+
 def run_gpu(lib, p, call, **kw):
     from bullseye_gb300.library import check
     res = run_imaging(lib, p, call, repack=True, norm_bins=(2 * p.conv_support + 1) ** 2, **kw)
@@ -49,7 +60,7 @@ def run_gpu(lib, p, call, **kw):
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
-def test_fp64_matches_reference_fixture(name, gpu_libs):
+def test_fp64_matches_reference_fixture(name, gpu_libs, form):
     """GPU FP64 vs the reference CPU library's own outputs (golden fixtures)."""
     call, _, rkw = CASES[name]
     p, out = load_case(name, "double")
@@ -73,7 +84,7 @@ def test_fp64_matches_reference_fixture(name, gpu_libs):
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
-def test_fp32_within_1e5_of_fp64(name, gpu_libs, oracle_libs):
+def test_fp32_within_1e5_of_fp64(name, gpu_libs, oracle_libs, form):
     """GPU FP32 vs the FP64 oracle run on the same (float) inputs."""
     call, _, rkw = CASES[name]
     p32, _ = load_case(name, "single")
