@@ -167,6 +167,11 @@ using SegKernel = void (*)(const GridArgs, const int);
 template <int NC, bool WPROJ, bool COMP, bool WIDE>
 SegKernel<NC, WPROJ, COMP> seg_kernel_of(int J, int regs) {
   if (J == 8) return romein_segment_kernel<NC, WPROJ, 8, COMP, WIDE>;
+#if defined(BULLSEYE_SINGLE)
+  if constexpr (NC == 4 && WPROJ) {
+    if (J == 6) return romein_segment_kernel<NC, WPROJ, 6, COMP, WIDE, kSegRegs6>;
+  }
+#endif
   if constexpr (NC == 4 && WPROJ) {
     if (regs == 64) return romein_segment_kernel<NC, WPROJ, 4, COMP, WIDE, 64>;
     if (regs == 72) return romein_segment_kernel<NC, WPROJ, 4, COMP, WIDE, 72>;
@@ -183,6 +188,7 @@ SegKernel<NC, WPROJ, COMP> seg_kernel(int J, bool wide, int regs) {
 template <int NC, bool WPROJ>
 std::vector<int> reg_caps(int J) {
   if (J == 8) return {kSegRegs<8>};
+  if (J == 6) return {kSegRegs6};
   if (NC == 4 && WPROJ) return {kSegRegs<4>, 72, 64};
   return {kSegRegs<4>};
 }
@@ -421,9 +427,13 @@ bool tune_class(const GridArgs &base, int k, int nfacets, Variant &out, int host
   auto key = std::make_tuple(W, NC, (int)WPROJ, (int)COMP);
   auto it = b.tuned.find(key);
   std::vector<Variant> cands;
-  for (int J : {8, 4})
+  // J = 6 (single precision, four correlations, w-projection): 48 accumulator registers, the
+  // column tap shared by 6 rows
+  const bool six = BZ_PRECISION_BITS == 32 && NC == 4 && WPROJ;
+  for (int J : {8, 6, 4})
     for (bool wide : {true, false})
       for (int regs : reg_caps<NC, WPROJ>(J)) {
+        if (J == 6 && !six) continue;
         Variant v;
         if (make_variant<NC, WPROJ>(W, J, wide, regs, v) && finish_variant<NC, WPROJ, COMP>(v)) cands.push_back(v);
       }

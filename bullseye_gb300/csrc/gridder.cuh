@@ -1157,6 +1157,8 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
 // 72 registers to the tuner (different support classes prefer different caps).
 template <int J>
 constexpr int kSegRegs = J == 4 ? 80 : 128;
+// the J = 6 layout of the single-precision w-projection visibility launches
+constexpr int kSegRegs6 = 96;
 
 // One CTA per track: blockIdx -> (facet, baseline slot or row segment, channel).
 template <int NC, bool WPROJ, int J, bool COMP, bool WIDE>
