@@ -17,8 +17,10 @@
 // Per-visibility work (the prologue) is done once per CTA, not once per thread: V threads each
 // prepare one visibility (correlation selection, weights x flags, Jones J_p^-1 V J_q^-H, facet
 // phase rotation, planar uv transform, cell and tap-offset selection) into shared memory, the
-// CTA then gathers the 2W taps of each staged visibility from the kernel table, and all
-// threads grid the staged chunk.
+// CTA then stages the 2W + J - 1 taps of each staged visibility (in the persistent batched
+// kernel: two TMA bulk copies per visibility from the support-window table, completed on an
+// mbarrier; otherwise per-tap asynchronous copies from the ABI's table), and all threads grid
+// the staged chunk.
 //
 // Numerics (matching the reference CPU library, bullseye/mo/cpu_algorithm/*):
 //  * uvw / lambda, the phase argument 2 pi (u dl + v dm + w dn), the uv transform and the
@@ -28,11 +30,13 @@
 //  * tap index = trunc((1 - u + round(u)) * os) + j*os; a visibility is dropped when
 //    disc + W + 2 >= n or disc < 0 (convolution_policies.h:86-97);
 //  * single-precision library: visibilities, taps and the register accumulation are FP32,
-//    the phase is evaluated by sincosf on the FP64-reduced argument; grid flushes can be
-//    compensated (hi/lo pair, TwoSum on the value returned by the atomic);
-//  * normalisation: sum over taps of the real tap weight times weight x flag, in FP64
+//    the phase is evaluated by sincospif on the argument reduced in FP64 to turns; grid
+//    flushes can be compensated (hi/lo pair, TwoSum on the value returned by the atomic);
+//  * normalisation: sum over taps of the real tap weight times weight x flag
 //    (templated_gridder.h:97 and store_normalization_term), computed per visibility as
-//    Re(sum_j k_u[j] * sum_i k_v[i]).
+//    Re(sum_j k_u[j] * sum_i k_v[i]) from kernel row sums precomputed in FP64, accumulated per
+//    staging slot (FP32 with Kahan compensation in the single library, FP64 in the double one)
+//    and reduced per warp into FP64.
 #pragma once
 #include <algorithm>
 #include <type_traits>
