@@ -260,15 +260,21 @@ BatchedState g_bs;
 // [floor(os/2), floor(3 os/2)] with round-to-nearest (w-projection) and [0, os] with floor (AA);
 // the window keeps every s that can reach a nonzero sample for some fu in that range, so the
 // taps left out are exactly zero.  Only the class widths some plane uses get a launch.
+// Candidate class widths for full support W, ascending; the last is W itself.
+std::vector<int> class_candidates(int W) {
+  std::vector<int> cand;
+  for (int w : {16, 18, 20, 22, 24, 28, 32, 36, 40, 44, 48, 56})
+    if (w < W) cand.push_back(w);
+  cand.push_back(W);
+  return cand;
+}
+
 bool plan_classes() {
   Context &c = g_ctx;
   BatchedState &b = g_bs;
   const int W = (int)c.W, os = (int)c.os, K = (int)c.K, P = (int)c.P;
   const bool wproj = c.P > 1;
-  std::vector<int> cand;
-  for (int w : {16, 18, 20, 22, 24, 28, 32, 36, 40, 44, 48, 56})
-    if (w < W) cand.push_back(w);
-  cand.push_back(W);
+  const std::vector<int> cand = class_candidates(W);
   const int fu_min = wproj ? (int)std::floor(0.5 * os - 1e-6) : 0;
   const int fu_max = wproj ? (int)std::floor(1.5 * os + 1e-6) : os;
   std::vector<int> pw(P), plo(P);
@@ -866,4 +872,245 @@ extern "C" int bullseye_grid_batched_facets(gridding_parameters *pp, const bulls
   if (rc != BZ_OK) return rc;
   bz_timer_stop();
   return bz_error_code();
+}
+
+// ---------------------------------------------------------------- support-aware workspace form
+// The batched gridder without library state, for the allocation-free workspace entry: the
+// per-plane windows, the support-window table and the run schedule are built on the device in the
+// caller's workspace from the call's own (device) tables, and every candidate class width gets
+// one persistent launch (a class no plane uses finds no work items).  The layout of a class is
+// the tuner's choice when the library has tuned that width, else J = 4 (J = 8 where the
+// J = 4 layout needs more than 512 threads).
+
+namespace {
+
+struct ClassList {
+  int n;
+  int w[kMaxClasses];
+};
+
+// One warp per w plane: the plane's nonzero window, its class and window start (the same rule as
+// plan_classes, evaluated on the device).
+__global__ void plane_window_kernel(const void *conv, int P, int K, int W, int os, int wproj, ClassList cl,
+                                    int *plane_class, int *plane_lo, int *plane_w) {
+  const int lane = threadIdx.x & 31;
+  const int pl = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (pl >= P) return;  // whole warps
+  int lo = 0x7fffffff, hi = -1;
+  for (int i = lane; i < K; i += 32) {
+    bool nz;
+    if (wproj) {
+      const vis_complex t = ((const vis_complex *)conv)[(long long)pl * K + i];
+      nz = t.re != (vis_real)0 || t.im != (vis_real)0;
+    } else {
+      nz = ((const vis_real *)conv)[i] != (vis_real)0;
+    }
+    if (nz) {
+      lo = min(lo, i);
+      hi = max(hi, i);
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, off));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, off));
+  }
+  if (lane != 0) return;
+  const int fu_min = wproj ? (int)floor(0.5 * os - 1e-6) : 0;
+  const int fu_max = wproj ? (int)floor(1.5 * os + 1e-6) : os;
+  int slo = 0, shi = 0;
+  if (hi >= 0) {
+    slo = max(0, (int)ceil((double)(lo - fu_max) / os));
+    shi = min(W - 1, (int)floor((double)(hi - fu_min) / os));
+    if (shi < slo) shi = slo;
+  }
+  const int width = shi - slo + 1;
+  int k = cl.n - 1;
+  for (int i = 0; i < cl.n; ++i)
+    if (cl.w[i] >= width) {
+      k = i;
+      break;
+    }
+  plane_class[pl] = k;
+  plane_w[pl] = cl.w[k];
+  plane_lo[pl] = min(slo, W - cl.w[k]);
+}
+
+// Support-window table [P][tap_f][L] (real or complex like conv), as plan_classes builds it.
+__global__ void window_table_kernel(const void *conv, int P, int K, int tap_f, int os, int wproj,
+                                    const int *__restrict__ plane_lo, const int *__restrict__ plane_w, int L,
+                                    vis_real *__restrict__ out) {
+  const long long n = (long long)P * tap_f * L;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)(e % L);
+    const long long pf = e / L;
+    const int f = (int)(pf % tap_f), p = (int)(pf / tap_f);
+    const int pw = plane_w[p];
+    const int jj = j < pw ? j : (j < pw + 7 ? j - pw : -1);
+    vis_real re = 0, im = 0;
+    if (jj >= 0) {
+      const long long i = f + (long long)(plane_lo[p] + jj) * os;
+      if (i < K) {
+        if (wproj) {
+          const vis_complex t = ((const vis_complex *)conv)[(long long)p * K + i];
+          re = t.re;
+          im = t.im;
+        } else {
+          re = ((const vis_real *)conv)[i];
+        }
+      }
+    }
+    if (wproj) {
+      out[2 * e] = re;
+      out[2 * e + 1] = im;
+    } else {
+      out[e] = re;
+    }
+  }
+}
+
+// Workspace layout of the support-aware form (every piece 256-byte aligned).
+struct SupportWs {
+  size_t plane_class, plane_lo, plane_w, table, row_class, nseg, seg_off, seg_total, segs, sorted, class_count,
+      class_off, class_cursor, work_next, bytes;
+  int L, tap_f;
+  long long maxseg;
+};
+
+SupportWs support_ws_layout(long long R, int nchan, int nslots, int P, int os, int W, bool wproj) {
+  SupportWs l;
+  const size_t ncomp = wproj ? 2 : 1;
+  const int E = (int)(16 / (ncomp * sizeof(vis_real)));
+  l.L = (W + 7 + E - 1) / E * E;
+  l.tap_f = 2 * os + 1;
+  l.maxseg = std::max<long long>(1, R * nchan);
+  const long long tracks = std::max<long long>(1, (long long)nslots * nchan);
+  size_t off = 0;
+  auto take = [&](size_t n) {
+    const size_t at = off;
+    off += (n + 255) / 256 * 256;
+    return at;
+  };
+  l.plane_class = take(sizeof(int) * P);
+  l.plane_lo = take(sizeof(int) * P);
+  l.plane_w = take(sizeof(int) * P);
+  l.table = take(sizeof(vis_real) * ncomp * (size_t)P * l.tap_f * l.L);
+  l.row_class = take((size_t)std::max<long long>(1, R * nchan));
+  l.nseg = take(sizeof(int) * tracks);
+  l.seg_off = take(sizeof(int) * tracks);
+  l.seg_total = take(sizeof(int));
+  l.segs = take(sizeof(int4) * l.maxseg);
+  l.sorted = take(sizeof(int4) * l.maxseg);
+  l.class_count = take(sizeof(int) * kMaxClasses);
+  l.class_off = take(sizeof(int) * kMaxClasses);
+  l.class_cursor = take(sizeof(int) * kMaxClasses);
+  l.work_next = take(sizeof(int) * kMaxClasses);
+  l.bytes = off;
+  return l;
+}
+
+template <bool WPROJ, bool COMP>
+bool support_aware_launches(const GridArgs &a, const ClassList &cl, int nfacets, int *class_count, int *class_off,
+                            int *work_next, cudaStream_t st) {
+  for (int k = 0; k < cl.n; ++k) {
+    const int W = cl.w[k];
+    Variant v;
+    bool have = false;
+    auto it = g_bs.tuned.find(std::make_tuple(W, 4, (int)WPROJ, (int)COMP));
+    if (it != g_bs.tuned.end())
+      have = make_variant<4, WPROJ>(W, std::get<0>(it->second), std::get<1>(it->second) != 0, std::get<2>(it->second), v) &&
+             finish_variant<4, WPROJ, COMP>(v);
+    for (int J : {4, 8})
+      if (!have) have = make_variant<4, WPROJ>(W, J, false, kSegRegs<4>, v) && finish_variant<4, WPROJ, COMP>(v);
+    if (!have) have = make_variant<4, WPROJ>(W, 8, true, kSegRegs<8>, v) && finish_variant<4, WPROJ, COMP>(v);
+    if (!have) {
+      bz_record_error(BZ_ERR_UNSUPPORTED, "support-aware gridding: no layout for class width %d", W);
+      return false;
+    }
+    GridArgs ak = a;
+    ak.W = W;
+    ak.V = v.V;
+    ak.segment_base = class_off + k;
+    ak.work_count = class_count + k;
+    ak.work_next = work_next + k;
+    auto kern = seg_kernel<4, WPROJ, COMP>(v.J, v.wide, v.regs);
+    if (!open_smem(kern)) {
+      bz_record_error(BZ_ERR_CUDA, "support-aware gridding: cudaFuncSetAttribute failed");
+      return false;
+    }
+    if (cudaMemsetAsync(work_next + k, 0, sizeof(int), st) != cudaSuccess) return false;
+    kern<<<v.grid, v.NT, v.smem, st>>>(ak, nfacets);
+    if (cudaGetLastError() != cudaSuccess) return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+size_t bz_support_aware_ws_bytes(long long rows, int nchan, int nslots, int P, int os, int W, bool wproj) {
+  return support_ws_layout(rows, nchan, nslots, P, os, W, wproj).bytes;
+}
+
+bool bz_grid_support_aware(const GridArgs &a_in, int nfacets, unsigned char *ws, size_t bytes, cudaStream_t st) {
+  const bool wproj = a_in.P > 1;
+  const int W = a_in.W;
+  const SupportWs l = support_ws_layout(a_in.nrows, a_in.nchan, a_in.nslots, a_in.P, a_in.os, W, wproj);
+  if (bytes < l.bytes) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "support-aware gridding: workspace of %zu bytes, need %zu", bytes, l.bytes);
+    return false;
+  }
+  const std::vector<int> cand = class_candidates(W);
+  ClassList cl;
+  cl.n = (int)cand.size();
+  for (int i = 0; i < cl.n; ++i) cl.w[i] = cand[i];
+  int *plane_class = reinterpret_cast<int *>(ws + l.plane_class);
+  int *plane_lo = reinterpret_cast<int *>(ws + l.plane_lo);
+  int *plane_w = reinterpret_cast<int *>(ws + l.plane_w);
+  vis_real *table = reinterpret_cast<vis_real *>(ws + l.table);
+  unsigned char *row_class = ws + l.row_class;
+  int *nseg = reinterpret_cast<int *>(ws + l.nseg);
+  int *seg_off = reinterpret_cast<int *>(ws + l.seg_off);
+  int *seg_total = reinterpret_cast<int *>(ws + l.seg_total);
+  int4 *segs = reinterpret_cast<int4 *>(ws + l.segs);
+  int4 *sorted = reinterpret_cast<int4 *>(ws + l.sorted);
+  int *class_count = reinterpret_cast<int *>(ws + l.class_count);
+  int *class_off = reinterpret_cast<int *>(ws + l.class_off);
+  int *class_cursor = reinterpret_cast<int *>(ws + l.class_cursor);
+  int *work_next = reinterpret_cast<int *>(ws + l.work_next);
+  const int P = a_in.P, K = a_in.K;
+  const long long R = a_in.nrows;
+  const int tracks = a_in.nslots * a_in.nchan;
+  if (cudaMemsetAsync(class_count, 0, sizeof(int) * kMaxClasses, st) != cudaSuccess) return false;
+  plane_window_kernel<<<(unsigned)((P * 32 + 255) / 256), 256, 0, st>>>(a_in.conv, P, K, W, a_in.os, wproj ? 1 : 0, cl,
+                                                                        plane_class, plane_lo, plane_w);
+  window_table_kernel<<<256, 256, 0, st>>>(a_in.conv, P, K, l.tap_f, a_in.os, wproj ? 1 : 0, plane_lo, plane_w, l.L,
+                                           table);
+  classify_kernel<<<1024, 256, 0, st>>>(a_in.uvw, a_in.spw, a_in.wavelengths, a_in.nchan, a_in.nspw, R, a_in.wmax, P,
+                                        plane_class, row_class);
+  seg_count_kernel<<<(tracks + 127) / 128, 128, 0, st>>>(a_in.starts, a_in.nslots, a_in.seg, R, a_in.nchan, row_class,
+                                                         nseg);
+  scan_kernel<<<1, 1024, 0, st>>>(nseg, seg_off, tracks, seg_total);
+  seg_write_kernel<<<(tracks + 127) / 128, 128, 0, st>>>(a_in.starts, a_in.nslots, a_in.seg, R, a_in.nchan, row_class,
+                                                         seg_off, segs, class_count);
+  class_offsets_kernel<<<1, 1, 0, st>>>(class_count, class_off, class_cursor, cl.n);
+  bucket_kernel<<<1024, 256, 0, st>>>(segs, seg_total, sorted, class_cursor, class_off);
+  if (cudaGetLastError() != cudaSuccess) return false;
+  GridArgs a = a_in;
+  a.W_full = W;
+  a.tap_f = l.tap_f;
+  a.plane_lo = plane_lo;
+  a.conv_w = table;
+  a.conv_w_stride = l.L;
+  a.segments = sorted;
+  a.segment_capacity = l.maxseg;
+  const bool comp = a.grid_lo != nullptr;
+#if defined(BULLSEYE_SINGLE)
+  if (comp)
+    return wproj ? support_aware_launches<true, true>(a, cl, nfacets, class_count, class_off, work_next, st)
+                 : support_aware_launches<false, true>(a, cl, nfacets, class_count, class_off, work_next, st);
+#else
+  (void)comp;
+#endif
+  return wproj ? support_aware_launches<true, false>(a, cl, nfacets, class_count, class_off, work_next, st)
+               : support_aware_launches<false, false>(a, cl, nfacets, class_count, class_off, work_next, st);
 }

@@ -107,6 +107,10 @@ void bz_timer_stop();
 // the visibilities (mode != CORR_SAMPLING, 4 correlations) or the sampling function; false on
 // error (recorded).
 bool bz_grid_batched_call(gridding_parameters &p, int mode, bool faceting, const char *name);
+// Support-aware gridding without library state (the workspace entry): bytes of workspace it needs,
+// and the call itself (a: the prepared arguments over the full support; ws: 256-byte aligned).
+size_t bz_support_aware_ws_bytes(long long rows, int nchan, int nslots, int P, int os, int W, bool wproj);
+bool bz_grid_support_aware(const GridArgs &a, int nfacets, unsigned char *ws, size_t bytes, cudaStream_t st);
 // upload = false reuses the rows a preceding prepare of the same call already uploaded.
 bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool faceting, GridArgs &a,
                           int &nslots, const char *name, bool upload = true);

@@ -28,6 +28,10 @@
 #include "common.h"
 #include "gridder.cuh"
 
+// Support-aware form of the batched gridder (batched.cu), used by the workspace entry.
+size_t bz_support_aware_ws_bytes(long long rows, int nchan, int nslots, int P, int os, int W, bool wproj);
+bool bz_grid_support_aware(const bz::GridArgs &a, int nfacets, unsigned char *ws, size_t bytes, cudaStream_t st);
+
 using namespace bz;
 
 #define BZ_NOALLOC_LO_BYTES (40u << 20)
@@ -173,6 +177,8 @@ struct Workspace {
   FacetXform *table;
   size_t table_bytes;
   int *err;
+  unsigned char *sched = nullptr;  // support-aware schedule and tables (workspace entry), or null
+  size_t sched_bytes = 0;
 };
 
 int grid_4cor_jones(const gridding_parameters &p, const Workspace &ws, void *stream) {
@@ -265,7 +271,12 @@ int grid_4cor_jones(const gridding_parameters &p, const Workspace &ws, void *str
   a.wmax = (double)(float)p.wmax_est;
   const long long blocks = (long long)F * a.nslots * (long long)a.nchan;
   if (blocks > 0x7fffffffLL) return BZ_ERR_UNSUPPORTED;
-  if (!(wproj ? noalloc_dispatch<true>(a, blocks, st) : noalloc_dispatch<false>(a, blocks, st))) return BZ_ERR_CUDA;
+  if (ws.sched) {
+    // workspace entry: support-aware (each w plane's nonzero window only; the same grids)
+    if (!bz_grid_support_aware(a, (int)F, ws.sched, ws.sched_bytes, st)) return bz_error_code() ? bz_error_code() : BZ_ERR_CUDA;
+  } else if (!(wproj ? noalloc_dispatch<true>(a, blocks, st) : noalloc_dispatch<false>(a, blocks, st))) {
+    return BZ_ERR_CUDA;
+  }
 #if defined(BULLSEYE_SINGLE)
   noalloc_fold_kernel<<<1024, 256, 0, st>>>(p.output_buffer, lo, (long long)grid_elems);
   if (cudaGetLastError() != cudaSuccess) return BZ_ERR_CUDA;
@@ -316,10 +327,17 @@ static size_t ws_table_bytes(const gridding_parameters &p) {
   return (F * sizeof(FacetXform) + 255) / 256 * 256;
 }
 
+static size_t ws_sched_bytes(const gridding_parameters &p) {
+  const int nslots = p.baseline_starting_indexes ? (int)p.baseline_count : (int)((p.row_count + 255) / 256);
+  return bz_support_aware_ws_bytes((long long)p.row_count, (int)p.channel_count, nslots,
+                                   (int)(p.wplanes > 1 ? p.wplanes : 1), (int)p.conv_oversample,
+                                   (int)(2 * p.conv_support + 1), p.wplanes > 1);
+}
+
 // See include/bullseye_gb300.h.
 extern "C" size_t bullseye_facet_4_cor_corrections_ws_bytes(const gridding_parameters *params) {
   if (!params) return 0;
-  return ws_lo_bytes(*params) + ws_table_bytes(*params) + 256;
+  return ws_lo_bytes(*params) + ws_table_bytes(*params) + 256 + ws_sched_bytes(*params);
 }
 
 // See include/bullseye_gb300.h.
@@ -341,6 +359,8 @@ extern "C" int bullseye_facet_4_cor_corrections_ws(const gridding_parameters *pa
   ws.table = reinterpret_cast<FacetXform *>(w + ws.lo_bytes);
   ws.table_bytes = ws_table_bytes(p);
   ws.err = reinterpret_cast<int *>(w + ws.lo_bytes + ws.table_bytes);
+  ws.sched = w + ws.lo_bytes + ws.table_bytes + 256;
+  ws.sched_bytes = ws_sched_bytes(p);
   return grid_4cor_jones(p, ws, stream);
 }
 

@@ -100,6 +100,42 @@ def test_noalloc_matches_regular_entry_point_on_two_calls(gpu_required, built_li
         assert _rel(norm, ref.normalization) <= TOL, f"call {call}: norm rel err {_rel(norm, ref.normalization):.2e}"
 
 
+def test_workspace_entry_is_support_aware_and_matches_full_support(gpu_required, built_libraries):
+    """bullseye_facet_4_cor_corrections_ws grids each w plane's nonzero window only, with the support
+    windows, the window table and the run schedule built in the caller's workspace.  Its grids and
+    normalisation must match the plain kernels over the full padded support (31 taps, planes of 11 to
+    31), on two calls in a row."""
+    import torch
+    from bullseye_gb300.library import check, load_library
+    torch.cuda.set_device(0)
+    lib = load_library("GPU", "single")
+    p = synth.small_problem("single", nx=128, n_ant=7, n_times=10, n_chan=3, n_facets=2, jones=True, s=15, os=5,
+                            wplanes=8, min_support=5)
+    lib.bullseye_set_batched_calls(0)
+    try:
+        ref = run_imaging(lib, p, "facet_4_cor_corrections", repack=True, keep_raw=True,
+                          norm_bins=(2 * p.conv_support + 1) ** 2)
+    finally:
+        lib.bullseye_set_batched_calls(1)
+    check(lib)
+    keep = []
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for call in range(2):
+        st, arrs = _device_struct(p, torch, keep)  # fresh Jones each call: the entry inverts them in place
+        nbytes = int(lib.bullseye_facet_4_cor_corrections_ws_bytes(ctypes.byref(st)))
+        ws = torch.empty(nbytes + 256, dtype=torch.uint8, device="cuda")
+        base = (ws.data_ptr() + 255) // 256 * 256
+        rc = lib.bullseye_facet_4_cor_corrections_ws(ctypes.byref(st), ctypes.c_void_p(base), nbytes, stream)
+        assert rc == 0, f"call {call}: status {rc}"
+        torch.cuda.synchronize()
+        check(lib)
+        grid = arrs["grid"].cpu().numpy()
+        norm = arrs["norm"].cpu().numpy().reshape(ref.normalization.shape)
+        assert np.max(np.abs(ref.raw_grid)) > 0
+        assert _rel(grid, ref.raw_grid) <= TOL, f"call {call}: grid rel err {_rel(grid, ref.raw_grid):.2e}"
+        assert _rel(norm, ref.normalization) <= TOL, f"call {call}: norm rel err {_rel(norm, ref.normalization):.2e}"
+
+
 def test_noalloc_rejects_grids_beyond_the_scratch(gpu_required, built_libraries):
     import torch
     from bullseye_gb300.library import ImagingError, check, load_library
