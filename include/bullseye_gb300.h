@@ -179,10 +179,13 @@ int bullseye_facet_4_cor_corrections_noalloc(const gridding_parameters *params, 
 
 /* The same gridding on device pointers with a CALLER-PROVIDED device workspace instead of the fixed
  * scratch array, so grids of any size are accepted and concurrent calls with their own workspaces
- * do not share state.  The workspace must be 256-byte aligned and at least
- * bullseye_facet_4_cor_corrections_ws_bytes(params) bytes (the 32-bit library's compensation grid,
- * the facet table and an error word); its contents need not be initialised.  jones_terms is
- * inverted in place.  No counterpart in the reference. */
+ * do not share state.  It is support-aware: each w plane's nonzero kernel window is found on the
+ * device and the visibilities are gridded by persistent per-support-class launches over a run
+ * schedule built in the workspace (the same grids as the full padded support).  The workspace must
+ * be 256-byte aligned and at least bullseye_facet_4_cor_corrections_ws_bytes(params) bytes (the
+ * 32-bit library's compensation grid, the facet table, an error word, and the support windows,
+ * window table and run schedule: about 33 bytes per (row, channel)); its contents need not be
+ * initialised.  jones_terms is inverted in place.  No counterpart in the reference. */
 size_t bullseye_facet_4_cor_corrections_ws_bytes(const gridding_parameters *params);
 int bullseye_facet_4_cor_corrections_ws(const gridding_parameters *params, void *workspace, size_t bytes,
                                         void *stream);
