@@ -719,6 +719,7 @@ int run_batched(const GridArgs &va, const GridArgs *sa, int nfacets, const GridA
     slot->key = key;
   }
   slot->used = ++b.graph_clock;
+  bz_trace_mark("schedule_tune_capture");
   BZ_CUDA_TRY_RET(cudaGraphLaunch(slot->exec, c.stream), BZ_ERR_CUDA);
   c.launches += 6 + (long long)b.ncls * ((vis ? 1 : 0) + (sf ? 1 : 0));
   return BZ_OK;
@@ -746,6 +747,7 @@ bool bz_grid_batched_call(gridding_parameters &p, int mode, bool faceting, const
   GridArgs a;
   int nslots = 0;
   if (!bz_prepare_grid_args(p, sampling ? 1 : 4, mode, faceting, a, nslots, name)) return false;
+  bz_trace_mark(sampling ? "sf.upload_prepare" : "vis.upload_prepare");
   if (p.row_count == 0) return true;
   if (!b.planned && !plan_classes()) {
     if (!bz_error_code()) bz_record_error(BZ_ERR_CUDA, "%s: support-class planning failed", name);
@@ -755,6 +757,7 @@ bool bz_grid_batched_call(gridding_parameters &p, int mode, bool faceting, const
   const bool wproj = p.wplanes > 1, comp = a.grid_lo != nullptr;
   const int rc = sampling ? run_batched(a, &a, 1, a, 1, wproj, comp, name, false)
                           : run_batched(a, nullptr, (int)c.F, a, (int)c.F, wproj, comp, name, true);
+  bz_trace_mark(sampling ? "sf.grid" : "vis.grid");
   return rc == BZ_OK;
 }
 

@@ -107,6 +107,10 @@ void bz_timer_stop();
 // the visibilities (mode != CORR_SAMPLING, 4 correlations) or the sampling function; false on
 // error (recorded).
 bool bz_grid_batched_call(gridding_parameters &p, int mode, bool faceting, const char *name);
+// Phase tracing (bullseye_set_tracing): when on, bz_trace_begin() and bz_trace_mark() synchronise
+// the library stream and record the host time of each phase of a call; off, they do nothing.
+void bz_trace_begin();
+void bz_trace_mark(const char *phase);
 // Support-aware gridding without library state (the workspace entry): bytes of workspace it needs,
 // and the call itself (a: the prepared arguments over the full support; ws: 256-byte aligned).
 size_t bz_support_aware_ws_bytes(long long rows, int nchan, int nslots, int P, int os, int W, bool wproj);

@@ -35,6 +35,7 @@
 #include <mutex>
 #include <numeric>
 #include <string>
+#include <chrono>
 #include <thread>
 #include <vector>
 
@@ -124,6 +125,48 @@ extern "C" void bullseye_set_compensated(int on) { g_ctx.compensated = on != 0; 
 
 // See include/bullseye_gb300.h.
 extern "C" void bullseye_set_batched_calls(int on) { g_ctx.batched_calls = on != 0; }
+
+// ---------------------------------------------------------------- phase tracing
+namespace {
+struct Trace {
+  bool on = false;
+  std::chrono::steady_clock::time_point last;
+  std::string log;  // "phase ms; " entries since the last report
+} g_trace;
+}  // namespace
+
+void bz_trace_begin() {
+  if (!g_trace.on) return;
+  if (g_ctx.stream) cudaStreamSynchronize(g_ctx.stream);
+  g_trace.last = std::chrono::steady_clock::now();
+}
+
+void bz_trace_mark(const char *phase) {
+  if (!g_trace.on) return;
+  if (g_ctx.stream) cudaStreamSynchronize(g_ctx.stream);
+  const auto now = std::chrono::steady_clock::now();
+  const double ms = std::chrono::duration<double, std::milli>(now - g_trace.last).count();
+  g_trace.last = now;
+  char buf[96];
+  snprintf(buf, sizeof buf, "%s %.3f; ", phase, ms);
+  if (g_trace.log.size() < (1u << 16)) g_trace.log += buf;
+}
+
+// See include/bullseye_gb300.h.
+extern "C" void bullseye_set_tracing(int on) {
+  g_trace.on = on != 0;
+  g_trace.log.clear();
+}
+
+// See include/bullseye_gb300.h.
+extern "C" size_t bullseye_trace_report(char *buf, size_t n) {
+  const size_t len = g_trace.log.size();
+  if (buf && n) {
+    snprintf(buf, n, "%s", g_trace.log.c_str());
+    g_trace.log.clear();
+  }
+  return len;
+}
 
 // Device-resident inputs: when on, the row arrays (visibilities, weights, flags, uvw, flagged
 // rows, field, spw, antenna and timestamp ids), jones_terms and baseline_starting_indexes in
@@ -590,6 +633,7 @@ static bool upload_rows(const gridding_parameters &p, bool need_ants, bool need_
   const size_t R = p.row_count;
   if (c.device_inputs) return true;
   if (!ensure_row_buffers()) return false;
+  bz_trace_mark("row_buffers");
   if (R > c.max_rows) {
     bz_record_error(BZ_ERR_INVALID_ARGUMENT, "row_count %zu exceeds chunk_max_row_count %zu", R, c.max_rows);
     return false;
@@ -704,6 +748,7 @@ bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool f
   }
   const bool jones = mode == CORR_QUAD_JONES;
   if (upload && !upload_rows(p, jones, jones, !sampling)) return false;
+  bz_trace_mark("rows_h2d");
   if (jones) {
     const size_t nj = p.no_timestamps_read * p.antenna_count * c.F * c.nspw * c.nchan;
     if (!p.jones_terms || nj == 0) {
@@ -717,9 +762,11 @@ bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool f
       BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.jones_raw.ptr, p.jones_terms, sizeof(vis_complex) * 4 * nj, cudaMemcpyHostToDevice, c.stream), false);
       jsrc = c.jones_raw.ptr;
     }
+    bz_trace_mark("jones_alloc_h2d");
     invert_jones_kernel<<<(unsigned)((nj + 255) / 256), 256, 0, c.stream>>>(jsrc, c.jones_inv.ptr, (long long)nj,
                                                                              c.dev_error.ptr);
     c.launches++;
+    bz_trace_mark("jones_invert");
   }
   int seg = 0;
   const size_t *starts = nullptr;
@@ -808,13 +855,17 @@ static void grid_common(gridding_parameters *pp, int nc, int mode, bool faceting
   if (c.batched_calls && c.C == 4 && (sampling || nc == 4)) {
     // the support-aware batched gridder (same results; see batched.cu)
     settle_kernel_timing();
+    bz_trace_begin();
     cudaEventRecord(c.ev_k0, c.stream);
     if (!bz_grid_batched_call(p, mode, faceting, name)) return;
     cudaEventRecord(c.ev_k1, c.stream);
     c.kernel_timing_pending = true;
     c.kernel_timing_kind = sampling ? 1 : 0;
     c.kernel_count[c.kernel_timing_kind]++;
-    if (p.is_final_data_chunk) copy_back_grids(p, sampling);
+    if (p.is_final_data_chunk) {
+      copy_back_grids(p, sampling);
+      bz_trace_mark(sampling ? "sf.copy_back" : "vis.copy_back");
+    }
     timer_stop();
     return;
   }

@@ -53,6 +53,8 @@ EXTENSIONS = {
     "bullseye_batched_plane_classes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "bullseye_selftest_bounded_wait": (ctypes.c_int, []),
     "bullseye_set_batched_calls": (None, [ctypes.c_int]),
+    "bullseye_set_tracing": (None, [ctypes.c_int]),
+    "bullseye_trace_report": (ctypes.c_size_t, [ctypes.c_char_p, ctypes.c_size_t]),
     "bullseye_grid_batched_facets": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     "bullseye_facet_4_cor_corrections_ws_bytes": (ctypes.c_size_t, [ctypes.c_void_p]),

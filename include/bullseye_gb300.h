@@ -154,6 +154,13 @@ int bullseye_batched_plane_classes(int *width, int max);
  * per-track kernels, which grid the full padded support.  Single and dual polarisation calls
  * always use the plain kernels. */
 void bullseye_set_batched_calls(int on);
+/* Phase tracing of the batched gridding calls: when on, each call synchronises its stream at phase
+ * boundaries (upload and prepare, schedule/tune/capture, the class kernels, copy-back) and records
+ * their host times; bullseye_trace_report writes "phase ms; ..." for the calls since the last
+ * report into buf (up to n bytes) and returns the length of the log.  Tracing changes the overlap
+ * of those phases: use it to see where a call's time goes, not to time it. */
+void bullseye_set_tracing(int on);
+size_t bullseye_trace_report(char *buf, size_t n);
 /* Self-test of the batched gridder's bounded waits: runs one CTA whose tap-copy barrier never
  * completes and returns the device error bits it recorded (16 = the wait ran out, as expected),
  * or -1 on a CUDA error.  Takes about 0.2 s; touches no library state. */
