@@ -882,8 +882,8 @@ extern "C" int bullseye_grid_batched_facets(gridding_parameters *pp, const bulls
 // per-plane windows, the support-window table and the run schedule are built on the device in the
 // caller's workspace from the call's own (device) tables, and every candidate class width gets
 // one persistent launch (a class no plane uses finds no work items).  The layout of a class is
-// the tuner's choice when the library has tuned that width, else J = 4 (J = 8 where the
-// J = 4 layout needs more than 512 threads).
+// fixed, J = 4 (J = 8 where the J = 4 layout needs more than 512 threads), so that concurrent
+// calls with their own workspaces read no shared state.
 
 namespace {
 
@@ -1019,10 +1019,6 @@ bool support_aware_launches(const GridArgs &a, const ClassList &cl, int nfacets,
     const int W = cl.w[k];
     Variant v;
     bool have = false;
-    auto it = g_bs.tuned.find(std::make_tuple(W, 4, (int)WPROJ, (int)COMP));
-    if (it != g_bs.tuned.end())
-      have = make_variant<4, WPROJ>(W, std::get<0>(it->second), std::get<1>(it->second) != 0, std::get<2>(it->second), v) &&
-             finish_variant<4, WPROJ, COMP>(v);
     for (int J : {4, 8})
       if (!have) have = make_variant<4, WPROJ>(W, J, false, kSegRegs<4>, v) && finish_variant<4, WPROJ, COMP>(v);
     if (!have) have = make_variant<4, WPROJ>(W, 8, true, kSegRegs<8>, v) && finish_variant<4, WPROJ, COMP>(v);

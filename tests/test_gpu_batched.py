@@ -130,3 +130,24 @@ def test_bounded_wait_runs_out_and_reports(precision, gpu_required, built_librar
     assert lib.bullseye_selftest_bounded_wait() == 16
     x = torch.ones(1024, device="cuda")
     assert float(x.sum()) == 1024.0  # the device still runs work afterwards
+
+
+def test_tracing_reports_the_phases_of_a_call(libs):
+    """bullseye_set_tracing records the phases of the batched gridding calls: upload and prepare,
+    schedule/tune/capture, the class kernels and copy-back; the report empties the log."""
+    import ctypes
+    lib = libs["single"]
+    p = synth.small_problem("single", nx=96, n_ant=6, n_times=8, n_chan=2, s=7, os=5, wplanes=4, min_support=5,
+                            n_facets=2, jones=True)
+    lib.bullseye_set_tracing(1)
+    try:
+        run_imaging(lib, p, "facet_4_cor_corrections", repack=True, keep_raw=True, psf=True)
+        buf = ctypes.create_string_buffer(1 << 16)
+        n = lib.bullseye_trace_report(buf, len(buf))
+        log = buf.value.decode()
+        assert n > 0 and n == len(log)
+        for phase in ("vis.upload_prepare", "schedule_tune_capture", "vis.grid", "vis.copy_back", "sf.grid"):
+            assert phase in log, (phase, log)
+        assert lib.bullseye_trace_report(buf, len(buf)) == 0  # emptied by the report
+    finally:
+        lib.bullseye_set_tracing(0)
