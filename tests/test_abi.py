@@ -83,3 +83,32 @@ def test_repack_input_data_is_a_stable_baseline_sort(built_libraries):
     np.testing.assert_array_equal(arrays["t"], p.timestamp_ids[perm][order])
     counts = np.bincount(b, minlength=p.baseline_count)
     np.testing.assert_array_equal(starts, np.concatenate([[0], np.cumsum(counts)]))
+
+
+@pytest.mark.parametrize("precision", ["single", "double"])
+def test_workspace_size_covers_the_support_aware_schedule(precision, built_libraries):
+    """bullseye_facet_4_cor_corrections_ws_bytes (host-only): the compensation grid (32-bit library),
+    the facet table and an error word, plus the support-aware form's tables and run schedule, which
+    grow by about 33 bytes per (row, channel)."""
+    from bullseye_gb300.library import load_library
+    lib = load_library("GPU", precision)
+
+    def size(rows, chans=32, nx=512, wplanes=32, support=15):
+        st = gridding_parameters_type(precision)()
+        st.row_count = rows
+        st.channel_count = chans
+        st.spw_count = 1
+        st.nx = st.ny = nx
+        st.num_facet_centres = 2
+        st.cube_channel_dim_size = 1
+        st.number_of_polarization_terms = st.number_of_polarization_terms_being_gridded = 4
+        st.conv_support, st.conv_oversample, st.wplanes = support, 15, wplanes
+        st.baseline_count = 0
+        return int(lib.bullseye_facet_4_cor_corrections_ws_bytes(ctypes.byref(st)))
+
+    grid_bytes = 2 * 4 * 512 * 512 * 8 if precision == "single" else 0
+    small, large = size(1000), size(101000)
+    assert small >= grid_bytes
+    per_vis = (large - small) / (100000 * 32)
+    assert 32.0 <= per_vis <= 34.0, per_vis
+    assert size(1000, wplanes=64) > small  # the window table grows with the w planes
