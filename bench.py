@@ -333,7 +333,7 @@ class ClockSampler:
 
 
 def clocks_path(name):
-    """Where the raw clock samples go: gpurun_out/ when it exists, else nowhere."""
+    """Where the raw clock samples go: the run's output folder when it exists, else nowhere."""
     d = os.path.join(REPO, "gpurun_out")
     return os.path.join(d, name) if os.path.isdir(d) else None
 

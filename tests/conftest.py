@@ -1,6 +1,6 @@
 """pytest configuration: the ``gpu`` marker and shared fixtures.
 
-Tests marked ``gpu`` need a CUDA device (a GB300 for the numbers quoted in the design doc); all other
+Tests marked ``gpu`` need a CUDA device (the libraries are built for GB300, sm_103a); all other
 tests run on a CPU-only machine.
 """
 import os
