@@ -69,6 +69,9 @@ void facet_single_pol(gridding_parameters *params);
 void grid_duel_pol(gridding_parameters *params);
 /* Two correlations, faceted (wrapper.cu:736-831). */
 void facet_duel_pol(gridding_parameters *params);
+/* The four-correlation and sampling-function calls below run the batched, support-aware gridder
+ * (see bullseye_grid_batched) when the library is initialised for 4 correlations, unless
+ * bullseye_set_batched_calls(0) selects the per-track kernels; the grids are the same. */
 /* Four correlations, no faceting (wrapper.cu:832-909). */
 void grid_4_cor(gridding_parameters *params);
 /* Four correlations, faceted (wrapper.cu:910-987). */
