@@ -53,6 +53,15 @@ WORKLOAD = ("facet_4_cor_corrections+facet_sampling_function, 27 ant x 2000 t x 
             "16 facets 1024^2, w-proj 64 planes support 15-63 (padded 63), os 15, Jones, uniform")
 
 
+# DRAM traffic of one batched step (dram__bytes_read.sum + dram__bytes_write.sum, every launch of
+# the step), captured with ncu on the 16-channel, 4-facet cut of this workload (4.372 GB for
+# 44.93 M vis-facet pairs) and scaled by vis-facet pairs: an upper estimate for the full step,
+# where 16 facets rather than 4 share each row in L2.
+TRAFFIC_BYTES_PER_PAIR = 4.372e9 / 44928000
+TRAFFIC_SOURCE = ("ncu dram bytes of one eager step of the 16-channel 4-facet case (4.372 GB / 44.93 M pairs), "
+                  "scaled by vis-facet pairs (upper estimate: more facets share each row in L2)")
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -991,7 +1000,11 @@ def main():
                 "form": "plain" if args.form == "batched" else "batched", "ms_per_step": other_ms,
                 "value": pairs_per_step * world / (other_ms * 1e-3) / 1e6, "unit": "Mvis/s"},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                         "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
+                         "frac": achieved / fp32_peak if fp32_peak else None,
+                         "traffic": (TRAFFIC_BYTES_PER_PAIR * pairs_per_step
+                                     if args.form == "batched" and not args.chans and not args.facets else None),
+                         "traffic_source": TRAFFIC_SOURCE if args.form == "batched" else None,
+                         "algorithmic_bytes": pairs_per_step * bytes_per_pair,
                          "peak_source": "measured FP32 FMA probe on this GPU (MEASURED_PEAKS.json has no FP32 rate)",
                          "kernel": kernel_name, "launch_ms": launch_ms,
                          "flops_per_pair": flops_per_pair,
