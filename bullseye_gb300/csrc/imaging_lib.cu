@@ -986,20 +986,36 @@ extern "C" void normalize(gridding_parameters *pp) {
 }
 
 // ---------------------------------------------------------------- finalize (cuFFT)
-static void finalize_buffer(vis_complex *host, size_t per_facet_slices, size_t nslices, const char *name) {
+// Combination applied by bullseye_finalize_stokes before the transform: slice c of facet f becomes
+// (G[f][c][a] + sign G[f][c][b]) / 2.
+struct StokesPair {
+  int a, b, sign;
+};
+
+static void finalize_buffer(vis_complex *host, size_t per_facet_slices, size_t nslices, const char *name,
+                            const StokesPair *stokes = nullptr) {
   Context &c = g_ctx;
   const size_t nxy = c.nx * c.ny, F = c.F;
   if (!host || nslices == 0) return;
   const size_t total = F * nslices * nxy;
   DevBuf<vis_complex> work, shifted;
   DevBuf<float> packed;
-  if (!work.alloc(total) || !shifted.alloc(total) || !packed.alloc(total)) return;
+  // with a Stokes combination the whole facet blocks are uploaded into `work` first
+  if (!work.alloc(stokes ? F * per_facet_slices * nxy : total) || !shifted.alloc(total) || !packed.alloc(total)) return;
   cudaStream_t s = c.stream;
   cudaEventRecord(c.ev_i0, s);
-  // upload the first nslices slices of every facet block
-  for (size_t f = 0; f < F; ++f)
-    BZ_CUDA_TRY(cudaMemcpyAsync(shifted.ptr + f * nslices * nxy, host + f * per_facet_slices * nxy,
-                                sizeof(vis_complex) * nslices * nxy, cudaMemcpyHostToDevice, s));
+  if (stokes) {
+    BZ_CUDA_TRY(cudaMemcpyAsync(work.ptr, host, sizeof(vis_complex) * F * per_facet_slices * nxy, cudaMemcpyHostToDevice,
+                                s));
+    stokes_combine_kernel<<<2048, 256, 0, s>>>(work.ptr, shifted.ptr, (long long)nxy, (int)F, (int)nslices,
+                                               (int)(per_facet_slices / nslices), stokes->a, stokes->b, stokes->sign);
+    c.launches++;
+  } else {
+    // upload the first nslices slices of every facet block
+    for (size_t f = 0; f < F; ++f)
+      BZ_CUDA_TRY(cudaMemcpyAsync(shifted.ptr + f * nslices * nxy, host + f * per_facet_slices * nxy,
+                                  sizeof(vis_complex) * nslices * nxy, cudaMemcpyHostToDevice, s));
+  }
   ifftshift_gather_kernel<<<2048, 256, 0, s>>>(shifted.ptr, work.ptr, (int)c.nx, (int)c.ny, (long long)(F * nslices));
   c.launches += 2;  // the gather and the packing kernel (cuFFT's own launches are not counted)
   cufftHandle plan;
@@ -1051,6 +1067,21 @@ extern "C" void finalize(gridding_parameters *pp) {
   gridding_barrier();
   finalize_buffer(pp->output_buffer, pp->cube_channel_dim_size * pp->number_of_polarization_terms_being_gridded,
                   pp->cube_channel_dim_size, "finalize");
+}
+
+// See include/bullseye_gb300.h.
+extern "C" void bullseye_finalize_stokes(gridding_parameters *pp, int corr_a, int corr_b, int sign) {
+  if (!check_ready("bullseye_finalize_stokes")) return;
+  const int C = (int)pp->number_of_polarization_terms_being_gridded;
+  if (corr_a < 0 || corr_a >= C || corr_b < 0 || corr_b >= C || (sign != 1 && sign != -1)) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "bullseye_finalize_stokes: correlations %d, %d of %d and sign %d", corr_a,
+                    corr_b, C, sign);
+    return;
+  }
+  gridding_barrier();
+  const StokesPair sp{corr_a, corr_b, sign};
+  finalize_buffer(pp->output_buffer, pp->cube_channel_dim_size * (size_t)C, pp->cube_channel_dim_size,
+                  "bullseye_finalize_stokes", &sp);
 }
 
 extern "C" void finalize_psf(gridding_parameters *pp) {

@@ -80,6 +80,25 @@ __global__ void broadcast_add_kernel(const vis_complex *__restrict__ init, const
 
 // Gather with the inverse shift of numpy's ifftshift: dst[y][x] = src[(y+ny/2)%ny][(x+nx/2)%nx]
 // for each of `slices` planes.  Equivalent to bullseye/mo/cpu_gpu_common/fft_shift_utils.cpp:75-111.
+// Stokes (or correlation) term of every (facet, cube slice): dst[f][c] = (src[f][c][a] +
+// sign * src[f][c][b]) / 2 over nxy cells, from facet blocks of `cube` x `corr` slices into
+// compact [facet][cube] slices (bullseye/data/stokes.py:90-172 combines the same pairs on the host).
+__global__ void stokes_combine_kernel(const vis_complex *__restrict__ src, vis_complex *__restrict__ dst, long long nxy,
+                                      int facets, int cube, int corr, int a, int b, int sign) {
+  const long long total = (long long)facets * cube * nxy;
+  const vis_real half = (vis_real)0.5, sg = (vis_real)sign;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long fc = i / nxy, r = i - fc * nxy;
+    const long long base = fc * corr * nxy + r;  // slice (f, c, 0) of the facet block
+    const vis_complex va = src[base + (long long)a * nxy], vb = src[base + (long long)b * nxy];
+    vis_complex o;
+    o.re = (va.re + sg * vb.re) * half;
+    o.im = (va.im + sg * vb.im) * half;
+    dst[i] = o;
+  }
+}
+
 __global__ void ifftshift_gather_kernel(const vis_complex *__restrict__ src, vis_complex *__restrict__ dst, int nx,
                                         int ny, long long slices) {
   long long nxy = (long long)nx * ny;

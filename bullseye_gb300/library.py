@@ -54,6 +54,7 @@ EXTENSIONS = {
     "bullseye_selftest_bounded_wait": (ctypes.c_int, []),
     "bullseye_set_batched_calls": (None, [ctypes.c_int]),
     "bullseye_set_tracing": (None, [ctypes.c_int]),
+    "bullseye_finalize_stokes": (None, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "bullseye_trace_report": (ctypes.c_size_t, [ctypes.c_char_p, ctypes.c_size_t]),
     "bullseye_grid_batched_facets": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),

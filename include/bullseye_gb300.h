@@ -157,6 +157,15 @@ int bullseye_batched_plane_classes(int *width, int max);
  * per-track kernels, which grid the full padded support.  Single and dual polarisation calls
  * always use the plain kernels. */
 void bullseye_set_batched_calls(int on);
+/* finalize with the Stokes (or correlation) combination and facet compaction done on the device:
+ * for every facet f and cube slice c, (G[f][c][corr_a] + sign * G[f][c][corr_b]) / 2 of the host
+ * grids (after weight_uniformly / normalize; corr_a and corr_b index the gridded correlation
+ * slices) is placed at cube slice c of the facet block, then transformed and packed as finalize
+ * does.  These are the combinations bullseye/data/stokes.py:90-172 forms on the host: linear feeds
+ * I = (XX, YY, +1), Q = (XX, YY, -1), U = (XY, YX, +1), V = (XY, YX, -1); circular feeds
+ * I = (RR, LL, +1), V = (RR, LL, -1), Q = (RL, LR, +1), U = (RL, LR, -1).  corr_a == corr_b with
+ * sign +1 selects one correlation.  No counterpart in the reference library. */
+void bullseye_finalize_stokes(gridding_parameters *params, int corr_a, int corr_b, int sign);
 /* Phase tracing of the batched gridding calls: when on, each call synchronises its stream at phase
  * boundaries (upload and prepare, schedule/tune/capture, the class kernels, copy-back) and records
  * their host times; bullseye_trace_report writes "phase ms; ..." for the calls since the last
