@@ -2,7 +2,8 @@
 """Benchmark: gridded Mvis/s on one GB300 for the multi-facet Jones + w-projection workload.
 
 Workload (one "step" = one pass of the facet-imaging hot path over the whole visibility set):
-  27 antennas (351 baselines) on a seeded Y layout, 2000 timesteps of Earth rotation, 64 channels
+  27 antennas (351 baselines) at the EVLA positions of the reference's benchmark
+  (bullseye/mo/benchmarks/benchmark.cpp:68-95), 2000 timesteps of Earth rotation, 64 channels
   1.0-1.5 GHz -> 702,000 rows x 64 channels = 44.93 M visibilities (4 correlations, complex64);
   50 seeded point sources + noise; seeded per-antenna, per-time, per-facet 2x2 gains; 16 facets
   of 1024^2 within 3 deg; w-projection with 64 planes, supports 15..63 (ABI table padded to 63,
@@ -87,6 +88,11 @@ def parse():
                     help="skip the eager, per-support-class timed step after the timed region")
     ap.add_argument("--eager", action="store_true",
                     help="batched form without graph replay (per-class launches with events; for profilers)")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the parity check of the batched FP32 path against the FP64 oracle on the row sample")
+    ap.add_argument("--sample-baselines", type=int, default=0,
+                    help="baselines (all their timesteps) in the CPU-baseline / parity row sample (0: sized by time)")
+    ap.add_argument("--clocks-dir", default=None, help="also write the raw nvidia-smi clock samples into this folder")
     return ap.parse_args()
 
 
@@ -97,8 +103,7 @@ def geometry(n_times, world=1, rank=0):
     from bullseye_gb300 import synth
     from bullseye_gb300.sharding import facet_shard
     dec = np.deg2rad(-30.0)
-    enu = synth.y_layout(N_ANT, 600.0, seed=2)
-    xyz = synth.enu_to_equatorial(enu, np.deg2rad(34.0))
+    xyz = synth.evla27_equatorial()  # the reference benchmark's EVLA-27 positions
     uvw, a1, a2, tid = synth.earth_rotation_rows(xyz, n_times, dec, np.deg2rad(120.0))
     freqs = np.linspace(1.0e9, 1.5e9, N_CHAN)
     lam = synth.C_LIGHT / freqs
@@ -341,65 +346,156 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+CLOCKS_DIR = None  # --clocks-dir
+
+
 def clocks_path(name):
-    """Where the raw clock samples go: the run's output folder when it exists, else nowhere."""
-    d = os.path.join(REPO, "gpurun_out")
-    return os.path.join(d, name) if os.path.isdir(d) else None
+    """Where the raw clock samples go: the --clocks-dir folder when one was given, else nowhere."""
+    return os.path.join(CLOCKS_DIR, name) if CLOCKS_DIR else None
 
 
-# ----------------------------------------------------------------------------- CPU (oracle port)
-def cpu_run(geo, conv1d, n_rows_sample, threads=None):
-    """Time the oracle port of the reference CPU library (single precision) on the first
-    ``n_rows_sample`` rows of every baseline-sorted track set (all facets, all channels)."""
-    from bullseye_gb300.abi import gridding_parameters_type
-    from bullseye_gb300.filters import outer_stack
-    from oracle.harness import load_oracle
-    lib = load_oracle("single")
-    idx = np.linspace(0, geo["uvw"].shape[0] - 1, n_rows_sample).astype(np.int64)
-    R = idx.size
-    rng = np.random.default_rng(3)
-    vis = (rng.normal(0, 1, (R, N_CHAN, 4)) + 1j * rng.normal(0, 1, (R, N_CHAN, 4))).astype(np.complex64)
-    wt = np.ones((R, N_CHAN, 4), np.float32)
-    fl = np.zeros((R, N_CHAN, 4), np.bool_)
-    uvw = geo["uvw"][idx].astype(np.float32)
-    T = 1
-    jones = np.zeros((T, N_ANT, N_FACETS, 1, N_CHAN, 4), np.complex64)
-    jones[..., 0] = 1.05 * np.exp(0.3j)
-    jones[..., 3] = 0.97 * np.exp(-0.2j)
-    jones[..., 1] = 0.02
-    conv2d = outer_stack(conv1d.astype(np.complex128)).astype(np.complex64)
-    tab = Tables(geo, conv2d)
-    st = gridding_parameters_type("single")()
+# ----------------------------------------------------------------------------- CPU (oracle port) and parity
+def sample_baselines(geo, n):
+    """``n`` cross baselines spread over the baseline slots, each with all its timesteps: the row
+    sample of the CPU baseline and of the parity check (whole tracks, as the gridder sees them)."""
+    starts = geo["starts"].astype(np.int64)
+    full = np.nonzero(starts[1:] > starts[:-1])[0]
+    pick = np.unique(full[np.linspace(0, full.size - 1, max(1, n)).astype(np.int64)])
+    rows = np.concatenate([np.arange(starts[b], starts[b + 1]) for b in pick])
+    return pick, rows
+
+
+def host_sample(geo, pick, vis=None, jones=None, seed=3):
+    """Host arrays of the rows of baselines ``pick`` (baseline-major, as the workload), with their
+    track starts.  ``vis`` [R, Ch, 4] and ``jones`` [T, A', F, 1, Ch, 4] (A' = the antennas the sample
+    uses, ascending) are the workload's own arrays when given (complex64), else seeded stand-ins of
+    the same distributions.  Antenna ids are renumbered to the antennas the sample uses."""
+    starts_all = geo["starts"].astype(np.int64)
+    counts = starts_all[pick + 1] - starts_all[pick]
+    rows = np.concatenate([np.arange(starts_all[b], starts_all[b + 1]) for b in pick])
+    a1, a2 = geo["a1"][rows], geo["a2"][rows]
+    ants = np.unique(np.concatenate([a1, a2]))
+    remap = np.full(N_ANT, -1, np.int64)
+    remap[ants] = np.arange(ants.size)
+    R, T = rows.size, geo["n_times"]
+    rng = np.random.default_rng(seed)
+    if vis is None:
+        vis = (rng.normal(0, 1, (R, N_CHAN, 4)) + 1j * rng.normal(0, 1, (R, N_CHAN, 4))).astype(np.complex64)
+    if jones is None:
+        shape = (T, ants.size, N_FACETS, 1, N_CHAN)
+        jones = np.zeros(shape + (4,), np.complex64)
+        for k in (0, 3):
+            jones[..., k] = (1 + rng.uniform(-0.1, 0.1, shape)) * np.exp(1j * rng.uniform(-np.pi, np.pi, shape))
+        for k in (1, 2):
+            jones[..., k] = 0.05 * (rng.normal(0, 1, shape) + 1j * rng.normal(0, 1, shape)) / np.sqrt(2)
+    return dict(vis=np.ascontiguousarray(vis, np.complex64), uvw=geo["uvw"][rows].astype(np.float32),
+                weights=np.ones((R, N_CHAN, 4), np.float32), flags=np.zeros((R, N_CHAN, 4), np.bool_),
+                flagged_rows=np.zeros(R, np.bool_), field=np.zeros(R, np.uint32), spw=np.zeros(R, np.uint32),
+                a1=remap[a1].astype(np.uint32), a2=remap[a2].astype(np.uint32),
+                tid=geo["tid"][rows].astype(np.uintp), jones=np.ascontiguousarray(jones, np.complex64),
+                starts=np.concatenate([[0], np.cumsum(counts)]).astype(np.uintp), n_ant=int(ants.size),
+                rows=rows, ants=ants)
+
+
+def run_sample(lib, precision, geo, conv, smp, post=True):
+    """The pipeliner's call sequence on the row sample: initLibrary, facet_4_cor_corrections +
+    facet_sampling_function (timed), then weight_uniformly and normalize when ``post``.  Returns the
+    seconds of the gridding calls and the normalised grids [F, 1, 4, NX, NX]."""
+    from bullseye_gb300.abi import complex_dtype, gridding_parameters_type, real_dtype
+    cd, rd = complex_dtype(precision), real_dtype(precision)
+    arr = {k: (v.astype(cd) if v.dtype == np.complex64 else v.astype(rd) if v.dtype == np.float32 else v)
+           for k, v in smp.items() if isinstance(v, np.ndarray) and k not in ("rows", "ants")}
+    arr = {k: np.ascontiguousarray(v) for k, v in arr.items()}
+    tab = Tables(geo, np.ascontiguousarray(conv.astype(cd)))
+    tab.lam = tab.lam.astype(rd)
+    tab.facets = tab.facets.astype(rd)
+    tab.grid = np.zeros((N_FACETS, 1, 4, NX, NX), dtype=cd)
+    tab.sf = np.zeros((N_FACETS, 1, 1, NX, NX), dtype=cd)
+    st = gridding_parameters_type(precision)()
+    R = arr["uvw"].shape[0]
     tab.fill(st, geo, R)
+    st.antenna_count = smp["n_ant"]
+    st.baseline_count = smp["starts"].size - 1
     P = ctypes.c_void_p
-    keep = dict(vis=vis, uvw=uvw, weights=wt, flags=fl, flagged_rows=np.zeros(R, np.bool_),
-                field=np.zeros(R, np.uint32), spw=np.zeros(R, np.uint32),
-                a1=geo["a1"][idx].astype(np.uint32), a2=geo["a2"][idx].astype(np.uint32),
-                tid=np.zeros(R, np.uintp), jones=jones, starts=np.zeros(2, np.uintp))
     lib.initLibrary(ctypes.byref(st))
-    set_rows(st, keep, lambda a: a.ctypes.data_as(P))
-    st.no_timestamps_read = T
-    st.baseline_starting_indexes = None
+    set_rows(st, arr, lambda a: a.ctypes.data_as(P))
+    st.is_final_data_chunk = True
     t0 = time.perf_counter()
     lib.facet_4_cor_corrections(ctypes.byref(st))
     lib.facet_sampling_function(ctypes.byref(st))
+    lib.gridding_barrier()
     dt = time.perf_counter() - t0
+    if post:
+        lib.weight_uniformly(ctypes.byref(st))
+        lib.normalize(ctypes.byref(st))
     lib.releaseLibrary()
+    return dt, tab.grid
+
+
+def cpu_baseline(geo, conv1d, target_s, smp=None, nbl=0):
+    """The oracle port of the reference CPU library (single precision, OpenMP over facets) timed on
+    a sample of whole baselines of the workload."""
+    from bullseye_gb300.filters import outer_stack
+    from oracle.harness import load_oracle
+    lib = load_oracle("single")
+    conv2d = outer_stack(conv1d.astype(np.complex128)).astype(np.complex64)
+    if smp is None:
+        if not nbl:
+            # one baseline first, to size the sample to about target_s seconds
+            pick, _ = sample_baselines(geo, 1)
+            dt1, _ = run_sample(lib, "single", geo, conv2d, host_sample(geo, pick), post=False)
+            nbl = int(max(1, min(64, round(target_s / max(dt1, 1e-3)))))
+        pick, _ = sample_baselines(geo, nbl)
+        smp = host_sample(geo, pick)
+    dt, _ = run_sample(lib, "single", geo, conv2d, smp, post=False)
+    R = smp["uvw"].shape[0]
     pairs = R * N_CHAN * N_FACETS
-    return pairs, dt
+    return {"value": pairs / dt / 1e6, "unit": "Mvis/s", "cores": min(os.cpu_count() or 1, N_FACETS), "kind": "port",
+            "sample": f"{smp['starts'].size - 1} whole baselines ({R} rows, all {geo['n_times']} timesteps) x "
+                      f"{N_CHAN} ch x {N_FACETS} facets = {pairs} vis-facet pairs of the same workload with its "
+                      f"per-time Jones terms, oracle port of the reference CPU library (FP32, OpenMP over facets, "
+                      f"{os.cpu_count()} cores available, one thread per facet), {dt:.1f} s"}
 
 
-def cpu_baseline(geo, conv1d, target_s):
-    threads = os.cpu_count() or 1
-    probe_rows = 16
-    pairs, dt = cpu_run(geo, conv1d, probe_rows)
-    per_row = dt / probe_rows
-    rows = int(max(probe_rows, min(20000, target_s / max(per_row, 1e-6))))
-    pairs, dt = cpu_run(geo, conv1d, rows)
-    return {"value": pairs / dt / 1e6, "unit": "Mvis/s", "cores": min(threads, N_FACETS), "kind": "port",
-            "sample": f"{rows} rows x 64 ch x 16 facets ({pairs} vis-facet pairs) of the same workload, "
-                      f"oracle port of the reference CPU library (FP32, OpenMP over facets, {os.cpu_count()} cores "
-                      f"available, one thread per facet), {dt:.1f} s"}
+def dirty(grid):
+    """Dirty images of grids [..., ny, nx] with the reference's shifts (FP64)."""
+    g = np.asarray(grid, np.complex128)
+    return np.fft.fftshift(np.fft.ifft2(np.fft.ifftshift(g, axes=(-2, -1))), axes=(-2, -1)).real
+
+
+def parity_check(lib32, geo, conv1d, smp):
+    """The batched FP32 path against the FP64 oracle on the row sample: the same reference exports
+    through the C-ABI (host inputs; the exports run the support-aware batched gridder with the
+    tuned class layouts and compensated FP32) and the oracle port in double precision on the same
+    values, both followed by weight_uniformly and normalize.  Per facet: max and RMS relative error
+    of the weighted, normalised grids and of the dirty images."""
+    from bullseye_gb300.filters import outer_stack
+    from bullseye_gb300.library import check
+    from oracle.harness import load_oracle
+    t0 = time.perf_counter()
+    _, g32 = run_sample(lib32, "single", geo, conv1d, smp)
+    check(lib32)
+    conv2d = outer_stack(conv1d.astype(np.complex128))
+    _, g64 = run_sample(load_oracle("double"), "double", geo, conv2d, smp)
+    facets = []
+    for f in range(N_FACETS):
+        a, b = g64[f, 0], g32[f, 0].astype(np.complex128)
+        ia, ib = dirty(a), dirty(b)
+        d, di = b - a, ib - ia
+        facets.append({"grid_max_rel": float(np.max(np.abs(d)) / np.max(np.abs(a))),
+                       "grid_rms_rel": float(np.sqrt(np.mean(np.abs(d) ** 2) / np.mean(np.abs(a) ** 2))),
+                       "image_max_rel": float(np.max(np.abs(di)) / np.max(np.abs(ia))),
+                       "image_rms_rel": float(np.sqrt(np.mean(di * di) / np.mean(ia * ia)))})
+    worst = max(x["image_max_rel"] for x in facets)
+    return {"against": "oracle port of the reference CPU library in FP64 (same input values, 2-D w-kernel stack "
+                       "of the FP32 1-D stack), weight_uniformly + normalize on both",
+            "form": "reference exports facet_4_cor_corrections + facet_sampling_function on the batched "
+                    "support-aware gridder (tuned class layouts, compensated FP32)",
+            "sample": f"{smp['starts'].size - 1} whole baselines, {smp['uvw'].shape[0]} rows x {N_CHAN} ch x "
+                      f"{N_FACETS} facets",
+            "max_rel": worst, "rms_rel": max(x["image_rms_rel"] for x in facets),
+            "grid_max_rel": max(x["grid_max_rel"] for x in facets), "tolerance": 1e-5, "pass": worst <= 1e-5,
+            "per_facet": facets, "seconds": time.perf_counter() - t0}
 
 
 # ----------------------------------------------------------------------------- precision form
@@ -751,8 +847,29 @@ def adjoint_main(args):
 
 
 # ----------------------------------------------------------------------------- main
+def relaunch(n):
+    """`bench.py --gpus N` started without torchrun: run N local ranks under torch.distributed.run
+    (one per GPU, rendezvous on 127.0.0.1) with the same arguments and return its exit status."""
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr", "127.0.0.1", f"--master-port={port}", os.path.abspath(__file__)] + sys.argv[1:]
+    return subprocess.call(cmd)
+
+
 def main():
     args = parse()
+    global CLOCKS_DIR
+    CLOCKS_DIR = args.clocks_dir
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(relaunch(args.gpus))
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world != args.gpus:
+        print(f"bench.py: --gpus {args.gpus} but WORLD_SIZE {world}", file=sys.stderr)
+        sys.exit(2)
     if args.workload == "uneven":
         return uneven_main(args)
     if args.workload == "adjoint":
@@ -762,8 +879,6 @@ def main():
         N_CHAN = args.chans
     if args.facets:
         N_FACETS = args.facets
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
     n_times = max(8, int(N_TIMES * args.time_frac))
     geo = geometry(n_times, world, rank)
     conv, supports = kernel_stack(geo["wmax"])
@@ -773,18 +888,28 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        steps = []
+        # the warm-up sizes the sample (whole baselines) to a bounded time per step
         per = max(2.0, min(20.0, 150.0 / max(1, args.steps + args.warmup)))
-        base = cpu_baseline(geo, conv, per)
-        for _ in range(args.steps):
-            steps.append(cpu_baseline(geo, conv, per)["value"])
+        from oracle.harness import load_oracle
+        from bullseye_gb300.filters import outer_stack
+        conv2d = outer_stack(conv.astype(np.complex128)).astype(np.complex64)
+        pick, _ = sample_baselines(geo, 1)
+        dt1, _ = run_sample(load_oracle("single"), "single", geo, conv2d, host_sample(geo, pick), post=False)
+        nbl = args.sample_baselines or int(max(1, min(64, round(per / max(dt1, 1e-3)))))
+        pick, _ = sample_baselines(geo, nbl)
+        smp = host_sample(geo, pick)
+        steps, base = [], None
+        for _ in range(max(1, args.steps)):
+            base = cpu_baseline(geo, conv, per, smp=smp)
+            steps.append(base["value"])
         v = float(np.median(steps))
         line = {"impl": "reference", "metric": "gridded Mvis/s (vis x facet pairs)", "value": v, "unit": "Mvis/s",
                 "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": pairs_per_step / v / 1e3,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": WORKLOAD, "l2": "inputs 4.2 GB > L2"},
                 "cpu_baseline": {"value": v, "unit": "Mvis/s", "cores": base["cores"], "kind": "port",
-                                 "sample": base["sample"]},
+                                 "sample": base["sample"] + "; each step times this sample, ms_per_step extrapolates "
+                                                            "to the whole workload"},
                 "e2e": {"value": v, "unit": "Mvis/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -909,9 +1034,20 @@ def main():
     lib.releaseLibrary()
     lib.bullseye_set_device_inputs(0)
 
+    # the row sample of the CPU baseline and the parity check: whole baselines of this workload with
+    # its own visibilities and Jones terms
+    smp = None
+    if rank == 0 and world == 1 and not (args.no_cpu and args.no_parity):
+        pick, rows = sample_baselines(geo, args.sample_baselines or 3)
+        ants = np.unique(np.concatenate([geo["a1"][rows], geo["a2"][rows]]))
+        vis_s = d["vis"][torch.as_tensor(rows.astype(np.int64), device="cuda")].cpu().numpy()
+        jones_s = d["jones"][:, torch.as_tensor(ants.astype(np.int64), device="cuda")].cpu().numpy()
+        smp = host_sample(geo, pick, vis=vis_s, jones=jones_s)
+        del vis_s, jones_s
+
     # ------------------------------------------------------------- end to end through the C-ABI
     e2e = None
-    if not args.no_e2e and rank == 0:
+    if not args.no_e2e:
         host = {k: v.cpu().pin_memory() for k, v in d.items()}
         hnp = {k: v.numpy() for k, v in host.items()}
         hnp["flagged_rows"] = hnp["flagged_rows"].view(np.bool_)
@@ -959,11 +1095,16 @@ def main():
         parts.clear()
         e2e_clocks = ClockSampler(clocks_path("clocks_e2e.csv"))
         e2e_clocks.start()
+        if world > 1:
+            torch.distributed.barrier()
         t0 = time.perf_counter()
         n_e2e = max(1, min(args.steps, 3))
         for _ in range(n_e2e):
             e2e_step()
         dt = (time.perf_counter() - t0) / n_e2e
+        if world > 1:  # every rank runs its own facets concurrently: the slowest one sets the time
+            from bullseye_gb300.sharding import max_over_ranks
+            dt = max_over_ranks(dt, device="cuda")
         e2e_clk = e2e_clocks.stop()
         h2d = sum(hnp[k].nbytes for k in ("vis", "weights", "flags", "uvw", "flagged_rows", "field", "spw", "a1",
                                           "a2", "tid", "jones", "starts"))
@@ -972,18 +1113,23 @@ def main():
         h2d += tab.conv.nbytes + tab.grid.nbytes + tab.sf.nbytes  # tables and initial grids (initLibrary)
         h2d += N_FACETS * NX * NX * 8  # finalize uploads the first cube slice of each facet
         d2h = tab.grid.nbytes + tab.sf.nbytes + N_FACETS * NX * NX * (8 + 4)
-        e2e = {"value": pairs_per_step / dt / 1e6, "unit": "Mvis/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "s_per_step": dt,
+        e2e = {"value": pairs_per_step * world / dt / 1e6, "unit": "Mvis/s", "h2d_bytes_per_step": int(h2d * world),
+               "d2h_bytes_per_step": int(d2h * world), "s_per_step": dt,
                "ms_by_call": {k: round(v / n_e2e, 1) for k, v in parts.items()}, "clocks": e2e_clk,
                "calls": ("initLibrary, facet_4_cor_corrections, facet_sampling_function (" +
                          ("plain kernels" if args.form == "plain" else "batched support-aware gridder") +
                          "), weight_uniformly, normalize, finalize, releaseLibrary (host pinned buffers)")}
 
     cpu = None
-    if not args.no_cpu and rank == 0 and world == 1:
-        cpu = cpu_baseline(geo, conv, args.cpu_seconds)
+    if not args.no_cpu and smp is not None:
+        cpu = cpu_baseline(geo, conv, args.cpu_seconds, smp=smp)
+    parity = None
+    if not args.no_parity and smp is not None:
+        lib.bullseye_set_batched_calls(0 if args.form == "plain" else 1)
+        parity = parity_check(lib, geo, conv, smp)
+        lib.bullseye_set_batched_calls(1)
     precision = None
-    if not args.no_precision and rank == 0:
+    if not args.no_precision and rank == 0 and world == 1:
         precision = precision_report()
 
     if rank == 0:
@@ -999,6 +1145,9 @@ def main():
             "other_form": None if other_ms is None else {
                 "form": "plain" if args.form == "batched" else "batched", "ms_per_step": other_ms,
                 "value": pairs_per_step * world / (other_ms * 1e-3) / 1e6, "unit": "Mvis/s"},
+            "batched_over_plain": None if other_ms is None else (
+                other_ms / ms_per_step if args.form == "batched" else ms_per_step / other_ms),
+            "parity": parity,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                          "frac": achieved / fp32_peak if fp32_peak else None,
                          "traffic": (TRAFFIC_BYTES_PER_PAIR * pairs_per_step

@@ -3,7 +3,7 @@
 :func:`facet_grid` grids four-correlation visibilities into per-facet grids exactly as
 ``facet_4_cor_corrections`` does (Jones correction J_p^-1 V J_q^-H, per-facet phase rotation and
 planar uv transform, Romein gridding with the AA or w-projection kernel:
-bullseye/mo/cpu_gpu_common/wrapper.cu:988-1150 and the CPU policies it mirrors,
+bullseye/mo/gpu_algorithm/wrapper.cu:988-1150 and the CPU policies it mirrors,
 correlation_gridding_policies.h:503-542, phase_transform_policies.h:110-134,
 baseline_transform_policies.h:117-149).  The forward pass runs the library's workspace entry point
 (bullseye_facet_4_cor_corrections_ws, with a torch-allocated workspace) on torch's current stream; the backward pass runs the library's adjoint (degridding) kernel
@@ -168,6 +168,11 @@ class _FacetGrid(torch.autograd.Function):
         if rc != 0:
             check(lib)
             raise ImagingError(f"bullseye_facet_4_cor_corrections_ws failed with status {rc}")
+        # device-side errors (singular Jones terms, ids out of range): waits for the forward kernels
+        rc = lib.bullseye_facet_4_cor_corrections_status(ctypes.byref(st), ctypes.c_void_p(aligned), _stream())
+        if rc != 0:
+            check(lib)
+            raise ImagingError(f"bullseye_facet_4_cor_corrections_ws reported device status {rc}")
         ctx.geom = geom
         ctx.save_for_backward(vis, jones)
         ctx.mark_non_differentiable(norm)
@@ -187,9 +192,45 @@ def facet_grid(geom: FacetGeometry, vis: torch.Tensor, jones: torch.Tensor):
 
     ``vis`` is [rows, channels, 4] in the geometry's row order, ``jones`` the raw (not inverted)
     terms [T, A, F, S, Ch, 4]; both complex64 (32-bit library) or both complex128 (64-bit).
-    Differentiable with respect to both.
+    Differentiable with respect to both.  The forward waits for its kernels and raises
+    :class:`ImagingError` on a device-side error (a singular Jones matrix, ids out of range).
     """
     geom._check(vis, jones)
     if jones is None:
         raise ValueError("jones terms are required (use identity matrices for none)")
     return _FacetGrid.apply(vis, jones, geom)
+
+
+def predict(geom: FacetGeometry, model: torch.Tensor, jones: torch.Tensor | None = None, *, faceting: bool = True,
+            normalise: bool = False, from_grid: bool = False, taper=None) -> torch.Tensor:
+    """Model visibilities [rows, channels, 4] (the geometry's row order) predicted by the library's
+    bullseye_predict from per-facet models [F, cube, 4, ny, nx]: images (divided by the gridding
+    correction ``taper`` = (taper_x [nx], taper_y [ny]) float64 tensors when given, then transformed
+    to uv grids) or, with ``from_grid``, uv grids.  ``jones`` (raw terms [T, A, F, S, Ch, 4]) are
+    applied forward; ``normalise`` divides each facet's degridded value by its tap sum (the
+    reference's prototype degridder).  Not differentiable."""
+    lib = load_library("GPU", geom.precision)
+    s = geom.scalars
+    dt = torch.complex64 if geom.precision == "single" else torch.complex128
+    if tuple(model.shape) != geom.grid_shape or model.dtype != dt or not model.is_contiguous():
+        raise ValueError(f"model must be contiguous {geom.grid_shape} of {dt}")
+    out = torch.empty((s["rows"], s["channels"], 4), dtype=dt, device=model.device)
+    st = geom.struct(None, jones)
+    ws, ws_ptr, nbytes = None, None, 0
+    if not from_grid:
+        nbytes = int(lib.bullseye_predict_ws_bytes(ctypes.byref(st)))
+        ws = torch.empty(nbytes + 256, dtype=torch.uint8, device=model.device)
+        ws_ptr = ctypes.c_void_p((ws.data_ptr() + 255) // 256 * 256)
+    tx = ty = None
+    if taper is not None:
+        tx = ctypes.c_void_p(taper[0].data_ptr())
+        ty = ctypes.c_void_p(taper[1].data_ptr())
+    flags = (1 if normalise else 0) | (2 if from_grid else 0)
+    rc = lib.bullseye_predict(ctypes.byref(st), ctypes.c_void_p(model.data_ptr()), tx, ty, 1 if faceting else 0, flags,
+                              ctypes.c_void_p(out.data_ptr()), ws_ptr, nbytes, _stream())
+    if rc != 0:
+        check(lib)
+        raise ImagingError(f"bullseye_predict failed with status {rc}")
+    if ws is not None:
+        torch.cuda.current_stream().synchronize()  # the workspace is released on return
+    return out

@@ -17,12 +17,25 @@
 // the footprint the gridder wrote.  The normalisation sums depend only on weights and taps, so they
 // carry no gradient.
 //
-// One warp per (row, channel) loops over the facets: lane 0 resolves Jones and geometry, the lanes
-// split the W x W footprint, the partial sums are reduced with shuffles, lane 0 forms the
-// gradients.  The visibility gradient (summed over facets) is written once; Jones gradients are
-// accumulated with atomics because
-// every antenna appears on many baselines.
+// Prediction (bullseye_predict) is the physical forward model of the same measurement, on the same
+// gather: from model grids G_f (the model images divided by the gridding correction, transformed
+// with the reference's shifts, or given as grids),
+//   D   = sum over the footprint of G_f conj(tap)            [/ Re sum tap: the normalised form of
+//                                                              the reference's prototype degridder,
+//                                                              Resampling.ipynb cell 17]
+//   V'  = D (w >= 0) or conj(D) (w < 0),   M = e^{-i phi_f} V'
+//   V  += J_p M J_q^H   (the gains applied forward; no weights, no flags), summed over facets.
+//
+// Work layout: a warp takes 32 (row, channel) items; each lane resolves its own item's Jones terms
+// and geometry, the warp gathers the footprints item by item with every lane, and shuffles reduce
+// each item's sums into its lane.  The visibility result (summed over facets) is written once;
+// Jones gradients are accumulated with atomics because every antenna appears on many baselines.
+#include <cufft.h>
+
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "common.h"
 #include "gridder.cuh"
@@ -52,6 +65,7 @@ struct AdjointArgs {
   vis_complex *grad_jones;        // like jones, accumulated; or null
   long long nrows;
   int nchan, nspw, nant, ntimes, nfacets, cube, nx, ny, W, os, K, P, faceting;
+  int normalise;  // prediction: divide each facet's gathered value by the real part of its tap sum
   unsigned imaging_field;
   double u_scale, v_scale, gcx, gcy, wmax, ra0, dec0;
 };
@@ -114,7 +128,9 @@ __device__ __forceinline__ void atomic_add_c(vis_complex *dst, cplx v) {
   atomicAdd(&dst->im, (vis_real)v.im);
 }
 
-template <bool WPROJ>
+// PREDICT = false: the adjoint (grad_grid -> grad_vis, grad_jones).  PREDICT = true: prediction
+// (model grids in grad_grid -> visibilities in grad_vis).
+template <bool WPROJ, bool PREDICT>
 __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   FacetXform *fx = reinterpret_cast<FacetXform *>(smem_raw);
@@ -252,6 +268,8 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
       cplx myD[4];
 #pragma unroll
       for (int k = 0; k < 4; ++k) { myD[k].re = 0; myD[k].im = 0; }
+      acc_real myTS = 0;  // prediction: real part of the item's tap sum
+      const bool want_ts = PREDICT && a.normalise;
       unsigned todo = __ballot_sync(0xffffffffu, ok);
       while (todo) {
         const int it = __ffs(todo) - 1;
@@ -270,6 +288,7 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
         cplx D[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) { D[k].re = 0; D[k].im = 0; }
+        acc_real TS = 0;
         int ju = w2.x + lane % ww, jv = w2.x + lane / ww;
         const int sju = 32 % ww, sjv = 32 / ww, wend = w2.y + 1;
         for (; jv < wend; ju += sju, jv += sjv) {
@@ -281,6 +300,7 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
           const cplx tap =
               cmul(tap_at<WPROJ>(a.conv, fu + (long long)ju * a.os), tap_at<WPROJ>(a.conv, fv + (long long)jv * a.os));
           const cplx ct = cconj(tap);
+          if (want_ts) TS += tap.re;
           const long long cidx = (long long)(v0 + jv) * a.nx + (u0 + ju);
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
@@ -299,12 +319,46 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
             D[k].im += __shfl_xor_sync(0xffffffffu, D[k].im, off);
           }
         }
+        if (want_ts) {
+#pragma unroll
+          for (int off = 16; off > 0; off >>= 1) TS += __shfl_xor_sync(0xffffffffu, TS, off);
+        }
         if (lane == it) {
 #pragma unroll
           for (int k = 0; k < 4; ++k) myD[k] = D[k];
+          myTS = TS;
         }
       }
       if (!ok) continue;
+      if (PREDICT) {
+        // V' = D or conj(D) (w < 0), normalised by the tap sum; M = e^{-i phi} V'; V += J_p M J_q^H
+        const acc_real inv = (want_ts && myTS != (acc_real)0) ? (acc_real)1 / myTS : (acc_real)1;
+        const cplx cph = cconj(ph);
+        cplx X[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          cplx v = cell.flip ? cconj(myD[k]) : myD[k];
+          v.re *= inv;
+          v.im *= inv;
+          X[k] = cmul(cph, v);
+        }
+        if (a.jones) {
+          cplx Pm[4], Qm[4], T[4], O[4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            Pm[k].re = a.jones[i1 + k].re; Pm[k].im = a.jones[i1 + k].im;
+            Qm[k].re = a.jones[i2 + k].re; Qm[k].im = a.jones[i2 + k].im;
+          }
+          mat2(Pm, false, X, false, T);  // J_p M
+          mat2(T, false, Qm, true, O);   // (J_p M) J_q^H
+#pragma unroll
+          for (int k = 0; k < 4; ++k) gV[k] = cadd(gV[k], O[k]);
+        } else {
+#pragma unroll
+          for (int k = 0; k < 4; ++k) gV[k] = cadd(gV[k], X[k]);
+        }
+        continue;
+      }
       // chain rule back to V (and the Jones terms), each lane for its own item
       cplx Pm[4], Qm[4];
       if (a.jones) {
@@ -377,19 +431,8 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
   }
 }
 
-}  // namespace
-
-// See include/bullseye_gb300.h.  Every pointer is a device pointer (as for the allocation-free
-// gridding entry); jones_terms holds the raw (not inverted) terms or is null.
-extern "C" int bullseye_grid_adjoint(const gridding_parameters *params, const void *grad_grid, void *grad_vis,
-                                     void *grad_jones, int faceting, void *stream) {
-  if (!params || !grad_grid || !grad_vis) return BZ_ERR_INVALID_ARGUMENT;
-  const gridding_parameters &p = *params;
-  if (p.number_of_polarization_terms != 4 || p.number_of_polarization_terms_being_gridded != 4) return BZ_ERR_INVALID_ARGUMENT;
-  if (!p.visibilities || !p.uvw_coords || !p.visibility_weights || !p.flags || !p.flagged_rows || !p.field_array ||
-      !p.spw_index_array || !p.conv || !p.reference_wavelengths || !p.enabled_channels || !p.channel_grid_indicies)
-    return BZ_ERR_INVALID_ARGUMENT;
-  if (p.jones_terms && (!p.antenna_1_ids || !p.antenna_2_ids || !p.timestamp_ids)) return BZ_ERR_INVALID_ARGUMENT;
+// Arguments shared by the adjoint and the prediction (device pointers, sizes from the struct).
+AdjointArgs degrid_args(const gridding_parameters &p, int faceting) {
   AdjointArgs a;
   std::memset(&a, 0, sizeof a);
   a.vis = p.visibilities; a.weights = p.visibility_weights; a.flags = (const uint8_t *)p.flags;
@@ -398,9 +441,6 @@ extern "C" int bullseye_grid_adjoint(const gridding_parameters *params, const vo
   a.time_ids = p.timestamp_ids; a.jones = p.jones_terms;
   a.wavelengths = p.reference_wavelengths; a.enabled = (const uint8_t *)p.enabled_channels; a.cgi = p.channel_grid_indicies;
   a.conv = p.conv; a.facet_centres = p.facet_centres;
-  a.grad_grid = (const vis_complex *)grad_grid;
-  a.grad_vis = (vis_complex *)grad_vis;
-  a.grad_jones = p.jones_terms ? (vis_complex *)grad_jones : nullptr;
   a.nrows = (long long)p.row_count;
   a.nchan = (int)p.channel_count; a.nspw = (int)p.spw_count; a.nant = (int)p.antenna_count;
   a.ntimes = (int)p.no_timestamps_read;
@@ -420,24 +460,190 @@ extern "C" int bullseye_grid_adjoint(const gridding_parameters *params, const vo
   a.wmax = (double)(float)p.wmax_est;
   a.ra0 = (double)p.phase_centre_ra;
   a.dec0 = (double)p.phase_centre_dec;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  return a;
+}
+
+// Zeroes the output, then one persistent-style launch of the gather (32 items per warp pass).
+template <bool PREDICT>
+int launch_degrid(const AdjointArgs &a, bool wproj, cudaStream_t st) {
   const size_t smem = sizeof(FacetXform) * (size_t)a.nfacets + sizeof(int2) * (size_t)a.P;
   if (smem > 200 * 1024) return BZ_ERR_UNSUPPORTED;
-  if (cudaMemsetAsync(grad_vis, 0, sizeof(vis_complex) * (size_t)a.nrows * a.nchan * 4, st) != cudaSuccess) return BZ_ERR_CUDA;
+  if (cudaMemsetAsync(a.grad_vis, 0, sizeof(vis_complex) * (size_t)a.nrows * a.nchan * 4, st) != cudaSuccess) return BZ_ERR_CUDA;
   if (a.nrows == 0) return BZ_OK;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const long long warps_needed = (a.nrows * a.nchan + 31) / 32;  // 32 items per warp pass
   const long long blocks = std::min<long long>((warps_needed + 7) / 8, (long long)sms * 16);
-  if (p.wplanes > 1) {
-    if (smem > 48 * 1024 && cudaFuncSetAttribute(degrid_adjoint_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-      return BZ_ERR_CUDA;
-    degrid_adjoint_kernel<true><<<(unsigned)blocks, 256, smem, st>>>(a);
-  } else {
-    if (smem > 48 * 1024 && cudaFuncSetAttribute(degrid_adjoint_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-      return BZ_ERR_CUDA;
-    degrid_adjoint_kernel<false><<<(unsigned)blocks, 256, smem, st>>>(a);
-  }
+  auto kern = wproj ? degrid_adjoint_kernel<true, PREDICT> : degrid_adjoint_kernel<false, PREDICT>;
+  if (smem > 48 * 1024 && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return BZ_ERR_CUDA;
+  kern<<<(unsigned)blocks, 256, smem, st>>>(a);
   return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
+
+// Model images -> the FFT input: dst[s][y][x] = img[s][(y+ny/2)%ny][(x+nx/2)%nx] / (taper_x[x'] taper_y[y'])
+// at the source pixel (x', y') (numpy's ifftshift; the tapers are the gridding correction c(l) c(m)
+// that finalize divides by, or null).
+__global__ void predict_taper_shift_kernel(const vis_complex *__restrict__ img, vis_complex *__restrict__ dst, int nx,
+                                           int ny, long long slices, const double *__restrict__ taper_x,
+                                           const double *__restrict__ taper_y) {
+  const long long nxy = (long long)nx * ny, total = nxy * slices;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const long long s = i / nxy, r = i - s * nxy;
+    const int y = (int)(r / nx), x = (int)(r - (long long)y * nx);
+    const int sy = (y + ny / 2) % ny, sx = (x + nx / 2) % nx;
+    vis_complex v = img[s * nxy + (long long)sy * nx + sx];
+    if (taper_x) {
+      const double c = taper_x[sx] * taper_y[sy];
+      v.re = (vis_real)((double)v.re / c);
+      v.im = (vis_real)((double)v.im / c);
+    }
+    dst[i] = v;
+  }
+}
+
+// After the forward transform: numpy's fftshift, dst[y][x] = src[(y-ny/2)%ny][(x-nx/2)%nx].
+__global__ void predict_fftshift_kernel(const vis_complex *__restrict__ src, vis_complex *__restrict__ dst, int nx,
+                                        int ny, long long slices) {
+  const long long nxy = (long long)nx * ny, total = nxy * slices;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const long long s = i / nxy, r = i - s * nxy;
+    const int y = (int)(r / nx), x = (int)(r - (long long)y * nx);
+    const int sy = (y + ny - ny / 2) % ny, sx = (x + nx - nx / 2) % nx;
+    dst[i] = src[s * nxy + (long long)sy * nx + sx];
+  }
+}
+
+// Batched 2-D forward plans, one per (device, ny, nx, batch), kept for the life of the process.
+// Plans are shared by host threads: setting the stream and executing happen under the lock.
+std::mutex g_plan_mutex;
+std::map<std::tuple<int, int, int, int>, cufftHandle> g_plans;
+
+int forward_fft(vis_complex *data, int nx, int ny, int batch, cudaStream_t st) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(g_plan_mutex);
+  const auto key = std::make_tuple(dev, ny, nx, batch);
+  auto it = g_plans.find(key);
+  if (it == g_plans.end()) {
+    cufftHandle plan;
+    int dims[2] = {ny, nx};
+    const int dist = nx * ny;
+#if defined(BULLSEYE_SINGLE)
+    const cufftType type = CUFFT_C2C;
+#else
+    const cufftType type = CUFFT_Z2Z;
+#endif
+    if (cufftPlanMany(&plan, 2, dims, nullptr, 1, dist, nullptr, 1, dist, type, batch) != CUFFT_SUCCESS) return BZ_ERR_CUFFT;
+    it = g_plans.emplace(key, plan).first;
+  }
+  if (cufftSetStream(it->second, st) != CUFFT_SUCCESS) return BZ_ERR_CUFFT;
+#if defined(BULLSEYE_SINGLE)
+  const cufftResult r = cufftExecC2C(it->second, (cufftComplex *)data, (cufftComplex *)data, CUFFT_FORWARD);
+#else
+  const cufftResult r = cufftExecZ2Z(it->second, (cufftDoubleComplex *)data, (cufftDoubleComplex *)data, CUFFT_FORWARD);
+#endif
+  return r == CUFFT_SUCCESS ? BZ_OK : BZ_ERR_CUFFT;
+}
+
+constexpr int kPredictNormalise = 1;
+constexpr int kPredictFromGrid = 2;
+
+}  // namespace
+
+// See include/bullseye_gb300.h.  Every pointer is a device pointer (as for the allocation-free
+// gridding entry); jones_terms holds the raw (not inverted) terms or is null.
+extern "C" int bullseye_grid_adjoint(const gridding_parameters *params, const void *grad_grid, void *grad_vis,
+                                     void *grad_jones, int faceting, void *stream) {
+  const char *name = "bullseye_grid_adjoint";
+  if (!params || !grad_grid || !grad_vis) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: params, grad_grid and grad_vis are required", name);
+    return BZ_ERR_INVALID_ARGUMENT;
+  }
+  const gridding_parameters &p = *params;
+  if (p.number_of_polarization_terms != 4 || p.number_of_polarization_terms_being_gridded != 4 || !p.visibilities ||
+      !p.uvw_coords || !p.visibility_weights || !p.flags || !p.flagged_rows || !p.field_array || !p.spw_index_array ||
+      !p.conv || !p.reference_wavelengths || !p.enabled_channels || !p.channel_grid_indicies ||
+      (p.jones_terms && (!p.antenna_1_ids || !p.antenna_2_ids || !p.timestamp_ids))) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: four polarisation terms and the row and table arrays are required", name);
+    return BZ_ERR_INVALID_ARGUMENT;
+  }
+  AdjointArgs a = degrid_args(p, faceting);
+  a.grad_grid = (const vis_complex *)grad_grid;
+  a.grad_vis = (vis_complex *)grad_vis;
+  a.grad_jones = p.jones_terms ? (vis_complex *)grad_jones : nullptr;
+  const int rc = launch_degrid<false>(a, p.wplanes > 1, static_cast<cudaStream_t>(stream));
+  if (rc != BZ_OK) bz_record_error(rc, "%s: launch failed (status %d)", name, rc);
+  return rc;
+}
+
+// See include/bullseye_gb300.h.
+extern "C" size_t bullseye_predict_ws_bytes(const gridding_parameters *params) {
+  if (!params) return 0;
+  const gridding_parameters &p = *params;
+  const size_t F = p.num_facet_centres ? p.num_facet_centres : 1;
+  return 2 * F * p.cube_channel_dim_size * 4 * p.nx * p.ny * sizeof(vis_complex);
+}
+
+// See include/bullseye_gb300.h.
+extern "C" int bullseye_predict(const gridding_parameters *params, const void *model, const double *taper_x,
+                                const double *taper_y, int faceting, int flags, void *vis_out, void *workspace,
+                                size_t ws_bytes, void *stream) {
+  const char *name = "bullseye_predict";
+  if (!params || !model || !vis_out) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: params, model and vis_out are required", name);
+    return BZ_ERR_INVALID_ARGUMENT;
+  }
+  const gridding_parameters &p = *params;
+  if (p.number_of_polarization_terms != 4 || p.number_of_polarization_terms_being_gridded != 4 || !p.uvw_coords ||
+      !p.spw_index_array || !p.conv || !p.reference_wavelengths || !p.enabled_channels || !p.channel_grid_indicies ||
+      (p.jones_terms && (!p.antenna_1_ids || !p.antenna_2_ids || !p.timestamp_ids)) || p.nx == 0 || p.ny == 0 ||
+      p.cube_channel_dim_size == 0 || p.conv_oversample == 0 || (flags & ~(kPredictNormalise | kPredictFromGrid))) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: four polarisation terms, uvw, spw and the tables are required", name);
+    return BZ_ERR_INVALID_ARGUMENT;
+  }
+  if ((taper_x == nullptr) != (taper_y == nullptr)) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: give both gridding-correction tapers or neither", name);
+    return BZ_ERR_INVALID_ARGUMENT;
+  }
+  const bool from_grid = (flags & kPredictFromGrid) != 0;
+  const size_t need = from_grid ? 0 : bullseye_predict_ws_bytes(params);
+  if (need && (!workspace || ws_bytes < need || (reinterpret_cast<uintptr_t>(workspace) & 255))) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: workspace of %zu bytes at %p, need %zu bytes 256-byte aligned", name,
+                    ws_bytes, workspace, need);
+    return BZ_ERR_INVALID_ARGUMENT;
+  }
+  const size_t F = p.num_facet_centres ? p.num_facet_centres : 1;
+  const long long slices = (long long)(F * p.cube_channel_dim_size * 4);
+  if (!from_grid && ((long long)p.nx * (long long)p.ny > 0x7fffffffLL || slices > 0x7fffffffLL)) {
+    bz_record_error(BZ_ERR_UNSUPPORTED, "%s: %lld model slices of %zu x %zu exceed one batched transform", name, slices,
+                    p.nx, p.ny);
+    return BZ_ERR_UNSUPPORTED;
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const vis_complex *grids = static_cast<const vis_complex *>(model);
+  if (!from_grid) {
+    vis_complex *buf = static_cast<vis_complex *>(workspace);
+    vis_complex *out = buf + (size_t)slices * p.nx * p.ny;
+    predict_taper_shift_kernel<<<2048, 256, 0, st>>>(grids, buf, (int)p.nx, (int)p.ny, slices, taper_x, taper_y);
+    int rc = cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+    if (rc == BZ_OK) rc = forward_fft(buf, (int)p.nx, (int)p.ny, (int)slices, st);
+    if (rc == BZ_OK) {
+      predict_fftshift_kernel<<<2048, 256, 0, st>>>(buf, out, (int)p.nx, (int)p.ny, slices);
+      rc = cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+    }
+    if (rc != BZ_OK) {
+      bz_record_error(rc, "%s: model transform failed (status %d)", name, rc);
+      return rc;
+    }
+    grids = out;
+  }
+  AdjointArgs a = degrid_args(p, faceting);
+  a.grad_grid = grids;
+  a.grad_vis = static_cast<vis_complex *>(vis_out);
+  a.normalise = (flags & kPredictNormalise) ? 1 : 0;
+  const int rc = launch_degrid<true>(a, p.wplanes > 1, st);
+  if (rc != BZ_OK) bz_record_error(rc, "%s: launch failed (status %d)", name, rc);
+  return rc;
 }

@@ -1012,31 +1012,46 @@ SupportWs support_ws_layout(long long R, int nchan, int nslots, int P, int os, i
   return l;
 }
 
+// Thread layout of one support class of the workspace form: J = 4 (J = 8 where the J = 4 layout
+// needs more than 512 threads), fixed so that concurrent calls share no tuning state.
 template <bool WPROJ, bool COMP>
-bool support_aware_launches(const GridArgs &a, const ClassList &cl, int nfacets, int *class_count, int *class_off,
-                            int *work_next, cudaStream_t st) {
-  for (int k = 0; k < cl.n; ++k) {
-    const int W = cl.w[k];
-    Variant v;
-    bool have = false;
-    for (int J : {4, 8})
-      if (!have) have = make_variant<4, WPROJ>(W, J, false, kSegRegs<4>, v) && finish_variant<4, WPROJ, COMP>(v);
-    if (!have) have = make_variant<4, WPROJ>(W, 8, true, kSegRegs<8>, v) && finish_variant<4, WPROJ, COMP>(v);
-    if (!have) {
-      bz_record_error(BZ_ERR_UNSUPPORTED, "support-aware gridding: no layout for class width %d", W);
+bool support_aware_variant(int W, Variant &v) {
+  for (int J : {4, 8})
+    if (make_variant<4, WPROJ>(W, J, false, kSegRegs<4>, v) && finish_variant<4, WPROJ, COMP>(v)) return true;
+  return make_variant<4, WPROJ>(W, 8, true, kSegRegs<8>, v) && finish_variant<4, WPROJ, COMP>(v);
+}
+
+template <bool WPROJ, bool COMP>
+bool support_aware_layouts(const ClassList &cl, Variant *vs) {
+  for (int k = 0; k < cl.n; ++k)
+    if (!support_aware_variant<WPROJ, COMP>(cl.w[k], vs[k])) {
+      bz_record_error(BZ_ERR_UNSUPPORTED, "support-aware gridding: no layout for class width %d", cl.w[k]);
       return false;
     }
+  return true;
+}
+
+bool support_aware_layouts(const ClassList &cl, bool wproj, bool comp, Variant *vs) {
+#if defined(BULLSEYE_SINGLE)
+  if (comp) return wproj ? support_aware_layouts<true, true>(cl, vs) : support_aware_layouts<false, true>(cl, vs);
+#else
+  (void)comp;
+#endif
+  return wproj ? support_aware_layouts<true, false>(cl, vs) : support_aware_layouts<false, false>(cl, vs);
+}
+
+template <bool WPROJ, bool COMP>
+bool support_aware_launches(const GridArgs &a, const ClassList &cl, const Variant *vs, int nfacets, int *class_count,
+                            int *class_off, int *work_next, cudaStream_t st) {
+  for (int k = 0; k < cl.n; ++k) {
+    const Variant &v = vs[k];
     GridArgs ak = a;
-    ak.W = W;
+    ak.W = cl.w[k];
     ak.V = v.V;
     ak.segment_base = class_off + k;
     ak.work_count = class_count + k;
     ak.work_next = work_next + k;
     auto kern = seg_kernel<4, WPROJ, COMP>(v.J, v.wide, v.regs);
-    if (!open_smem(kern)) {
-      bz_record_error(BZ_ERR_CUDA, "support-aware gridding: cudaFuncSetAttribute failed");
-      return false;
-    }
     if (cudaMemsetAsync(work_next + k, 0, sizeof(int), st) != cudaSuccess) return false;
     kern<<<v.grid, v.NT, v.smem, st>>>(ak, nfacets);
     if (cudaGetLastError() != cudaSuccess) return false;
@@ -1044,10 +1059,30 @@ bool support_aware_launches(const GridArgs &a, const ClassList &cl, int nfacets,
   return true;
 }
 
+ClassList candidate_classes(int W) {
+  const std::vector<int> cand = class_candidates(W);
+  ClassList cl;
+  cl.n = (int)cand.size();
+  for (int i = 0; i < cl.n; ++i) cl.w[i] = cand[i];
+  return cl;
+}
+
 }  // namespace
 
 size_t bz_support_aware_ws_bytes(long long rows, int nchan, int nslots, int P, int os, int W, bool wproj) {
   return support_ws_layout(rows, nchan, nslots, P, os, W, wproj).bytes;
+}
+
+bool bz_support_aware_check(const GridArgs &a, size_t bytes) {
+  const bool wproj = a.P > 1;
+  const SupportWs l = support_ws_layout(a.nrows, a.nchan, a.nslots, a.P, a.os, a.W, wproj);
+  if (bytes < l.bytes) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "support-aware gridding: workspace of %zu bytes, need %zu", bytes, l.bytes);
+    return false;
+  }
+  const ClassList cl = candidate_classes(a.W);
+  Variant vs[kMaxClasses];
+  return support_aware_layouts(cl, wproj, a.grid_lo != nullptr, vs);
 }
 
 bool bz_grid_support_aware(const GridArgs &a_in, int nfacets, unsigned char *ws, size_t bytes, cudaStream_t st) {
@@ -1058,10 +1093,10 @@ bool bz_grid_support_aware(const GridArgs &a_in, int nfacets, unsigned char *ws,
     bz_record_error(BZ_ERR_INVALID_ARGUMENT, "support-aware gridding: workspace of %zu bytes, need %zu", bytes, l.bytes);
     return false;
   }
-  const std::vector<int> cand = class_candidates(W);
-  ClassList cl;
-  cl.n = (int)cand.size();
-  for (int i = 0; i < cl.n; ++i) cl.w[i] = cand[i];
+  const ClassList cl = candidate_classes(W);
+  Variant vs[kMaxClasses];
+  const bool comp = a_in.grid_lo != nullptr;
+  if (!support_aware_layouts(cl, wproj, comp, vs)) return false;
   int *plane_class = reinterpret_cast<int *>(ws + l.plane_class);
   int *plane_lo = reinterpret_cast<int *>(ws + l.plane_lo);
   int *plane_w = reinterpret_cast<int *>(ws + l.plane_w);
@@ -1102,14 +1137,11 @@ bool bz_grid_support_aware(const GridArgs &a_in, int nfacets, unsigned char *ws,
   a.conv_w_stride = l.L;
   a.segments = sorted;
   a.segment_capacity = l.maxseg;
-  const bool comp = a.grid_lo != nullptr;
 #if defined(BULLSEYE_SINGLE)
   if (comp)
-    return wproj ? support_aware_launches<true, true>(a, cl, nfacets, class_count, class_off, work_next, st)
-                 : support_aware_launches<false, true>(a, cl, nfacets, class_count, class_off, work_next, st);
-#else
-  (void)comp;
+    return wproj ? support_aware_launches<true, true>(a, cl, vs, nfacets, class_count, class_off, work_next, st)
+                 : support_aware_launches<false, true>(a, cl, vs, nfacets, class_count, class_off, work_next, st);
 #endif
-  return wproj ? support_aware_launches<true, false>(a, cl, nfacets, class_count, class_off, work_next, st)
-               : support_aware_launches<false, false>(a, cl, nfacets, class_count, class_off, work_next, st);
+  return wproj ? support_aware_launches<true, false>(a, cl, vs, nfacets, class_count, class_off, work_next, st)
+               : support_aware_launches<false, false>(a, cl, vs, nfacets, class_count, class_off, work_next, st);
 }

@@ -189,26 +189,18 @@ __device__ __forceinline__ void jmul(const cplx *A, const cplx *B, cplx *O) {
   O[3].re = t6.re + t7.re; O[3].im = t6.im + t7.im;
 }
 
-// Phase factor e^{i x} for an FP64 argument.  The single-precision library reduces x to
-// [-pi, pi] in FP64 and evaluates sincosf on the reduced value; the double library uses sincos.
+// Phase factor e^{i x} for an FP64 argument (double-precision library; the single-precision
+// library evaluates sincospif on the argument reduced to turns, in choose_cells).
+#if !defined(BULLSEYE_SINGLE)
 __device__ __forceinline__ cplx phase_factor(double x) {
   cplx r;
-#if defined(BULLSEYE_SINGLE)
-  const double two_pi = 6.283185307179586476925286766559;
-  double n = rint(x * (1.0 / two_pi));
-  double red = fma(-n, two_pi, x);
-  float s, c;
-  sincosf((float)red, &s, &c);
-  r.re = c;
-  r.im = s;
-#else
   double s, c;
   sincos(x, &s, &c);
   r.re = c;
   r.im = s;
-#endif
   return r;
 }
+#endif
 
 // Flush one owned cell's register accumulator into the grid.  Compensated mode adds with
 // atomics that return the previous value, then recovers each addition's rounding error exactly

@@ -24,12 +24,15 @@
 #include <cstring>
 
 #include <algorithm>
+#include <atomic>
+#include <mutex>
 
 #include "common.h"
 #include "gridder.cuh"
 
 // Support-aware form of the batched gridder (batched.cu), used by the workspace entry.
 size_t bz_support_aware_ws_bytes(long long rows, int nchan, int nslots, int P, int os, int W, bool wproj);
+bool bz_support_aware_check(const bz::GridArgs &a, size_t bytes);
 bool bz_grid_support_aware(const bz::GridArgs &a, int nfacets, unsigned char *ws, size_t bytes, cudaStream_t st);
 
 using namespace bz;
@@ -42,8 +45,10 @@ using namespace bz;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[BZ_NOALLOC_SCRATCH_BYTES];
 
 // Device address of g_noalloc_scratch per device, resolved once with that device current.  In
-// host code the symbol is only a host-side stand-in, never a device address.
-static void *g_noalloc_addr[BZ_NOALLOC_MAX_DEVICES];
+// host code the symbol is only a host-side stand-in, never a device address.  Host threads may
+// call concurrently: the addresses are atomics and the first resolution per device is serialised.
+static std::atomic<void *> g_noalloc_addr[BZ_NOALLOC_MAX_DEVICES];
+static std::mutex g_noalloc_resolve_mutex;
 
 namespace {
 
@@ -181,55 +186,44 @@ struct Workspace {
   size_t sched_bytes = 0;
 };
 
-int grid_4cor_jones(const gridding_parameters &p, const Workspace &ws, void *stream) {
+// Every rejection happens before the first launch, so a rejected call leaves the caller's arrays
+// (jones_terms included) untouched.  Only a launch failure reported by the runtime after the Jones
+// inversion was queued (the device is then unusable anyway) returns with the terms inverted.
+int grid_4cor_jones(const gridding_parameters &p, const Workspace &ws, void *stream, const char *name) {
   const size_t F = p.num_facet_centres ? p.num_facet_centres : 1;
   const size_t nxy = p.nx * p.ny;
   const size_t grid_elems = F * p.cube_channel_dim_size * 4 * nxy;
   const int W = (int)(2 * p.conv_support + 1);
   const bool wproj = p.wplanes > 1;
-  if (p.number_of_polarization_terms_being_gridded != 4 || p.number_of_polarization_terms != 4) return BZ_ERR_INVALID_ARGUMENT;
+  if (p.number_of_polarization_terms_being_gridded != 4 || p.number_of_polarization_terms != 4) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: four polarisation terms are gridded", name);
+    return BZ_ERR_INVALID_ARGUMENT;
+  }
   if (!p.visibilities || !p.uvw_coords || !p.visibility_weights || !p.flags || !p.flagged_rows || !p.field_array ||
       !p.spw_index_array || !p.antenna_1_ids || !p.antenna_2_ids || !p.timestamp_ids || !p.jones_terms || !p.conv ||
       !p.reference_wavelengths || !p.enabled_channels || !p.channel_grid_indicies || !p.output_buffer ||
-      !p.normalization_terms)
+      !p.normalization_terms) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: a required device array is null", name);
     return BZ_ERR_INVALID_ARGUMENT;
+  }
   if (p.nx == 0 || p.ny == 0 || p.channel_count == 0 || p.spw_count == 0 || p.conv_oversample == 0 ||
-      p.cube_channel_dim_size == 0)
+      p.cube_channel_dim_size == 0) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: nx, ny, channels, spws, oversampling and cube must be > 0", name);
     return BZ_ERR_INVALID_ARGUMENT;
+  }
 #if defined(BULLSEYE_SINGLE)
   if (grid_elems * sizeof(vis_complex) > ws.lo_bytes) {
     bz_record_error(BZ_ERR_UNSUPPORTED,
-                    "bullseye_facet_4_cor_corrections_noalloc: %zu grid cells need %zu bytes of compensation scratch, "
-                    "more than the fixed %u-byte scratch array",
-                    grid_elems, grid_elems * sizeof(vis_complex), (unsigned)BZ_NOALLOC_LO_BYTES);
+                    "%s: %zu grid cells need %zu bytes of compensation scratch, more than the %zu bytes available "
+                    "(the fixed scratch array of the allocation-free entry)",
+                    name, grid_elems, grid_elems * sizeof(vis_complex), ws.lo_bytes);
     return BZ_ERR_UNSUPPORTED;
   }
 #endif
   if (F * sizeof(FacetXform) > ws.table_bytes) {
-    bz_record_error(BZ_ERR_UNSUPPORTED, "bullseye_facet_4_cor_corrections_noalloc: %zu facets exceed the scratch facet table", F);
+    bz_record_error(BZ_ERR_UNSUPPORTED, "%s: %zu facets exceed the scratch facet table", name, F);
     return BZ_ERR_UNSUPPORTED;
   }
-  if (noalloc_shape<true>(W).NT > 512) {
-    bz_record_error(BZ_ERR_UNSUPPORTED, "bullseye_facet_4_cor_corrections_noalloc: full support %d is not supported", W);
-    return BZ_ERR_UNSUPPORTED;
-  }
-
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  vis_complex *lo = ws.lo;
-  FacetXform *table = ws.table;
-  int *err = ws.err;
-#if defined(BULLSEYE_SINGLE)
-  if (cudaMemsetAsync(lo, 0, grid_elems * sizeof(vis_complex), st) != cudaSuccess) return BZ_ERR_CUDA;
-#endif
-  if (cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess) return BZ_ERR_CUDA;
-  noalloc_facet_table_kernel<<<(unsigned)((F + 127) / 128), 128, 0, st>>>(
-      table, p.facet_centres, (int)F, (double)p.phase_centre_ra, (double)p.phase_centre_dec, (int)p.nx, (int)p.ny,
-      (double)p.nx * (double)p.cell_size_x * (double)kArcsecToRad,
-      -((double)p.ny * (double)p.cell_size_y * (double)kArcsecToRad), (double)(p.nx / 2 - p.conv_support),
-      (double)(p.ny / 2 - p.conv_support), (long long)(p.cube_channel_dim_size * 4 * nxy));
-  const long long nj = (long long)(p.no_timestamps_read * p.antenna_count * F * p.spw_count * p.channel_count);
-  if (nj > 0) noalloc_invert_kernel<<<(unsigned)((nj + 255) / 256), 256, 0, st>>>(p.jones_terms, nj, err);
-  if (p.row_count == 0) return BZ_OK;
 
   GridArgs a;
   std::memset(&a, 0, sizeof a);
@@ -237,17 +231,17 @@ int grid_4cor_jones(const gridding_parameters &p, const Workspace &ws, void *str
   a.uvw = (const vis_real *)p.uvw_coords; a.flagged_rows = (const uint8_t *)p.flagged_rows;
   a.field = p.field_array; a.spw = p.spw_index_array; a.ant1 = p.antenna_1_ids; a.ant2 = p.antenna_2_ids;
   a.time_ids = p.timestamp_ids;
-  a.jones_inv = p.jones_terms;  // inverted in place above
+  a.jones_inv = p.jones_terms;  // inverted in place before gridding
   a.starts = p.baseline_starting_indexes;
   a.wavelengths = p.reference_wavelengths; a.enabled = (const uint8_t *)p.enabled_channels; a.cgi = p.channel_grid_indicies;
   a.conv = p.conv;
-  a.facets = table;
+  a.facets = ws.table;
   a.grid = p.output_buffer;
 #if defined(BULLSEYE_SINGLE)
-  a.grid_lo = lo;
+  a.grid_lo = ws.lo;
 #endif
   a.norm = p.normalization_terms;
-  a.error = err;
+  a.error = ws.err;
   a.nrows = (long long)p.row_count;
   a.nchan = (int)p.channel_count; a.npol = 4; a.pol0 = 0; a.pol1 = 0;
   a.nspw = (int)p.spw_count; a.nant = (int)p.antenna_count; a.ntimes = (int)p.no_timestamps_read;
@@ -270,18 +264,104 @@ int grid_4cor_jones(const gridding_parameters &p, const Workspace &ws, void *str
   a.gcy = (double)(p.ny / 2 - p.conv_support);
   a.wmax = (double)(float)p.wmax_est;
   const long long blocks = (long long)F * a.nslots * (long long)a.nchan;
-  if (blocks > 0x7fffffffLL) return BZ_ERR_UNSUPPORTED;
+  if (p.row_count > 0) {
+    if (ws.sched) {
+      // workspace entry: persistent per-class launches (no limit on work items); the workspace size
+      // and a thread layout for every class width are checked here
+      if (!bz_support_aware_check(a, ws.sched_bytes)) return bz_error_code() ? bz_error_code() : BZ_ERR_UNSUPPORTED;
+    } else {
+      // plain entry: one CTA per (facet, track, channel)
+      if (blocks > 0x7fffffffLL) {
+        bz_record_error(BZ_ERR_UNSUPPORTED, "%s: %lld (facet, track, channel) work items exceed one launch", name, blocks);
+        return BZ_ERR_UNSUPPORTED;
+      }
+      if ((wproj ? noalloc_shape<true>(W) : noalloc_shape<false>(W)).NT > 512) {
+        bz_record_error(BZ_ERR_UNSUPPORTED, "%s: full support %d is not supported", name, W);
+        return BZ_ERR_UNSUPPORTED;
+      }
+    }
+  }
+
+  // launches
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+#if defined(BULLSEYE_SINGLE)
+  if (cudaMemsetAsync(ws.lo, 0, grid_elems * sizeof(vis_complex), st) != cudaSuccess) return BZ_ERR_CUDA;
+#endif
+  if (cudaMemsetAsync(ws.err, 0, sizeof(int), st) != cudaSuccess) return BZ_ERR_CUDA;
+  noalloc_facet_table_kernel<<<(unsigned)((F + 127) / 128), 128, 0, st>>>(
+      ws.table, p.facet_centres, (int)F, (double)p.phase_centre_ra, (double)p.phase_centre_dec, (int)p.nx, (int)p.ny,
+      a.u_scale, a.v_scale, a.gcx, a.gcy, (long long)(p.cube_channel_dim_size * 4 * nxy));
+  if (cudaGetLastError() != cudaSuccess) return BZ_ERR_CUDA;
+  const long long nj = (long long)(p.no_timestamps_read * p.antenna_count * F * p.spw_count * p.channel_count);
+  if (nj > 0) noalloc_invert_kernel<<<(unsigned)((nj + 255) / 256), 256, 0, st>>>(p.jones_terms, nj, ws.err);
+  if (cudaGetLastError() != cudaSuccess) return BZ_ERR_CUDA;
+  if (p.row_count == 0) return BZ_OK;
   if (ws.sched) {
     // workspace entry: support-aware (each w plane's nonzero window only; the same grids)
     if (!bz_grid_support_aware(a, (int)F, ws.sched, ws.sched_bytes, st)) return bz_error_code() ? bz_error_code() : BZ_ERR_CUDA;
   } else if (!(wproj ? noalloc_dispatch<true>(a, blocks, st) : noalloc_dispatch<false>(a, blocks, st))) {
+    bz_record_error(BZ_ERR_CUDA, "%s: gridder launch failed", name);
     return BZ_ERR_CUDA;
   }
 #if defined(BULLSEYE_SINGLE)
-  noalloc_fold_kernel<<<1024, 256, 0, st>>>(p.output_buffer, lo, (long long)grid_elems);
+  noalloc_fold_kernel<<<1024, 256, 0, st>>>(p.output_buffer, ws.lo, (long long)grid_elems);
   if (cudaGetLastError() != cudaSuccess) return BZ_ERR_CUDA;
 #endif
   return BZ_OK;
+}
+
+// Maps the error bits of a call's error word to the library's sticky error (as the regular entry
+// points do when they synchronise); returns the first status, 0 when the word is clear.
+int report_device_error(int h, const char *name) {
+  if (!h) return BZ_OK;
+  if (h & DEV_ERR_SINGULAR) bz_record_error(BZ_ERR_SINGULAR_JONES, "%s: Jones matrix set contains singular matrices", name);
+  if (h & DEV_ERR_GRID_INDEX)
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: channel grid index, spw or schedule entry out of range", name);
+  if (h & DEV_ERR_JONES_INDEX)
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: timestamp or antenna id out of range of the Jones terms", name);
+  if (h & DEV_ERR_WAIT_TIMEOUT) bz_record_error(BZ_ERR_CUDA, "%s: a bounded wait for staged kernel taps ran out", name);
+  if (h & DEV_ERR_SINGULAR) return BZ_ERR_SINGULAR_JONES;
+  if (h & (DEV_ERR_GRID_INDEX | DEV_ERR_JONES_INDEX)) return BZ_ERR_INVALID_ARGUMENT;
+  return BZ_ERR_CUDA;
+}
+
+// Device address of the scratch array on the current device (resolved on the first call there).
+// Resolution loads the module's symbol table, which a stream capture does not allow: a first call
+// made while `st` is capturing is rejected.
+unsigned char *noalloc_scratch(cudaStream_t st, bool resolve, const char *name) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= BZ_NOALLOC_MAX_DEVICES) {
+    bz_record_error(BZ_ERR_CUDA, "%s: no current CUDA device below %d", name, BZ_NOALLOC_MAX_DEVICES);
+    return nullptr;
+  }
+  void *ptr = g_noalloc_addr[dev].load(std::memory_order_acquire);
+  if (ptr || !resolve) return static_cast<unsigned char *>(ptr);
+  std::lock_guard<std::mutex> lk(g_noalloc_resolve_mutex);
+  ptr = g_noalloc_addr[dev].load(std::memory_order_acquire);
+  if (ptr) return static_cast<unsigned char *>(ptr);
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    bz_record_error(BZ_ERR_UNSUPPORTED, "%s: the first call on a device must come before any stream capture", name);
+    return nullptr;
+  }
+  const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+  if (e != cudaSuccess || !ptr) {
+    bz_record_error(BZ_ERR_CUDA, "%s: cudaGetSymbolAddress of the scratch array failed (%s)", name, cudaGetErrorString(e));
+    return nullptr;
+  }
+  g_noalloc_addr[dev].store(ptr, std::memory_order_release);
+  return static_cast<unsigned char *>(ptr);
+}
+
+Workspace noalloc_workspace(unsigned char *scratch) {
+  Workspace ws;
+  ws.lo = reinterpret_cast<vis_complex *>(scratch);
+  ws.lo_bytes = BZ_NOALLOC_LO_BYTES;
+  ws.table = reinterpret_cast<FacetXform *>(scratch + BZ_NOALLOC_LO_BYTES);
+  ws.table_bytes = BZ_NOALLOC_TABLE_BYTES - 256;
+  ws.err = reinterpret_cast<int *>(scratch + BZ_NOALLOC_LO_BYTES + BZ_NOALLOC_TABLE_BYTES - 256);
+  return ws;
 }
 
 }  // namespace
@@ -289,27 +369,13 @@ int grid_4cor_jones(const gridding_parameters &p, const Workspace &ws, void *str
 // See include/bullseye_gb300.h.  Every pointer in *params is a device pointer; returns 0 when
 // the work was queued on `stream`, or a bz_status code (nothing queued) when the arguments are
 // rejected.  The first call on each device resolves the scratch array's device address
-// (cudaGetSymbolAddress) and should therefore come before any stream capture on that device.
+// (cudaGetSymbolAddress) and must therefore come before any stream capture on that device.
 extern "C" int bullseye_facet_4_cor_corrections_noalloc(const gridding_parameters *params, void *stream) {
+  const char *name = "bullseye_facet_4_cor_corrections_noalloc";
   if (!params) return BZ_ERR_INVALID_ARGUMENT;
-  const gridding_parameters &p = *params;
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= BZ_NOALLOC_MAX_DEVICES) return BZ_ERR_CUDA;
-  if (!g_noalloc_addr[dev]) {
-    void *ptr = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-    if (e != cudaSuccess || !ptr) return BZ_ERR_CUDA;
-    g_noalloc_addr[dev] = ptr;
-  }
-  unsigned char *scratch = static_cast<unsigned char *>(g_noalloc_addr[dev]);
-
-  Workspace ws;
-  ws.lo = reinterpret_cast<vis_complex *>(scratch);
-  ws.lo_bytes = BZ_NOALLOC_LO_BYTES;
-  ws.table = reinterpret_cast<FacetXform *>(scratch + BZ_NOALLOC_LO_BYTES);
-  ws.table_bytes = BZ_NOALLOC_TABLE_BYTES - 256;
-  ws.err = reinterpret_cast<int *>(scratch + BZ_NOALLOC_LO_BYTES + BZ_NOALLOC_TABLE_BYTES - 256);
-  return grid_4cor_jones(p, ws, stream);
+  unsigned char *scratch = noalloc_scratch(static_cast<cudaStream_t>(stream), true, name);
+  if (!scratch) return bz_error_code() ? bz_error_code() : BZ_ERR_CUDA;
+  return grid_4cor_jones(*params, noalloc_workspace(scratch), stream, name);
 }
 
 // Bytes of caller workspace bullseye_facet_4_cor_corrections_ws needs for these parameters.
@@ -340,19 +406,9 @@ extern "C" size_t bullseye_facet_4_cor_corrections_ws_bytes(const gridding_param
   return ws_lo_bytes(*params) + ws_table_bytes(*params) + 256 + ws_sched_bytes(*params);
 }
 
-// See include/bullseye_gb300.h.
-extern "C" int bullseye_facet_4_cor_corrections_ws(const gridding_parameters *params, void *workspace, size_t bytes,
-                                                   void *stream) {
-  if (!params || !workspace) return BZ_ERR_INVALID_ARGUMENT;
-  const gridding_parameters &p = *params;
-  const size_t need = bullseye_facet_4_cor_corrections_ws_bytes(params);
-  if (bytes < need || (reinterpret_cast<uintptr_t>(workspace) & 255)) {
-    bz_record_error(BZ_ERR_INVALID_ARGUMENT,
-                    "bullseye_facet_4_cor_corrections_ws: workspace of %zu bytes at %p, need %zu bytes 256-byte aligned",
-                    bytes, workspace, need);
-    return BZ_ERR_INVALID_ARGUMENT;
-  }
-  unsigned char *w = static_cast<unsigned char *>(workspace);
+// Workspace pieces of bullseye_facet_4_cor_corrections_ws: compensation grid, facet table, error
+// word, support-aware schedule.
+static Workspace caller_workspace(const gridding_parameters &p, unsigned char *w) {
   Workspace ws;
   ws.lo = reinterpret_cast<vis_complex *>(w);
   ws.lo_bytes = ws_lo_bytes(p);
@@ -361,6 +417,50 @@ extern "C" int bullseye_facet_4_cor_corrections_ws(const gridding_parameters *pa
   ws.err = reinterpret_cast<int *>(w + ws.lo_bytes + ws.table_bytes);
   ws.sched = w + ws.lo_bytes + ws.table_bytes + 256;
   ws.sched_bytes = ws_sched_bytes(p);
-  return grid_4cor_jones(p, ws, stream);
+  return ws;
 }
 
+// See include/bullseye_gb300.h.
+extern "C" int bullseye_facet_4_cor_corrections_ws(const gridding_parameters *params, void *workspace, size_t bytes,
+                                                   void *stream) {
+  const char *name = "bullseye_facet_4_cor_corrections_ws";
+  if (!params || !workspace) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: params and workspace are required", name);
+    return BZ_ERR_INVALID_ARGUMENT;
+  }
+  const size_t need = bullseye_facet_4_cor_corrections_ws_bytes(params);
+  if (bytes < need || (reinterpret_cast<uintptr_t>(workspace) & 255)) {
+    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: workspace of %zu bytes at %p, need %zu bytes 256-byte aligned", name,
+                    bytes, workspace, need);
+    return BZ_ERR_INVALID_ARGUMENT;
+  }
+  return grid_4cor_jones(*params, caller_workspace(*params, static_cast<unsigned char *>(workspace)), stream, name);
+}
+
+// See include/bullseye_gb300.h.
+extern "C" int bullseye_facet_4_cor_corrections_status(const gridding_parameters *params, const void *workspace,
+                                                       void *stream) {
+  const char *name = workspace ? "bullseye_facet_4_cor_corrections_ws" : "bullseye_facet_4_cor_corrections_noalloc";
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int *err = nullptr;
+  if (workspace) {
+    if (!params) {
+      bz_record_error(BZ_ERR_INVALID_ARGUMENT, "bullseye_facet_4_cor_corrections_status: params are required");
+      return BZ_ERR_INVALID_ARGUMENT;
+    }
+    err = caller_workspace(*params, static_cast<unsigned char *>(const_cast<void *>(workspace))).err;
+  } else {
+    unsigned char *scratch = noalloc_scratch(st, false, name);
+    if (!scratch) return bz_error_code();  // no call on this device yet: nothing to report
+    err = noalloc_workspace(scratch).err;
+  }
+  int h = 0;
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && h) e = cudaMemset(err, 0, sizeof(int));
+  if (e != cudaSuccess) {
+    bz_record_error(BZ_ERR_CUDA, "bullseye_facet_4_cor_corrections_status: %s", cudaGetErrorString(e));
+    return BZ_ERR_CUDA;
+  }
+  return report_device_error(h, name);
+}

@@ -61,6 +61,10 @@ EXTENSIONS = {
     "bullseye_facet_4_cor_corrections_ws_bytes": (ctypes.c_size_t, [ctypes.c_void_p]),
     "bullseye_facet_4_cor_corrections_ws": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                                            ctypes.c_void_p]),
+    "bullseye_facet_4_cor_corrections_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "bullseye_predict_ws_bytes": (ctypes.c_size_t, [ctypes.c_void_p]),
+    "bullseye_predict": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "bullseye_reset_counters": (None, []),
     "bullseye_zero_grids": (None, []),
     "bullseye_set_gridding_correction": (None, [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t]),

@@ -27,3 +27,15 @@ def max_over_ranks(value: float, device=None) -> float:
     t = torch.tensor([float(value)], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def shard_problem(problem, world: int, rank: int):
+    """The part of a faceted problem that ``rank`` grids: its facet range's centres and the Jones
+    terms of those facets (the terms are laid out [time][antenna][facet][spw][channel][4], so the
+    facet axis is cut), with every row replicated.  Returns (sub-problem, facet range)."""
+    from dataclasses import replace
+    if problem.facet_centres is None:
+        raise ValueError("facet sharding needs a faceted problem")
+    rg = facet_shard(problem.n_facets, world, rank)
+    jones = None if problem.jones is None else problem.jones[:, :, rg.start:rg.stop].copy()
+    return replace(problem, facet_centres=problem.facet_centres[rg.start:rg.stop].copy(), jones=jones), rg

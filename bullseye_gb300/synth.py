@@ -47,6 +47,38 @@ def y_layout(n: int, arm_m: float, seed: int) -> np.ndarray:
     return np.asarray(pos[:n])
 
 
+# Geocentric (ITRF) positions in metres of the 27 EVLA antennas that the reference's benchmark
+# simulates (bullseye/mo/benchmarks/benchmark.cpp:68-95, taken there from a measurement set of an
+# observation of G55.7+3.4).  The same numbers, so that the multi-facet workload grids the
+# reference benchmark's uv coverage.
+EVLA27_ITRF = np.array([
+    [-1601710.017000, -5042006.925200, 3554602.355600], [-1601150.060300, -5042000.619800, 3554860.729400],
+    [-1600715.950800, -5042273.187000, 3554668.184500], [-1601189.030140, -5042000.493300, 3554843.425700],
+    [-1601614.091000, -5042001.652900, 3554652.509300], [-1601162.591000, -5041828.999000, 3555095.896400],
+    [-1601014.462000, -5042086.252000, 3554800.799800], [-1601185.634945, -5041978.156586, 3554876.424700],
+    [-1600951.588000, -5042125.911000, 3554773.012300], [-1601177.376760, -5041925.073200, 3554954.584100],
+    [-1601068.790300, -5042051.910200, 3554824.835300], [-1600801.926000, -5042219.366500, 3554706.448200],
+    [-1601155.635800, -5041783.843800, 3555162.374100], [-1601447.198000, -5041992.502500, 3554739.687600],
+    [-1601225.255200, -5041980.383590, 3554855.675000], [-1601526.387300, -5041996.840100, 3554698.327400],
+    [-1601139.485100, -5041679.036800, 3555316.533200], [-1601315.893000, -5041985.320170, 3554808.304600],
+    [-1601168.786100, -5041869.054000, 3555036.936000], [-1601192.467800, -5042022.856800, 3554810.438800],
+    [-1601173.979400, -5041902.657700, 3554987.517500], [-1600880.571400, -5042170.388000, 3554741.457400],
+    [-1601377.009500, -5041988.665500, 3554776.393400], [-1601180.861480, -5041947.453400, 3554921.628700],
+    [-1601265.153600, -5041982.533050, 3554834.858400], [-1601114.365500, -5042023.151800, 3554844.944000],
+    [-1601147.940400, -5041733.837000, 3555235.956000],
+])
+
+
+def evla27_equatorial() -> np.ndarray:
+    """The EVLA-27 positions in the local equatorial frame of the array (X towards the local meridian
+    at H = 0, Y east, Z pole): the geocentric positions rotated about the pole by the array's
+    longitude, centred on the array."""
+    xyz = EVLA27_ITRF - EVLA27_ITRF.mean(axis=0)
+    lon = np.arctan2(EVLA27_ITRF[:, 1].mean(), EVLA27_ITRF[:, 0].mean())
+    c, s_ = np.cos(lon), np.sin(lon)
+    return np.stack([c * xyz[:, 0] + s_ * xyz[:, 1], -s_ * xyz[:, 0] + c * xyz[:, 1], xyz[:, 2]], axis=1)
+
+
 def enu_to_equatorial(enu: np.ndarray, lat_rad: float) -> np.ndarray:
     """Local (east, north, up) to the local equatorial frame (X towards H = 0, Y east, Z pole)."""
     e, nn, u = enu[:, 0], enu[:, 1], enu[:, 2]
@@ -160,12 +192,12 @@ def config1(precision="single", *, n_ant=64, n_times=120, nx=1024, cell=2.0, s=3
 def config2(precision="single", *, n_ant=27, n_times=2000, n_chan=64, n_facets=16, nx=1024,
             cell=10.0, wplanes=64, s=31, min_support=15, os=63, n_src=50, seed=2,
             jones=True, vis_chunk=1 << 14) -> GriddingProblem:
-    """Multi-facet with phase rotation and Jones: 27 antennas (Y layout), 2000 timesteps, 64
-    channels 1.0-1.5 GHz, 50 sources, per-antenna/time gains, 16 facets of 1024^2 within 3 deg,
-    w-projection with 64 planes and supports 15..63 (padded to 63 in the ABI table)."""
+    """Multi-facet with phase rotation and Jones: 27 antennas (the reference benchmark's EVLA
+    positions, or a Y layout for other counts), 2000 timesteps, 64 channels 1.0-1.5 GHz, 50
+    sources, per-antenna/time gains, 16 facets of 1024^2 within 3 deg, w-projection with 64 planes
+    and supports 15..63 (padded to 63 in the ABI table)."""
     dec = np.deg2rad(-30.0)
-    enu = y_layout(n_ant, 600.0, seed)
-    xyz = enu_to_equatorial(enu, np.deg2rad(34.0))
+    xyz = evla27_equatorial() if n_ant == 27 else enu_to_equatorial(y_layout(n_ant, 600.0, seed), np.deg2rad(34.0))
     uvw, a1, a2, tid = earth_rotation_rows(xyz, n_times, dec, np.deg2rad(120.0))
     freqs = np.linspace(1.0e9, 1.5e9, n_chan)
     rng = np.random.default_rng(seed + 7)

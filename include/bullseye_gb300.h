@@ -192,8 +192,10 @@ int bullseye_selftest_bounded_wait(void);
  * grids beyond 5,242,880 complex cells (facets x cube x 4 x ny x nx) are rejected with
  * BZ_ERR_UNSUPPORTED (5)
  * and a message in bullseye_last_error().  Calls whose work overlaps on one GPU race on the shared
- * scratch.  The first call on each device resolves the scratch address and should come before any
- * stream capture on that device.  Returns 0 when queued. */
+ * scratch.  The first call on each device resolves the scratch address and must come before any
+ * stream capture on that device (a first call made while `stream` is capturing is rejected).
+ * Device-side errors are read with bullseye_facet_4_cor_corrections_status.  Returns 0 when
+ * queued. */
 int bullseye_facet_4_cor_corrections_noalloc(const gridding_parameters *params, void *stream);
 
 /* The same gridding on device pointers with a CALLER-PROVIDED device workspace instead of the fixed
@@ -208,6 +210,17 @@ int bullseye_facet_4_cor_corrections_noalloc(const gridding_parameters *params, 
 size_t bullseye_facet_4_cor_corrections_ws_bytes(const gridding_parameters *params);
 int bullseye_facet_4_cor_corrections_ws(const gridding_parameters *params, void *workspace, size_t bytes,
                                         void *stream);
+/* Device-side errors of the last bullseye_facet_4_cor_corrections_noalloc call on the current device
+ * (workspace null; params may be null) or of the last bullseye_facet_4_cor_corrections_ws call on
+ * `workspace` (params as passed to that call): waits for `stream`, reads the call's error word
+ * (singular Jones matrices, which are zeroed as in the reference's jones_2x2.h; channel grid index,
+ * spw, antenna or timestamp ids out of range; a bounded wait that ran out), records the first
+ * error for bullseye_last_error, clears the word and returns its status (0 = none, else
+ * BZ_ERR_SINGULAR_JONES (4), BZ_ERR_INVALID_ARGUMENT (2) or BZ_ERR_CUDA (3)).  Allocates nothing.
+ * Both entries reject bad arguments before queuing any work, so a rejected call leaves
+ * jones_terms as it was.  No counterpart in the reference (its CPU library throws from
+ * invert_all, bullseye/mo/cpu_gpu_common/jones_2x2.h:118-123). */
+int bullseye_facet_4_cor_corrections_status(const gridding_parameters *params, const void *workspace, void *stream);
 
 /* Adjoint of four-correlation gridding (a degridder): given grad_grid = dL/dG for the grids
  * G [facets][cube][4][ny][nx] that facet_4_cor_corrections (jones_terms set, faceting != 0),
@@ -224,6 +237,32 @@ int bullseye_facet_4_cor_corrections_ws(const gridding_parameters *params, void 
  * allocated.  Returns 0 when queued. */
 int bullseye_grid_adjoint(const gridding_parameters *params, const void *grad_grid, void *grad_vis,
                           void *grad_jones, int faceting, void *stream);
+
+/* Prediction (degridding as a forward operator): model visibilities from per-facet model images.
+ * `model` holds complex [facets][cube][4][ny][nx] images (each facet's model sky per cube slice and
+ * correlation, image pixels laid out as finalize writes them).  Each slice is divided by the
+ * gridding correction taper_y[y] * taper_x[x] (the tapers finalize divides by, see
+ * bullseye_set_gridding_correction; both null for none), transformed to a uv grid with the inverse
+ * of finalize's shifts (grid = fftshift(FFT(ifftshift(image))), unnormalised forward transform), and
+ * every (row, channel) visibility of vis_out [rows][channels][4] is OVERWRITTEN with
+ *   sum over facets of  J_p (e^{-i phi_f} D_f') J_q^H,
+ *   D_f = sum over the visibility's footprint of grid_f x conj(tap)      (flags & 1: divided by the
+ *         real part of the footprint's tap sum, the normalised form of the reference's prototype
+ *         degridder, writing_and_wiki/notebooks/Resampling.ipynb cell 17),
+ * with D_f' = D_f, or conj(D_f) for w < 0; the cells, taps, w plane, phase rotation (phi_f, applied
+ * with the opposite sign to the gridder's) and planar uv transform are selected exactly as the
+ * gridder selects them (faceting != 0: facet_4_cor geometry; 0: grid_4_cor), and jones_terms (raw,
+ * not inverted; null for none) are applied forward.  Weights and flags are not applied.  flags & 2:
+ * `model` already holds the uv grids (no taper, no transform, no workspace needed).  Otherwise
+ * `workspace` (256-byte aligned, at least bullseye_predict_ws_bytes(params) bytes: two grids)
+ * holds the transform.  Every pointer is a DEVICE pointer; row arrays may be in any order.  Work
+ * is queued on `stream`; the library's batched forward transform plans are created on first use
+ * per (device, size, batch) and kept.  Returns 0 when queued.  No counterpart in the reference's
+ * library (its only degridder is the notebook prototype). */
+size_t bullseye_predict_ws_bytes(const gridding_parameters *params);
+int bullseye_predict(const gridding_parameters *params, const void *model, const double *taper_x,
+                     const double *taper_y, int faceting, int flags, void *vis_out, void *workspace,
+                     size_t ws_bytes, void *stream);
 
 /* Integer sampling-function counts with the reference's nearest-neighbour policy
  * (bullseye/mo/cpu_algorithm/convolution_policies.h:35-65 composed with the sampling-function policy,

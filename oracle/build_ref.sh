@@ -10,7 +10,9 @@
 # and an FFTW-API header implemented by oracle/fftw_shim.c (FFTW is absent from this image).
 # cufft.h is only needed for the __host__/__device__ macros (cu_common.h:41).
 #
-# Usage: oracle/build_ref.sh [reference_root]   (default /root/reference)
+# Usage: oracle/build_ref.sh [reference_root]
+# The reference root is the argument, else $BULLSEYE_REFERENCE, else the read-only mount where
+# this build environment keeps the reference (this recipe is the one place that names it).
 # Exits 0 without building when the reference tree is absent (e.g. on a machine that only
 # has this repository).
 set -euo pipefail

@@ -7,7 +7,7 @@
  * It restates the algorithm of the reference CPU imaging library
  * (the bullseye/mo/cpu_algorithm and bullseye/mo/cpu_gpu_common sources) in plain C with the same
  * arithmetic types and operation order, so that its results agree bit-for-bit with the
- * reference built from source (oracle/build_ref.sh) on x86-64; tests/test_oracle_pin.py
+ * reference built from source (oracle/build_ref.sh) on x86-64; tests/test_oracle_golden.py
  * holds that check.  It exports the same C-ABI (bullseye/mo/cpu_gpu_common/wrapper.h:41-61)
  * so one harness drives the reference, this restatement and the GPU drop-in alike.
  *

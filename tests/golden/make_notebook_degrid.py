@@ -94,4 +94,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("BULLSEYE_REFERENCE")
+    if not root:
+        raise SystemExit(f"usage: {sys.argv[0]} <reference root> (or set BULLSEYE_REFERENCE)")
+    main(root)

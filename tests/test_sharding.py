@@ -2,6 +2,7 @@
 import os
 import socket
 
+import numpy as np
 import pytest
 
 from bullseye_gb300.sharding import facet_shard
@@ -63,3 +64,18 @@ def test_two_gloo_ranks():
         assert sorted(f for part in gathered for f in part) == list(range(n))
         assert all(len(set(a) & set(b)) == 0 for i, a in enumerate(gathered) for b in gathered[i + 1:])
         assert t == 11.0  # max over ranks of 10 + rank
+
+
+def test_shard_problem_cuts_facets_and_their_jones_terms():
+    from bullseye_gb300 import synth
+    from bullseye_gb300.sharding import shard_problem
+    p = synth.small_problem("double", nx=48, n_ant=5, n_times=4, n_chan=2, n_facets=5, jones=True)
+    seen = []
+    for r in range(2):
+        q, rg = shard_problem(p, 2, r)
+        assert q.n_facets == len(rg) and q.rows == p.rows
+        assert np.array_equal(q.facet_centres, p.facet_centres[rg.start:rg.stop])
+        for i, f in enumerate(rg):  # [T][A][F][S][Ch][4]: facet i of the shard is facet f of the field
+            assert np.array_equal(q.jones[:, :, i], p.jones[:, :, f])
+        seen.extend(rg)
+    assert seen == list(range(5))
