@@ -93,6 +93,9 @@ def parse():
     ap.add_argument("--sample-baselines", type=int, default=0,
                     help="baselines (all their timesteps) in the CPU-baseline / parity row sample (0: sized by time)")
     ap.add_argument("--clocks-dir", default=None, help="also write the raw nvidia-smi clock samples into this folder")
+    ap.add_argument("--reference-vs-port", action="store_true",
+                    help="time the reference's own CPU build (oracle/_ref, where it is built) against the oracle "
+                         "port on the same row sample, and exit (CPU only)")
     return ap.parse_args()
 
 
@@ -415,10 +418,11 @@ def run_sample(lib, precision, geo, conv, smp, post=True):
     R = arr["uvw"].shape[0]
     tab.fill(st, geo, R)
     st.antenna_count = smp["n_ant"]
-    st.baseline_count = smp["starts"].size - 1
+    st.baseline_count = smp["n_ant"] * (smp["n_ant"] - 1) // 2 + smp["n_ant"]  # slots of the renumbered antennas
     P = ctypes.c_void_p
     lib.initLibrary(ctypes.byref(st))
     set_rows(st, arr, lambda a: a.ctypes.data_as(P))
+    st.baseline_starting_indexes = None  # the GPU library sorts by baseline itself; the oracle reads no starts
     st.is_final_data_chunk = True
     t0 = time.perf_counter()
     lib.facet_4_cor_corrections(ctypes.byref(st))
@@ -541,33 +545,42 @@ def precision_report():
 UNEVEN_FACETS, UNEVEN_TIMES, UNEVEN_PLANES = 96, 2226, 128
 
 
+UNEVEN_MIN_VIS, UNEVEN_MAX_VIS = 1e5, 5e7
+
+
 def uneven_layout(seed=21):
     """96 facets with sizes log-uniform in [256, 4096] (multiples of 64), 5 arcsec cells, centres
-    within 3 deg, and per-facet row masks dropping a fraction in [0, 0.6] of the rows through
-    whole baselines and whole time ranges."""
+    within 3 deg, and per-facet visibility counts log-uniform in [1e5, 5e7] (the facet's kept
+    fraction of the 5e7 shared visibilities)."""
     rng = np.random.default_rng(seed)
     sizes = (np.exp(rng.uniform(np.log(256), np.log(4096), UNEVEN_FACETS)) // 64 * 64).astype(np.int64)
     sizes = np.clip(sizes, 256, 4096)
     lim = np.deg2rad(3.0)
-    return sizes, rng.uniform(-lim, lim, UNEVEN_FACETS), rng.uniform(-lim, lim, UNEVEN_FACETS), \
-        rng.uniform(0.0, 0.6, UNEVEN_FACETS)
+    counts = np.exp(rng.uniform(np.log(UNEVEN_MIN_VIS), np.log(UNEVEN_MAX_VIS), UNEVEN_FACETS))
+    return sizes, rng.uniform(-lim, lim, UNEVEN_FACETS), rng.uniform(-lim, lim, UNEVEN_FACETS), counts
 
 
-def uneven_masks(geo, fracs, seed=22):
-    """[F][R] uint8 masks: each facet drops baselines and time ranges until about `frac` of its rows go."""
+def uneven_masks(geo, counts, seed=22):
+    """[F][R] uint8 masks from baseline and time flagging: facet f keeps a random subset of the
+    baselines and one contiguous time range, each about sqrt(kept fraction) of the whole, so that it
+    keeps about counts[f] visibilities (rows x channels)."""
     from bullseye_gb300.imaging import baseline_index
     rng = np.random.default_rng(seed)
     b = baseline_index(geo["a1"], geo["a2"], N_ANT)
     t = np.asarray(geo["tid"], np.int64)
     T = int(t.max()) + 1
-    nb = int(b.max()) + 1
-    out = np.ones((len(fracs), b.size), np.uint8)
-    for f, frac in enumerate(fracs):
-        drop_b = rng.uniform(0, 1, nb) < frac / 2                  # half the loss from whole baselines
+    ub = np.unique(b)
+    total = b.size * N_CHAN
+    out = np.zeros((len(counts), b.size), np.uint8)
+    for f, n in enumerate(counts):
+        frac = min(1.0, float(n) / total)
+        keep_b = np.zeros(int(b.max()) + 1, bool)
+        nbk = max(1, int(round(ub.size * np.sqrt(frac))))
+        keep_b[rng.choice(ub, nbk, replace=False)] = True
+        span = max(1, min(T, int(round(frac * b.size / max(1, np.count_nonzero(keep_b[b])) * T))))
         t0 = int(rng.integers(0, T))
-        span = int(T * frac / 2)                                   # the other half from one time range
-        drop_t = ((t - t0) % T) < span
-        out[f] = ~(drop_b[b] | drop_t)
+        keep_t = ((t - t0) % T) < span
+        out[f] = keep_b[b] & keep_t
     return out
 
 
@@ -584,8 +597,8 @@ def uneven_main(args):
     conv, supports = kernel_stack(geo["wmax"])  # w kernels for a 1024-pixel field
     NX = 256  # the library's own grid only hosts the tuner
     R = geo["uvw"].shape[0]
-    sizes, fl, fm, fracs = uneven_layout()
-    masks = uneven_masks(geo, fracs)
+    sizes, fl, fm, targets = uneven_layout()
+    masks = uneven_masks(geo, targets)
     kept_rows = masks.sum(axis=1).astype(np.int64)
     pairs_per_step = int(kept_rows.sum()) * N_CHAN
     dec = geo["dec0"] * np.pi / (180 * 3600)
@@ -653,14 +666,33 @@ def uneven_main(args):
         true_taps += float((masks.astype(np.float64) @ sup2[pl]).sum())
     step_flops = true_taps * 8 * 4 + pairs_per_step * (6 * 4)
     achieved = step_flops / (ms * 1e-3) / 1e12
+    # load balance: one eager step with an event pair around every support-class launch
+    lib.bullseye_set_batched_profiling(1)
+    try:
+        step()
+        torch.cuda.synchronize()
+    finally:
+        lib.bullseye_set_batched_profiling(0)
+    nrec = 32
+    arrs = [np.zeros(nrec, np.int32) for _ in range(5)] + [np.zeros(nrec, np.float32)]
+    cnt = lib.bullseye_batched_profile(*[a.ctypes.data_as(ctypes.c_void_p) for a in arrs], nrec)
+    width, _, Jl, _, items, cms = arrs
+    classes = [{"width": int(width[i]), "J": int(Jl[i]), "work_items": int(items[i]), "ms": float(cms[i])}
+               for i in range(min(cnt, nrec))]
+    busy = float(sum(c["ms"] for c in classes))
     lib.releaseLibrary()
+    check(lib)
+    parity, cpu = None, None
+    if not args.no_parity:
+        parity, cpu = uneven_parity(lib, geo, conv, sizes, fl, fm, masks, d, torch, args.no_comp)
     lib.bullseye_set_device_inputs(0)
     value = pairs_per_step / (ms * 1e-3) / 1e6
     line = {"metric": "gridded Mvis/s (vis x facet pairs)", "value": value, "unit": "Mvis/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"uneven facets: {UNEVEN_FACETS} facets of {int(sizes.min())}^2..{int(sizes.max())}^2 "
-                                   f"(log-uniform), 5 arcsec cells, per-facet row masks dropping 0-60% of rows, "
+                                   f"(log-uniform), 5 arcsec cells, per-facet baseline/time flagging masks keeping "
+                                   f"1e5..5e7 visibilities per facet (log-uniform), "
                                    f"27 ant x {UNEVEN_TIMES} t x {N_CHAN} ch ({R * N_CHAN / 1e6:.1f}M vis), w-proj "
                                    f"{WPLANES} planes support {MIN_SUPPORT}-{2 * S_HALF + 1}, facet_4_cor, compensated FP32",
                        "facet_vis_min": int(kept_rows.min()) * N_CHAN, "facet_vis_max": int(kept_rows.max()) * N_CHAN,
@@ -669,8 +701,113 @@ def uneven_main(args):
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                          "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
                          "peak_source": "measured FP32 FMA probe on this GPU"},
-            "clocks": clk, "gpu_launches": launches, "e2e": None, "cpu_baseline": None}
+            "clocks": clk, "gpu_launches": launches, "e2e": None, "cpu_baseline": cpu, "parity": parity,
+            "load_balance": {"class_launches": classes, "class_ms_sum": busy,
+                             "class_share_of_eager_step": busy / (ms if ms else 1.0),
+                             "what": "per-class persistent launches of one eager step (event pair each) against the "
+                                     "graph step time; the launches of a step run back to back on one stream"}}
     print(json.dumps(line))
+
+
+def uneven_parity(lib, geo, conv1d, sizes, fl, fm, masks, d, torch, no_comp, nbl=3):
+    """The uneven layout's batched form against the FP64 oracle on a sample: the rows of `nbl` whole
+    baselines, the facets of smallest and largest kept count and the median one among facets of at
+    most 2048^2, each facet's row mask applied.  The GPU grids the sample's facets in one
+    bullseye_grid_batched_facets call; the oracle grids each facet on its own grid (masked rows
+    flagged) with the 2-D stack of the same w kernels.  Also times the oracle port in FP32 on the
+    same facet runs as the CPU baseline."""
+    from bullseye_gb300.abi import BullseyeFacet, gridding_parameters_type
+    from bullseye_gb300.filters import outer_stack
+    from bullseye_gb300.imaging import GriddingProblem, run_imaging
+    from bullseye_gb300.library import check
+    from oracle.harness import load_oracle
+    t0 = time.perf_counter()
+    pick, rows = sample_baselines(geo, nbl)
+    ms_rows = masks[:, rows]
+    kept = ms_rows.sum(axis=1)
+    small = np.nonzero((sizes <= 2048) & (kept > 0))[0]
+    sel = sorted({int(small[np.argmin(kept[small])]), int(small[np.argmax(kept[small])]),
+                  int(small[np.argsort(kept[small])[small.size // 2]])})
+    R = rows.size
+    dec = geo["dec0"] * np.pi / (180 * 3600)
+    ras = [float(fl[f] / np.cos(dec) * 180 * 3600 / np.pi) for f in sel]
+    decs = [float(geo["dec0"] + fm[f] * 180 * 3600 / np.pi) for f in sel]
+    facets = (BullseyeFacet * len(sel))()
+    off, offs = 0, []
+    for i, f in enumerate(sel):
+        n = int(sizes[f])
+        facets[i] = BullseyeFacet(ras[i], decs[i], CELL, CELL, n, n, off)
+        offs.append(off)
+        off += 4 * n * n
+    idx = torch.as_tensor(rows.astype(np.int64), device="cuda")
+    ds = {k: (v if k in ("jones", "starts") else v[idx].contiguous()) for k, v in d.items()}
+    ds["starts"] = torch.as_tensor(np.concatenate([[0], np.cumsum(geo["starts"][pick + 1] - geo["starts"][pick])])
+                                   .astype(np.int64), device="cuda")
+    grids = torch.zeros(off, dtype=torch.complex64, device="cuda")
+    lo = torch.zeros(off, dtype=torch.complex64, device="cuda")
+    norms = torch.zeros(len(sel) * 4, dtype=torch.float64, device="cuda")
+    mask_dev = torch.as_tensor(np.ascontiguousarray(ms_rows[sel]), device="cuda")
+    tab = Tables(geo, conv1d)
+    st = gridding_parameters_type("single")()
+    tab.fill(st, geo, R)
+    st.should_grid_sampling_function = False
+    st.num_facet_centres = 1
+    lib.bullseye_set_device_inputs(1)
+    lib.initLibrary(ctypes.byref(st))
+    set_rows(st, ds, lambda t: ctypes.c_void_p(t.data_ptr()))
+    st.baseline_count = pick.size
+    st.is_final_data_chunk = False
+    rc = lib.bullseye_grid_batched_facets(ctypes.byref(st), ctypes.cast(facets, ctypes.c_void_p), len(sel),
+                                          ctypes.c_void_p(mask_dev.data_ptr()), ctypes.c_void_p(grids.data_ptr()),
+                                          None if no_comp else ctypes.c_void_p(lo.data_ptr()),
+                                          ctypes.c_void_p(norms.data_ptr()), 1)
+    torch.cuda.synchronize()
+    lib.releaseLibrary()
+    check(lib)
+    assert rc == 0
+    G = (grids + lo).cpu().numpy()
+    N = norms.cpu().numpy().reshape(len(sel), 4)
+    host = {k: v.cpu().numpy() for k, v in ds.items() if k not in ("jones", "starts")}
+    conv2d = outer_stack(conv1d.astype(np.complex128))
+    per_facet, cpu_pairs, cpu_s = [], 0, 0.0
+    for i, f in enumerate(sel):
+        n = int(sizes[f])
+        prob = GriddingProblem(
+            precision="double", vis=host["vis"].astype(np.complex128), uvw=host["uvw"].astype(np.float64),
+            wavelengths=geo["lam"].astype(np.float32).astype(np.float64).reshape(1, -1),
+            weights=host["weights"].astype(np.float64), flags=host["flags"].astype(bool),
+            flagged_rows=~ms_rows[f].astype(bool), field_ids=np.zeros(R, np.uint32), spw_ids=np.zeros(R, np.uint32),
+            antenna1=host["a1"].astype(np.uint32), antenna2=host["a2"].astype(np.uint32),
+            timestamp_ids=host["tid"].astype(np.uintp), n_antennas=N_ANT, n_timestamps=geo["n_times"], nx=n, ny=n,
+            cell_x=CELL, cell_y=CELL, conv=conv2d, conv_support=S_HALF, conv_oversample=OS, wplanes=WPLANES,
+            wmax=float(np.float32(geo["wmax"])), phase_centre=(0.0, float(np.float32(geo["dec0"]))),
+            facet_centres=np.array([[np.float32(ras[i]), np.float32(decs[i])]], np.float64))
+        ref = run_imaging(load_oracle("double"), prob, "facet_4_cor", keep_raw=True)
+        g = G[offs[i]:offs[i] + 4 * n * n].reshape(4, n, n).astype(np.complex128)
+        a = ref.raw_grid[0, 0]
+        ia = dirty(a / ref.normalization[0, 0][:, None, None])
+        ib = dirty(g / N[i][:, None, None])
+        d_ = g - a
+        per_facet.append({"facet": f, "grid": n, "vis_in_sample": int(kept[f]) * N_CHAN,
+                          "grid_max_rel": float(np.max(np.abs(d_)) / np.max(np.abs(a))),
+                          "image_max_rel": float(np.max(np.abs(ib - ia)) / np.max(np.abs(ia))),
+                          "image_rms_rel": float(np.sqrt(np.mean((ib - ia) ** 2) / np.mean(ia * ia)))})
+        p32 = prob.astype("single").with_conv(conv2d.astype(np.complex64))
+        c0 = time.perf_counter()
+        run_imaging(load_oracle("single"), p32, "facet_4_cor")
+        cpu_s += time.perf_counter() - c0
+        cpu_pairs += int(kept[f]) * N_CHAN
+    worst = max(x["image_max_rel"] for x in per_facet)
+    parity = {"against": "oracle port of the reference CPU library in FP64 on each facet's own grid (masked rows "
+                         "flagged), 2-D stack of the FP32 1-D w kernels",
+              "form": "bullseye_grid_batched_facets over the sampled facets (device inputs, compensated FP32)",
+              "sample": f"{pick.size} whole baselines ({R} rows x {N_CHAN} ch), facets {sel}",
+              "max_rel": worst, "tolerance": 1e-5, "pass": worst <= 1e-5, "per_facet": per_facet,
+              "seconds": time.perf_counter() - t0}
+    cpu = {"value": cpu_pairs / cpu_s / 1e6, "unit": "Mvis/s", "cores": 1, "kind": "port",
+           "sample": f"the parity sample's {len(sel)} facet runs (one facet per call, so one OpenMP thread), "
+                     f"{cpu_pairs} vis-facet pairs, oracle port in FP32 with initLibrary/releaseLibrary, {cpu_s:.1f} s"}
+    return parity, cpu
 
 
 # ----------------------------------------------------------------------------- differentiation
@@ -847,6 +984,31 @@ def adjoint_main(args):
 
 
 # ----------------------------------------------------------------------------- main
+def reference_vs_port(geo, conv1d, nbl, reps=3):
+    """The reference's own CPU library (oracle/_ref, compiled from its sources) against the oracle
+    port on the same sample of whole baselines: best of `reps` seconds of the gridding calls and a
+    checksum of the normalised grids; prints one JSON line."""
+    from bullseye_gb300.filters import outer_stack
+    from oracle.harness import load_oracle, load_reference, reference_available
+    if not reference_available():
+        print(json.dumps({"reference_vs_port": None, "why": "oracle/_ref is not built here"}))
+        return
+    conv2d = outer_stack(conv1d.astype(np.complex128)).astype(np.complex64)
+    pick, rows = sample_baselines(geo, nbl)
+    smp = host_sample(geo, pick)
+    out = {"sample": f"{pick.size} whole baselines x {geo['n_times']} timesteps x {N_CHAN} ch x {N_FACETS} facets "
+                     f"({rows.size * N_CHAN * N_FACETS} vis-facet pairs)", "threads": os.cpu_count()}
+    for name, lib in (("port", load_oracle("single")), ("reference", load_reference("single"))):
+        ts, g = [], None
+        for _ in range(reps):
+            dt, g = run_sample(lib, "single", geo, conv2d, smp, post=True)
+            ts.append(dt)
+        out[name] = {"seconds": min(ts), "mvis_s": rows.size * N_CHAN * N_FACETS / min(ts) / 1e6,
+                     "checksum": float(np.abs(g).astype(np.float64).sum())}
+    out["port_over_reference_speed"] = out["reference"]["seconds"] / out["port"]["seconds"]
+    print(json.dumps(out))
+
+
 def relaunch(n):
     """`bench.py --gpus N` started without torchrun: run N local ranks under torch.distributed.run
     (one per GPU, rendezvous on 127.0.0.1) with the same arguments and return its exit status."""
@@ -884,6 +1046,8 @@ def main():
     conv, supports = kernel_stack(geo["wmax"])
     R = geo["uvw"].shape[0]
     pairs_per_step = R * N_CHAN * N_FACETS
+    if args.reference_vs_port:
+        return reference_vs_port(geo, conv, args.sample_baselines or 2)
 
     if args.impl == "reference":
         if rank != 0:
@@ -1048,27 +1212,38 @@ def main():
     # ------------------------------------------------------------- end to end through the C-ABI
     e2e = None
     if not args.no_e2e:
-        host = {k: v.cpu().pin_memory() for k, v in d.items()}
+        # the caller's arrays in Measurement Set order (time-major, as a reader delivers them), pinned;
+        # each step runs the pipeliner's sequence including repack_input_data
+        ms_order = torch.as_tensor(np.lexsort((np.arange(R), geo["tid"].astype(np.int64))), device="cuda")
+        host = {k: (v if k in ("jones", "starts") else v[ms_order]).cpu().pin_memory() for k, v in d.items()}
         hnp = {k: v.numpy() for k, v in host.items()}
         hnp["flagged_rows"] = hnp["flagged_rows"].view(np.bool_)
         hnp["flags"] = hnp["flags"].view(np.bool_)
-        hnp["starts"] = hnp["starts"].view(np.uintp)
+        hnp["starts"] = np.zeros(geo["nb"] + 1, np.uintp)  # filled by repack_input_data
         hnp["tid"] = hnp["tid"].view(np.uintp)
         del d
         torch.cuda.empty_cache()
         P = ctypes.c_void_p
+        # the caller's output buffers, allocated once (pinned) and zeroed every step
+        out_grid = torch.zeros((N_FACETS, 1, 4, NX, NX), dtype=torch.complex64).pin_memory()
+        out_sf = torch.zeros((N_FACETS, 1, 1, NX, NX), dtype=torch.complex64).pin_memory()
+        tab2 = Tables(geo, conv)
+        tab2.grid, tab2.sf = out_grid.numpy(), out_sf.numpy()
+        lib.bullseye_set_host_repack(0)
 
         parts = {}
 
         def e2e_step():
             marks = [time.perf_counter()]
-            tab2 = Tables(geo, conv)
+            out_grid.zero_()
+            out_sf.zero_()
             s2 = gridding_parameters_type("single")()
             tab2.fill(s2, geo, R)
             lib.initLibrary(ctypes.byref(s2))
             set_rows(s2, hnp, lambda a: a.ctypes.data_as(P))
             s2.is_final_data_chunk = True
             marks.append(time.perf_counter())
+            lib.repack_input_data(ctypes.byref(s2))
             # the reference's own call sequence; the exports run the batched gridder unless the
             # plain form is the headline
             lib.bullseye_set_batched_calls(0 if args.form == "plain" else 1)
@@ -1106,19 +1281,21 @@ def main():
             from bullseye_gb300.sharding import max_over_ranks
             dt = max_over_ranks(dt, device="cuda")
         e2e_clk = e2e_clocks.stop()
+        lib.bullseye_set_host_repack(1)
         h2d = sum(hnp[k].nbytes for k in ("vis", "weights", "flags", "uvw", "flagged_rows", "field", "spw", "a1",
-                                          "a2", "tid", "jones", "starts"))
-        # the sampling-function call uploads the rows it reads again (not the visibilities)
-        h2d += sum(hnp[k].nbytes for k in ("uvw", "flagged_rows", "field", "spw", "starts"))
+                                          "a2", "tid", "jones"))
         h2d += tab.conv.nbytes + tab.grid.nbytes + tab.sf.nbytes  # tables and initial grids (initLibrary)
         h2d += N_FACETS * NX * NX * 8  # finalize uploads the first cube slice of each facet
         d2h = tab.grid.nbytes + tab.sf.nbytes + N_FACETS * NX * NX * (8 + 4)
         e2e = {"value": pairs_per_step * world / dt / 1e6, "unit": "Mvis/s", "h2d_bytes_per_step": int(h2d * world),
                "d2h_bytes_per_step": int(d2h * world), "s_per_step": dt,
                "ms_by_call": {k: round(v / n_e2e, 1) for k, v in parts.items()}, "clocks": e2e_clk,
-               "calls": ("initLibrary, facet_4_cor_corrections, facet_sampling_function (" +
+               "calls": ("initLibrary, repack_input_data (baseline starts; rows sorted on the device), "
+                         "facet_4_cor_corrections, facet_sampling_function (" +
                          ("plain kernels" if args.form == "plain" else "batched support-aware gridder") +
-                         "), weight_uniformly, normalize, finalize, releaseLibrary (host pinned buffers)")}
+                         "), gridding_barrier, weight_uniformly, normalize, finalize, releaseLibrary; rows handed "
+                         "over in Measurement Set (time-major) order from pinned host arrays, output buffers pinned "
+                         "and zeroed every step")}
 
     cpu = None
     if not args.no_cpu and smp is not None:

@@ -45,7 +45,7 @@ def _cmd(precision: str, out: str, verbose_ptxas: bool = False):
            "-Xcompiler", "-fPIC", "-shared", "--expt-relaxed-constexpr",
            os.path.join(CSRC, "imaging_lib.cu"), os.path.join(CSRC, "noalloc.cu"),
            os.path.join(CSRC, "batched.cu"), os.path.join(CSRC, "adjoint.cu"),
-           os.path.join(CSRC, "sampling_nn.cu"), "-o", out,
+           os.path.join(CSRC, "sampling_nn.cu"), os.path.join(CSRC, "rows.cu"), "-o", out,
            "-L" + os.path.join(ch, "lib64"), "-lcufft",
            "-Xlinker", "-rpath," + os.path.join(ch, "lib64")]
     if verbose_ptxas:

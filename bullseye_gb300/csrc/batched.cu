@@ -32,14 +32,16 @@ namespace {
 
 constexpr int kMaxClasses = 16;
 
+// Rows [r0, r0 + n) of R: cls[c * R + r].
 __global__ void classify_kernel(const vis_real *__restrict__ uvw, const unsigned *__restrict__ spw,
                                 const vis_real *__restrict__ wavelengths, int nchan, int nspw, long long R,
-                                double wmax, int P, const int *__restrict__ plane_class, unsigned char *__restrict__ cls) {
+                                double wmax, int P, const int *__restrict__ plane_class, unsigned char *__restrict__ cls,
+                                long long r0, long long n) {
   const double plane_scale = P > 1 ? (double)(P - 1) / wmax : 0.0;  // as the gridder's prologue
-  const long long total = (long long)nchan * R;
+  const long long total = (long long)nchan * n;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-    const int c = (int)(i / R);
-    const long long r = i - (long long)c * R;
+    const int c = (int)(i / n);
+    const long long r = r0 + (i - (long long)c * n);
     int k = plane_class[0];
     if (P > 1) {
       const unsigned s = spw[r];
@@ -50,7 +52,7 @@ __global__ void classify_kernel(const vis_real *__restrict__ uvw, const unsigned
         if (pl >= 0.0 && pl < (double)P) k = plane_class[(int)pl];
       }
     }
-    cls[i] = (unsigned char)k;
+    cls[(long long)c * R + r] = (unsigned char)k;
   }
 }
 
@@ -112,9 +114,11 @@ __global__ void scan_kernel(const int *__restrict__ in, int *__restrict__ out, i
   if (tid == nt - 1) *total = part[nt - 1];
 }
 
+// Class indices come from plane_class (< the class count, <= kMaxClasses); a run whose class lies
+// outside the table is left out and reported rather than counted out of bounds.
 __global__ void seg_write_kernel(const size_t *starts, int nslots, int seg_len, long long R, int nchan,
                                  const unsigned char *__restrict__ cls, const int *__restrict__ off,
-                                 int4 *__restrict__ segs, int *__restrict__ class_count) {
+                                 int4 *__restrict__ segs, int *__restrict__ class_count, int ncls, int *err) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nslots * nchan) return;
   int c;
@@ -125,8 +129,10 @@ __global__ void seg_write_kernel(const size_t *starts, int nslots, int seg_len, 
   long long begin = r0;
   for (long long r = r0; r < r1; ++r) {
     if (r + 1 == r1 || k[r + 1] != k[r]) {
-      segs[o++] = make_int4((int)begin, (int)(r + 1), c, (int)k[r]);
-      atomicAdd(&class_count[k[r]], 1);
+      const int kc = k[r] < ncls ? (int)k[r] : -1;
+      if (kc < 0) atomicOr(err, DEV_ERR_GRID_INDEX);
+      segs[o++] = make_int4((int)begin, (int)(r + 1), c, kc);
+      if (kc >= 0) atomicAdd(&class_count[kc], 1);
       begin = r + 1;
     }
   }
@@ -147,6 +153,7 @@ __global__ void bucket_kernel(const int4 *__restrict__ segs, const int *total, i
   const int n = *total;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int4 s = segs[i];
+    if (s.w < 0) continue;  // reported by seg_write_kernel
     const int pos = class_off[s.w] + atomicAdd(&class_cursor[s.w], 1);
     sorted[pos] = s;
   }
@@ -470,6 +477,7 @@ bool tune_class(const GridArgs &base, int k, int nfacets, Variant &out, int host
   a.grid = c.scratch.ptr;
   a.grid_lo = COMP ? c.scratch.ptr : nullptr;
   a.norm = nullptr;
+  BZ_CUDA_TRY_RET(cudaStreamWaitEvent(c.stream, c.ev_copied_vis, 0), false);  // a copy-back may read the scratch grid
   float best = 1e30f;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
@@ -560,20 +568,22 @@ bool run_dispatch(const GridArgs &va, const GridArgs *sa, bool wproj, bool comp,
                : dispatch<false, false>(va, sa, F, tune, counts, st, vis);
 }
 
-// The schedule-building kernels (everything before the per-class launches).
-bool enqueue_schedule(const GridArgs &va, cudaStream_t st) {
+// The schedule-building kernels (everything before the per-class launches), for the tracks of
+// va.starts / va.nslots, whose rows lie in [r0, r0 + n) (n < 0: all rows).
+bool enqueue_schedule(const GridArgs &va, cudaStream_t st, long long r0 = 0, long long n = -1) {
   Context &c = g_ctx;
   BatchedState &b = g_bs;
   const long long R = va.nrows;
+  if (n < 0) n = R - r0;
   const int tracks = va.nslots * va.nchan;
   BZ_CUDA_TRY_RET(cudaMemsetAsync(b.class_count.ptr, 0, sizeof(int) * kMaxClasses, st), false);
   classify_kernel<<<1024, 256, 0, st>>>(va.uvw, va.spw, c.wavelengths.ptr, va.nchan, va.nspw, R, va.wmax, va.P,
-                                        b.plane_class.ptr, b.row_class.ptr);
+                                        b.plane_class.ptr, b.row_class.ptr, r0, n);
   seg_count_kernel<<<(tracks + 127) / 128, 128, 0, st>>>(va.starts, va.nslots, va.seg, R, va.nchan, b.row_class.ptr,
                                                          b.nseg.ptr);
   scan_kernel<<<1, 1024, 0, st>>>(b.nseg.ptr, b.seg_off.ptr, tracks, b.seg_total.ptr);
   seg_write_kernel<<<(tracks + 127) / 128, 128, 0, st>>>(va.starts, va.nslots, va.seg, R, va.nchan, b.row_class.ptr,
-                                                         b.seg_off.ptr, b.segs.ptr, b.class_count.ptr);
+                                                         b.seg_off.ptr, b.segs.ptr, b.class_count.ptr, b.ncls, va.error);
   class_offsets_kernel<<<1, 1, 0, st>>>(b.class_count.ptr, b.class_off.ptr, b.class_cursor.ptr, b.ncls);
   bucket_kernel<<<1024, 256, 0, st>>>(b.segs.ptr, b.seg_total.ptr, b.sorted.ptr, b.class_cursor.ptr, b.class_off.ptr);
   c.launches += 6;
@@ -736,6 +746,43 @@ bool call_mode(int call, int &mode, bool &faceting, const char *name) {
   }
 }
 
+// Whether every support class has a tuned layout for these visibility launches.
+bool classes_tuned(int nc, bool wproj, bool comp) {
+  for (int k = 0; k < g_bs.ncls; ++k)
+    if (!g_bs.tuned.count(std::make_tuple(g_bs.cls[k].width, nc, (int)wproj, (int)comp))) return false;
+  return true;
+}
+
+// Host inputs: the visibilities are streamed in row chunks (rows.cu); each chunk's schedule and
+// per-class launches are queued eagerly as soon as its rows are sorted, so the next chunk's upload
+// overlaps them.  The first chunk of a library lifetime whose classes are not tuned yet also tunes.
+bool stream_visibilities(gridding_parameters &p, const GridArgs &va, int nfacets, bool jones, const char *name) {
+  Context &c = g_ctx;
+  const bool wproj = va.P > 1, comp = va.grid_lo != nullptr;
+  RowsPlan plan;
+  if (!bz_plan_rows(p, plan)) return false;
+  if (!ensure_capacity(p.row_count, (size_t)plan.chunks * plan.slots * c.nchan)) return false;
+  std::vector<int> counts(kMaxClasses, 0);
+  auto chunk = [&](int k, long long r0, long long r1) -> bool {
+    GridArgs vk = va;
+    vk.starts = c.track_starts.ptr + (size_t)k * plan.slots;
+    vk.nslots = (int)plan.slots;
+    if (!enqueue_schedule(vk, c.stream, r0, r1 - r0)) return false;
+    if (!classes_tuned(4, wproj, comp)) {
+      BZ_CUDA_TRY_RET(cudaMemcpyAsync(counts.data(), g_bs.class_count.ptr, sizeof(int) * kMaxClasses,
+                                      cudaMemcpyDeviceToHost, c.stream), false);
+      BZ_CUDA_TRY_RET(cudaStreamSynchronize(c.stream), false);
+      if (!run_dispatch(vk, nullptr, wproj, comp, true, counts, c.stream, nfacets, true)) return false;
+    }
+    return run_dispatch(vk, nullptr, wproj, comp, false, counts, c.stream, nfacets, true);
+  };
+  if (!bz_stream_rows(p, true, jones, plan, chunk)) {
+    if (!bz_error_code()) bz_record_error(BZ_ERR_CUDA, "%s: streamed gridding failed", name);
+    return false;
+  }
+  return true;
+}
+
 }  // namespace
 
 // The batched gridder behind the reference's 4-correlation and sampling-function exports (one
@@ -746,15 +793,22 @@ bool bz_grid_batched_call(gridding_parameters &p, int mode, bool faceting, const
   const bool sampling = mode == CORR_SAMPLING;
   GridArgs a;
   int nslots = 0;
-  if (!bz_prepare_grid_args(p, sampling ? 1 : 4, mode, faceting, a, nslots, name)) return false;
+  // host-input visibilities are streamed (and gridded chunk by chunk) below, not uploaded here
+  const bool stream = !c.device_inputs && !sampling;
+  if (!bz_prepare_grid_args(p, sampling ? 1 : 4, mode, faceting, a, nslots, name, !stream)) return false;
   bz_trace_mark(sampling ? "sf.upload_prepare" : "vis.upload_prepare");
   if (p.row_count == 0) return true;
   if (!b.planned && !plan_classes()) {
     if (!bz_error_code()) bz_record_error(BZ_ERR_CUDA, "%s: support-class planning failed", name);
     return false;
   }
-  if (!ensure_capacity(p.row_count, (size_t)nslots * c.nchan)) return false;
   const bool wproj = p.wplanes > 1, comp = a.grid_lo != nullptr;
+  if (stream) {
+    const bool ok = stream_visibilities(p, a, (int)c.F, mode == CORR_QUAD_JONES, name);
+    bz_trace_mark("vis.grid");
+    return ok;
+  }
+  if (!ensure_capacity(p.row_count, (size_t)nslots * c.nchan)) return false;
   const int rc = sampling ? run_batched(a, &a, 1, a, 1, wproj, comp, name, false)
                           : run_batched(a, nullptr, (int)c.F, a, (int)c.F, wproj, comp, name, true);
   bz_trace_mark(sampling ? "sf.grid" : "vis.grid");
@@ -778,19 +832,32 @@ extern "C" int bullseye_grid_batched(gridding_parameters *pp, int call, int with
   bz_timer_start();
   GridArgs va, sa;
   int nslots = 0, nslots_sf = 0;
-  if (!bz_prepare_grid_args(p, 4, mode, faceting, va, nslots, "bullseye_grid_batched")) return bz_error_code();
-  // the sampling function reads the rows the visibility prepare just uploaded
-  if (sf && !bz_prepare_grid_args(p, 1, CORR_SAMPLING, faceting, sa, nslots_sf, "bullseye_grid_batched", false))
-    return bz_error_code();
+  const bool stream = !c.device_inputs;
+  if (!bz_prepare_grid_args(p, 4, mode, faceting, va, nslots, "bullseye_grid_batched", !stream)) return bz_error_code();
   if (p.row_count == 0) {
     bz_timer_stop();
     return BZ_OK;
   }
   if (!b.planned && !plan_classes()) return bz_error_code() ? bz_error_code() : BZ_ERR_CUDA;
-  if (!ensure_capacity(p.row_count, (size_t)nslots * c.nchan)) return bz_error_code();
-  const int rc = run_batched(va, sf ? &sa : nullptr, (int)c.F, va, (int)c.F, p.wplanes > 1, va.grid_lo != nullptr,
-                             "bullseye_grid_batched");
-  if (rc != BZ_OK) return rc;
+  if (stream) {
+    // host inputs: the visibilities gridded chunk by chunk as their rows arrive, then the sampling
+    // function over the rows now on the device
+    if (!stream_visibilities(p, va, (int)c.F, mode == CORR_QUAD_JONES, "bullseye_grid_batched")) return bz_error_code();
+    if (sf) {
+      if (!bz_prepare_grid_args(p, 1, CORR_SAMPLING, faceting, sa, nslots_sf, "bullseye_grid_batched")) return bz_error_code();
+      if (!ensure_capacity(p.row_count, (size_t)nslots_sf * c.nchan)) return bz_error_code();
+      const int rc = run_batched(sa, &sa, 1, sa, 1, p.wplanes > 1, sa.grid_lo != nullptr, "bullseye_grid_batched", false);
+      if (rc != BZ_OK) return rc;
+    }
+  } else {
+    // the sampling function reads the rows the visibility prepare set up
+    if (sf && !bz_prepare_grid_args(p, 1, CORR_SAMPLING, faceting, sa, nslots_sf, "bullseye_grid_batched", false))
+      return bz_error_code();
+    if (!ensure_capacity(p.row_count, (size_t)nslots * c.nchan)) return bz_error_code();
+    const int rc = run_batched(va, sf ? &sa : nullptr, (int)c.F, va, (int)c.F, p.wplanes > 1, va.grid_lo != nullptr,
+                               "bullseye_grid_batched");
+    if (rc != BZ_OK) return rc;
+  }
   if (p.is_final_data_chunk) {
     bz_copy_back_grids(p, false);
     if (sf) bz_copy_back_grids(p, true);
@@ -822,6 +889,11 @@ extern "C" int bullseye_grid_batched_facets(gridding_parameters *pp, const bulls
   if (call == 0 && (size_t)nfacets != c.F) {
     bz_record_error(BZ_ERR_INVALID_ARGUMENT, "%s: Jones terms are laid out for %zu facets, not %d", name, c.F, nfacets);
     return BZ_ERR_INVALID_ARGUMENT;
+  }
+  if (row_mask && !c.device_inputs) {
+    // host rows are reordered by baseline on the device; a row mask is indexed in the caller's order
+    bz_record_error(BZ_ERR_UNSUPPORTED, "%s: a row mask needs device-resident inputs (bullseye_set_device_inputs)", name);
+    return BZ_ERR_UNSUPPORTED;
   }
   const long long s = (long long)p.conv_support;
   for (int f = 0; f < nfacets; ++f) {
@@ -1120,12 +1192,12 @@ bool bz_grid_support_aware(const GridArgs &a_in, int nfacets, unsigned char *ws,
   window_table_kernel<<<256, 256, 0, st>>>(a_in.conv, P, K, l.tap_f, a_in.os, wproj ? 1 : 0, plane_lo, plane_w, l.L,
                                            table);
   classify_kernel<<<1024, 256, 0, st>>>(a_in.uvw, a_in.spw, a_in.wavelengths, a_in.nchan, a_in.nspw, R, a_in.wmax, P,
-                                        plane_class, row_class);
+                                        plane_class, row_class, 0, R);
   seg_count_kernel<<<(tracks + 127) / 128, 128, 0, st>>>(a_in.starts, a_in.nslots, a_in.seg, R, a_in.nchan, row_class,
                                                          nseg);
   scan_kernel<<<1, 1024, 0, st>>>(nseg, seg_off, tracks, seg_total);
   seg_write_kernel<<<(tracks + 127) / 128, 128, 0, st>>>(a_in.starts, a_in.nslots, a_in.seg, R, a_in.nchan, row_class,
-                                                         seg_off, segs, class_count);
+                                                         seg_off, segs, class_count, cl.n, a_in.error);
   class_offsets_kernel<<<1, 1, 0, st>>>(class_count, class_off, class_cursor, cl.n);
   bucket_kernel<<<1024, 256, 0, st>>>(segs, seg_total, sorted, class_cursor, class_off);
   if (cudaGetLastError() != cudaSuccess) return false;

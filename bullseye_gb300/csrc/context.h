@@ -1,6 +1,7 @@
 // Library context of the GB300 imaging library (shared by its translation units).
 #pragma once
 #include <cstring>
+#include <functional>
 #include <vector>
 
 #include "common.h"
@@ -10,6 +11,11 @@ using bz::FacetXform;
 using bz::GridArgs;
 
 // ------------------------------------------------------------------ device buffer helper
+// Library device memory (rows.cu): a stream-ordered pool that keeps freed memory mapped, so
+// buffers released by releaseLibrary are reused by the next initLibrary without first-touch costs.
+bool bz_dev_alloc(void **p, size_t bytes);
+void bz_dev_free(void *p);
+
 template <typename T>
 struct DevBuf {
   T *ptr = nullptr;
@@ -21,19 +27,35 @@ struct DevBuf {
   bool alloc(size_t count) {
     release();
     if (count == 0) count = 1;
-    if (cudaMalloc((void **)&ptr, sizeof(T) * count) != cudaSuccess) {
+    if (!bz_dev_alloc((void **)&ptr, sizeof(T) * count)) {
       ptr = nullptr;
-      bz_record_error(BZ_ERR_CUDA, "cudaMalloc of %zu bytes failed", sizeof(T) * count);
+      bz_record_error(BZ_ERR_CUDA, "device allocation of %zu bytes failed", sizeof(T) * count);
       return false;
     }
     n = count;
     return true;
   }
   void release() {
-    if (ptr) cudaFree(ptr);
+    if (ptr) bz_dev_free(ptr);
     ptr = nullptr;
     n = 0;
   }
+};
+
+// One staging buffer of the chunked row upload (rows.cu): a chunk's rows in the caller's order.
+struct StageBuf {
+  DevBuf<vis_complex> vis;
+  DevBuf<vis_real> weights, uvw;
+  DevBuf<uint8_t> flags, flagged_rows;
+  DevBuf<unsigned> field, spw, ant1, ant2;
+  DevBuf<size_t> time_ids;
+};
+
+// How the rows of a call are streamed: chunks of consecutive rows, baseline slots per chunk.
+struct RowsPlan {
+  int chunks = 0;
+  unsigned slots = 0;
+  long long chunk_rows = 0;
 };
 
 // ------------------------------------------------------------------ library context
@@ -41,6 +63,14 @@ struct Context {
   bool initialized = false;
   int device = 0;
   cudaStream_t stream = nullptr;
+  // host <-> device copies of the row chunks and the grids overlap the library stream's kernels
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_stage_full[2] = {nullptr, nullptr}, ev_stage_free[2] = {nullptr, nullptr};
+  cudaEvent_t ev_jones_up = nullptr, ev_jones_read = nullptr, ev_ready_vis = nullptr, ev_ready_sf = nullptr;
+  cudaEvent_t ev_copied_vis = nullptr, ev_copied_sf = nullptr;
+  bool host_repack = true;      // repack_input_data permutes the caller's arrays (the reference's behaviour)
+  bool norm_pending = false;    // host normalisation terms are published by the next gridding_barrier
+  double *norm_host = nullptr;  // pinned copy of the device normalisation sums [F][cube][C]
   cudaEvent_t ev_g0 = nullptr, ev_g1 = nullptr, ev_i0 = nullptr, ev_i1 = nullptr;
   bool grid_timing_pending = false, inv_timing_pending = false;
   double grid_seconds = 0.0, inv_seconds = 0.0;
@@ -77,6 +107,18 @@ struct Context {
   DevBuf<uint8_t> flags, flagged_rows;
   DevBuf<unsigned> field, spw, ant1, ant2;
   DevBuf<size_t> time_ids, starts;
+  // chunked upload: two staging buffers, the sort's keys/values/scratch, and the track table
+  // [chunks][baseline slots] + 1 of absolute row starts (track k*slots + b = baseline slot b of chunk k)
+  StageBuf stage[2];
+  size_t stage_rows = 0;
+  DevBuf<unsigned> sort_keys;
+  DevBuf<int> sort_vals;
+  DevBuf<unsigned char> sort_tmp;
+  DevBuf<size_t> track_starts;
+  RowsPlan rows_plan;           // of the rows now on the device
+  const void *rows_key[3] = {nullptr, nullptr, nullptr};  // host uvw, ant1, vis of those rows
+  size_t rows_key_count = 0;
+  bool rows_with_vis = false, rows_with_time = false;
   DevBuf<vis_complex> jones_raw, jones_inv;
   DevBuf<FacetXform> facets, facets_sf;
   // grids
@@ -84,7 +126,7 @@ struct Context {
   // same sampling-function contribution (the phase policy of the sampling function reports the
   // phase centre as facet centre, phase_transform_policies.h:77-82, so the uv transform is the
   // identity), which is gridded once into sf_acc/sf_lo [sf][ny][nx] and added to every facet.
-  DevBuf<vis_complex> grid, grid_lo, sf, sf_acc, sf_lo, scratch;
+  DevBuf<vis_complex> grid, grid_lo, sf, sf_acc, sf_lo, scratch, sf_out;
   DevBuf<double> norm;
   DevBuf<int> dev_error;
   std::vector<double> host_norm;  // published through params.normalization_terms
@@ -115,6 +157,20 @@ void bz_trace_mark(const char *phase);
 // and the call itself (a: the prepared arguments over the full support; ws: 256-byte aligned).
 size_t bz_support_aware_ws_bytes(long long rows, int nchan, int nslots, int P, int os, int W, bool wproj);
 bool bz_grid_support_aware(const GridArgs &a, int nfacets, unsigned char *ws, size_t bytes, cudaStream_t st);
-// upload = false reuses the rows a preceding prepare of the same call already uploaded.
+// upload = false reuses the rows a preceding prepare of the same call already uploaded.  With host
+// inputs, prepare only sets the arguments up (device row buffers, Jones terms, the track table of
+// `plan`); the rows themselves are streamed by bz_stream_rows (or bz_upload_rows) afterwards.
 bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool faceting, GridArgs &a,
                           int &nslots, const char *name, bool upload = true);
+// Chunked row upload with the device sort (rows.cu): on_chunk(k, row_begin, row_end) runs after the
+// chunk's sort is queued, so its gridding launches overlap the next chunk's upload.
+bool bz_stream_rows(const gridding_parameters &p, bool need_vis, bool need_time, RowsPlan &plan,
+                    const std::function<bool(int, long long, long long)> &on_chunk);
+// Streams every chunk of a host-input call unless the rows of the same host arrays are still on the
+// device (the sampling-function call that follows a visibility call); returns the plan in use.
+bool bz_upload_rows(const gridding_parameters &p, bool need_vis, bool need_time, RowsPlan &plan,
+                    const std::function<bool(int, long long, long long)> &on_chunk = nullptr);
+// The plan a host-input call will stream with (chunks, baseline slots), allocating the device rows.
+bool bz_plan_rows(const gridding_parameters &p, RowsPlan &plan);
+// Forget which host arrays the device rows came from (gridding_barrier: the caller may change them).
+void bz_forget_rows();

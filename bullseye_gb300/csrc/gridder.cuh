@@ -135,7 +135,8 @@ enum DeviceError {
   DEV_ERR_JONES_INDEX = 2,
   DEV_ERR_SINGULAR = 4,
   DEV_ERR_POL_INDEX = 8,
-  DEV_ERR_WAIT_TIMEOUT = 16  // a bounded wait on the tap-copy barrier ran out
+  DEV_ERR_WAIT_TIMEOUT = 16,  // a bounded wait on the tap-copy barrier ran out
+  DEV_ERR_ANTENNA = 32        // an antenna pair outside baseline_count (row sort)
 };
 
 template <bool WPROJ>

@@ -76,6 +76,7 @@ static void bz_clear_error() {
 
 Context g_ctx;
 void bz_release_batched();
+void bz_release_fft_plans();
 
 static bool check_ready(const char *fn) {
   if (!g_ctx.initialized) {
@@ -92,6 +93,7 @@ static void drain_device_error() {
     if (h & DEV_ERR_GRID_INDEX) bz_record_error(BZ_ERR_INVALID_ARGUMENT, "channel grid index out of range of the cube");
     if (h & DEV_ERR_JONES_INDEX) bz_record_error(BZ_ERR_INVALID_ARGUMENT, "timestamp or antenna id out of range of the Jones terms");
     if (h & DEV_ERR_WAIT_TIMEOUT) bz_record_error(BZ_ERR_CUDA, "gridder: a bounded wait for staged kernel taps ran out");
+    if (h & DEV_ERR_ANTENNA) bz_record_error(BZ_ERR_INVALID_ARGUMENT, "antenna pair outside baseline_count");
     int z = 0;
     cudaMemcpy(g_ctx.dev_error.ptr, &z, sizeof(int), cudaMemcpyHostToDevice);
   }
@@ -248,13 +250,30 @@ extern "C" double get_gridding_walltime() {
 
 extern "C" double get_inversion_walltime() { return g_ctx.inv_seconds; }
 
+// Publishes the normalisation sums of the last copy-back (copied into pinned memory on the copy
+// stream) as the library-owned host terms, in the reference GPU library's [F][cube][C][W*W] layout
+// (the sum in bin 0).
+static void publish_norms() {
+  Context &c = g_ctx;
+  if (!c.norm_pending) return;
+  const size_t bins = c.W * c.W, n = c.F * c.cube * c.C;
+  std::fill(c.host_norm.begin(), c.host_norm.end(), 0.0);
+  for (size_t i = 0; i < n; ++i) c.host_norm[i * bins] = c.norm_host[i];
+  c.norm_pending = false;
+}
+
+// Waits for the library stream and the copy stream (row uploads, copy-backs); after it the caller
+// may change its arrays, so rows on the device are no longer taken for the caller's.
 extern "C" void gridding_barrier() {
   if (!g_ctx.initialized || !g_ctx.stream) return;
   cudaError_t e = cudaStreamSynchronize(g_ctx.stream);
+  if (e == cudaSuccess && g_ctx.copy_stream) e = cudaStreamSynchronize(g_ctx.copy_stream);
   if (e != cudaSuccess) {
     bz_record_error(BZ_ERR_CUDA, "gridding_barrier: %s", cudaGetErrorString(e));
     return;
   }
+  publish_norms();
+  bz_forget_rows();
   drain_device_error();
 }
 
@@ -318,6 +337,13 @@ extern "C" void initLibrary(gridding_parameters *pp) {
     return;
   }
   BZ_CUDA_TRY(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+  BZ_CUDA_TRY(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
+  for (cudaEvent_t *ev : {&c.ev_stage_full[0], &c.ev_stage_full[1], &c.ev_stage_free[0], &c.ev_stage_free[1], &c.ev_jones_up,
+                          &c.ev_jones_read, &c.ev_ready_vis, &c.ev_ready_sf, &c.ev_copied_vis, &c.ev_copied_sf})
+    BZ_CUDA_TRY(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
+  c.norm_pending = false;
+  c.stage_rows = 0;
+  bz_forget_rows();
   BZ_CUDA_TRY(cudaEventCreate(&c.ev_g0));
   BZ_CUDA_TRY(cudaEventCreate(&c.ev_g1));
   BZ_CUDA_TRY(cudaEventCreate(&c.ev_i0));
@@ -385,6 +411,7 @@ extern "C" void initLibrary(gridding_parameters *pp) {
     BZ_CUDA_TRY(cudaMemcpy(c.facet_centres.ptr, p.facet_centres, sizeof(vis_real) * 2 * c.F, cudaMemcpyHostToDevice));
   BZ_CUDA_TRY(cudaMemset(c.dev_error.ptr, 0, sizeof(int)));
   BZ_CUDA_TRY(cudaMemset(c.norm.ptr, 0, sizeof(double) * c.F * c.cube * c.C));
+  BZ_CUDA_TRY(cudaHostAlloc((void **)&c.norm_host, sizeof(double) * c.F * c.cube * c.C, cudaHostAllocDefault));
   // row buffers are allocated on the first host-input gridding call (ensure_row_buffers)
   // grids: the caller's initial contents are uploaded (wrapper.cu:179-186)
   const size_t ng = c.F * c.cube * c.C * nxy;
@@ -404,6 +431,7 @@ extern "C" void initLibrary(gridding_parameters *pp) {
       BZ_CUDA_TRY(cudaMemcpy(c.sf.ptr, p.sampling_function_buffer, sizeof(vis_complex) * ns, cudaMemcpyHostToDevice));
     else
       BZ_CUDA_TRY(cudaMemset(c.sf.ptr, 0, sizeof(vis_complex) * ns));
+    if (!c.sf_out.alloc(ns)) return;
     const size_t na = c.sf_count * nxy;
     if (!c.sf_acc.alloc(na)) return;
     BZ_CUDA_TRY(cudaMemset(c.sf_acc.ptr, 0, sizeof(vis_complex) * na));
@@ -424,25 +452,40 @@ extern "C" void releaseLibrary() {
   Context &c = g_ctx;
   if (!c.initialized) return;
   if (c.stream) cudaStreamSynchronize(c.stream);
+  if (c.copy_stream) cudaStreamSynchronize(c.copy_stream);
+  // buffers go back to the library's memory pool (ordered on the library stream)
   c.conv.release(); c.tap_sums.release(); c.conv_t.release(); c.wavelengths.release(); c.facet_centres.release(); c.enabled.release();
   c.cgi.release(); c.sf_cgi.release(); c.vis.release(); c.weights.release(); c.uvw.release();
   c.flags.release(); c.flagged_rows.release(); c.field.release(); c.spw.release(); c.ant1.release();
   c.ant2.release(); c.time_ids.release(); c.starts.release(); c.jones_raw.release(); c.jones_inv.release();
   c.facets.release(); c.facets_sf.release(); c.grid.release(); c.grid_lo.release(); c.sf.release(); c.sf_acc.release(); c.sf_lo.release();
-  c.scratch.release(); c.norm.release(); c.dev_error.release(); c.corr_x.release(); c.corr_y.release();
-  if (c.ev_g0) cudaEventDestroy(c.ev_g0);
-  if (c.ev_g1) cudaEventDestroy(c.ev_g1);
-  if (c.ev_i0) cudaEventDestroy(c.ev_i0);
-  if (c.ev_i1) cudaEventDestroy(c.ev_i1);
-  if (c.ev_k0) cudaEventDestroy(c.ev_k0);
-  if (c.ev_k1) cudaEventDestroy(c.ev_k1);
-  c.ev_g0 = c.ev_g1 = c.ev_i0 = c.ev_i1 = c.ev_k0 = c.ev_k1 = nullptr;
+  c.scratch.release(); c.sf_out.release(); c.norm.release(); c.dev_error.release(); c.corr_x.release(); c.corr_y.release();
+  for (StageBuf &g : c.stage) {
+    g.vis.release(); g.weights.release(); g.uvw.release(); g.flags.release(); g.flagged_rows.release();
+    g.field.release(); g.spw.release(); g.ant1.release(); g.ant2.release(); g.time_ids.release();
+  }
+  c.sort_keys.release(); c.sort_vals.release(); c.sort_tmp.release(); c.track_starts.release();
+  c.stage_rows = 0;
+  bz_forget_rows();
+  bz_release_batched();
+  bz_release_fft_plans();
+  if (c.stream) cudaStreamSynchronize(c.stream);
+  for (cudaEvent_t *ev : {&c.ev_g0, &c.ev_g1, &c.ev_i0, &c.ev_i1, &c.ev_k0, &c.ev_k1, &c.ev_stage_full[0],
+                          &c.ev_stage_full[1], &c.ev_stage_free[0], &c.ev_stage_free[1], &c.ev_jones_up, &c.ev_jones_read,
+                          &c.ev_ready_vis, &c.ev_ready_sf, &c.ev_copied_vis, &c.ev_copied_sf}) {
+    if (*ev) cudaEventDestroy(*ev);
+    *ev = nullptr;
+  }
+  if (c.copy_stream) cudaStreamDestroy(c.copy_stream);
+  c.copy_stream = nullptr;
   if (c.stream) cudaStreamDestroy(c.stream);
   c.stream = nullptr;
+  if (c.norm_host) cudaFreeHost(c.norm_host);
+  c.norm_host = nullptr;
+  c.norm_pending = false;
   c.host_norm.clear();
   c.host_norm.shrink_to_fit();
   c.conv_host.clear();
-  bz_release_batched();
   c.initialized = false;
 }
 
@@ -475,6 +518,9 @@ extern "C" void repack_input_data(gridding_parameters *pp) {
     ++p.baseline_starting_indexes[b + 1];
   }
   std::partial_sum(p.baseline_starting_indexes, p.baseline_starting_indexes + B + 1, p.baseline_starting_indexes);
+  // bullseye_set_host_repack(0): the gridding calls sort their rows by baseline on the device, so
+  // the caller's arrays stay in place and only the baseline starts are reported
+  if (!g_ctx.host_repack) return;
   std::vector<size_t> dest(R), cursor(p.baseline_starting_indexes, p.baseline_starting_indexes + B);
   for (size_t r = 0; r < R; ++r) dest[r] = cursor[slot[r]]++;
   auto permute = [&](auto *arr, size_t width) {
@@ -615,112 +661,55 @@ static bool launch_gridder(const GridArgs &a, int nc, bool wproj, long long bloc
   return wproj ? launch_nc<4, true>(a, blocks, st, comp) : launch_nc<4, false>(a, blocks, st, comp);
 }
 
-// Device mirrors for chunk_max_row_count rows (wrapper.cu:146-164), allocated once.
-static bool ensure_row_buffers() {
-  Context &c = g_ctx;
-  if (c.vis.ptr) return true;
-  const size_t R = std::max<size_t>(1, c.max_rows);
-  const size_t RC = R * c.nchan * c.npol;
-  return c.vis.alloc(RC) && c.weights.alloc(RC) && c.flags.alloc(RC) && c.uvw.alloc(3 * R) &&
-         c.flagged_rows.alloc(R) && c.field.alloc(R) && c.spw.alloc(R) && c.ant1.alloc(R) && c.ant2.alloc(R) &&
-         c.time_ids.alloc(R) && c.starts.alloc(c.baselines + 2);
-}
-
-// need_vis = false (the sampling function) leaves out the visibilities, weights and flags, which
-// that gridding does not read.
-static bool upload_rows(const gridding_parameters &p, bool need_ants, bool need_time, bool need_vis = true) {
-  Context &c = g_ctx;
-  const size_t R = p.row_count;
-  if (c.device_inputs) return true;
-  if (!ensure_row_buffers()) return false;
-  bz_trace_mark("row_buffers");
-  if (R > c.max_rows) {
-    bz_record_error(BZ_ERR_INVALID_ARGUMENT, "row_count %zu exceeds chunk_max_row_count %zu", R, c.max_rows);
-    return false;
-  }
-  if (R == 0) return true;
-  const size_t RC = R * c.nchan * c.npol;
-  cudaStream_t s = c.stream;
-  if (need_vis) {
-    BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.vis.ptr, p.visibilities, sizeof(vis_complex) * RC, cudaMemcpyHostToDevice, s), false);
-    BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.weights.ptr, p.visibility_weights, sizeof(vis_real) * RC, cudaMemcpyHostToDevice, s),
-                    false);
-    BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.flags.ptr, p.flags, RC, cudaMemcpyHostToDevice, s), false);
-  }
-  BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.uvw.ptr, p.uvw_coords, sizeof(vis_real) * 3 * R, cudaMemcpyHostToDevice, s), false);
-  BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.flagged_rows.ptr, p.flagged_rows, R, cudaMemcpyHostToDevice, s), false);
-  BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.field.ptr, p.field_array, sizeof(unsigned) * R, cudaMemcpyHostToDevice, s), false);
-  BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.spw.ptr, p.spw_index_array, sizeof(unsigned) * R, cudaMemcpyHostToDevice, s), false);
-  if (need_ants) {
-    BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.ant1.ptr, p.antenna_1_ids, sizeof(unsigned) * R, cudaMemcpyHostToDevice, s), false);
-    BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.ant2.ptr, p.antenna_2_ids, sizeof(unsigned) * R, cudaMemcpyHostToDevice, s), false);
-  }
-  if (need_time)
-    BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.time_ids.ptr, p.timestamp_ids, sizeof(size_t) * R, cudaMemcpyHostToDevice, s), false);
-  return true;
-}
-
-// Validates and uploads the caller's baseline starts; returns number of track slots.
-static bool setup_tracks(const gridding_parameters &p, int &nslots, int &seg, const size_t **starts_dev) {
-  Context &c = g_ctx;
-  const size_t R = p.row_count;
-  *starts_dev = nullptr;
-  if (c.device_inputs) {
-    if (p.baseline_starting_indexes) {
-      *starts_dev = p.baseline_starting_indexes;
-      nslots = (int)p.baseline_count;
-      seg = 0;
-      return true;
-    }
-    seg = 256;
-    nslots = (int)((R + seg - 1) / seg);
-    return true;
-  }
+// Track setup of device-resident inputs (bullseye_set_device_inputs): the caller's baseline starts
+// (device pointer) or fixed 256-row segments.
+static void device_tracks(const gridding_parameters &p, int &nslots, int &seg, const size_t **starts_dev) {
   if (p.baseline_starting_indexes) {
-    const size_t B = p.baseline_count;
-    const size_t *s = p.baseline_starting_indexes;
-    bool ok = s[0] == 0 && s[B] == R;
-    for (size_t b = 0; ok && b < B; ++b) ok = s[b] <= s[b + 1];
-    if (ok && B + 1 <= c.starts.n) {
-      BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.starts.ptr, s, sizeof(size_t) * (B + 1), cudaMemcpyHostToDevice, c.stream), false);
-      *starts_dev = c.starts.ptr;
-      nslots = (int)B;
-      seg = 0;
-      return true;
-    }
-    // starts that do not describe this chunk: fall back to fixed segments
+    *starts_dev = p.baseline_starting_indexes;
+    nslots = (int)p.baseline_count;
+    seg = 0;
+    return;
   }
+  *starts_dev = nullptr;
   seg = 256;
-  nslots = (int)((R + seg - 1) / seg);
-  return true;
+  nslots = (int)((p.row_count + seg - 1) / seg);
 }
 
 bool bz_check_ready(const char *fn) { return check_ready(fn); }
 void bz_copy_back_grids(gridding_parameters &p, bool sampling);
+// Final-chunk copy-back, queued without waiting: the resolved grids (hi + lo) and the normalisation
+// sums are copied to the caller's buffers on the copy stream, overlapping whatever the library
+// stream does next (the sampling-function call of the chunk); gridding_barrier waits for them and
+// publishes the normalisation terms.  A copy-back buffer is rewritten only after its previous copy.
 static void copy_back_grids(gridding_parameters &p, bool sampling) {
   Context &c = g_ctx;
   const size_t nxy = c.nx * c.ny;
   if (!sampling) {
     const size_t n = c.F * c.cube * c.C * nxy;
+    BZ_CUDA_TRY(cudaStreamWaitEvent(c.stream, c.ev_copied_vis, 0));
     resolve_compensated_kernel<<<1024, 256, 0, c.stream>>>(c.grid.ptr, c.grid_lo.ptr, c.scratch.ptr, (long long)n);
     c.launches++;
+    BZ_CUDA_TRY(cudaEventRecord(c.ev_ready_vis, c.stream));
+    BZ_CUDA_TRY(cudaStreamWaitEvent(c.copy_stream, c.ev_ready_vis, 0));
     if (p.output_buffer)
-      BZ_CUDA_TRY(cudaMemcpyAsync(p.output_buffer, c.scratch.ptr, sizeof(vis_complex) * n, cudaMemcpyDeviceToHost, c.stream));
-    std::vector<double> tmp(c.F * c.cube * c.C);
-    BZ_CUDA_TRY(cudaMemcpyAsync(tmp.data(), c.norm.ptr, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost, c.stream));
-    BZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
-    const size_t bins = c.W * c.W;
-    std::fill(c.host_norm.begin(), c.host_norm.end(), 0.0);
-    for (size_t i = 0; i < tmp.size(); ++i) c.host_norm[i * bins] = tmp[i];
+      BZ_CUDA_TRY(cudaMemcpyAsync(p.output_buffer, c.scratch.ptr, sizeof(vis_complex) * n, cudaMemcpyDeviceToHost,
+                                  c.copy_stream));
+    BZ_CUDA_TRY(cudaMemcpyAsync(c.norm_host, c.norm.ptr, sizeof(double) * c.F * c.cube * c.C, cudaMemcpyDeviceToHost,
+                                c.copy_stream));
+    BZ_CUDA_TRY(cudaEventRecord(c.ev_copied_vis, c.copy_stream));
+    c.norm_pending = true;
   } else {
     const size_t n = c.F * c.sf_count * nxy;
-    broadcast_add_kernel<<<1024, 256, 0, c.stream>>>(c.sf.ptr, c.sf_acc.ptr, c.sf_lo.ptr, c.scratch.ptr,
+    BZ_CUDA_TRY(cudaStreamWaitEvent(c.stream, c.ev_copied_sf, 0));
+    broadcast_add_kernel<<<1024, 256, 0, c.stream>>>(c.sf.ptr, c.sf_acc.ptr, c.sf_lo.ptr, c.sf_out.ptr,
                                                     (long long)(c.sf_count * nxy), (long long)c.F);
     c.launches++;
+    BZ_CUDA_TRY(cudaEventRecord(c.ev_ready_sf, c.stream));
+    BZ_CUDA_TRY(cudaStreamWaitEvent(c.copy_stream, c.ev_ready_sf, 0));
     if (p.sampling_function_buffer)
-      BZ_CUDA_TRY(cudaMemcpyAsync(p.sampling_function_buffer, c.scratch.ptr, sizeof(vis_complex) * n,
-                                  cudaMemcpyDeviceToHost, c.stream));
-    BZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
+      BZ_CUDA_TRY(cudaMemcpyAsync(p.sampling_function_buffer, c.sf_out.ptr, sizeof(vis_complex) * n,
+                                  cudaMemcpyDeviceToHost, c.copy_stream));
+    BZ_CUDA_TRY(cudaEventRecord(c.ev_copied_sf, c.copy_stream));
   }
 }
 
@@ -747,7 +736,22 @@ bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool f
     return false;
   }
   const bool jones = mode == CORR_QUAD_JONES;
-  if (upload && !upload_rows(p, jones, jones, !sampling)) return false;
+  // rows: device-resident inputs are used as they are; host inputs are streamed in chunks and
+  // sorted by baseline on the device (rows.cu), into the library's row buffers and track table
+  int seg = 0;
+  const size_t *starts = nullptr;
+  RowsPlan plan;
+  if (c.device_inputs) {
+    device_tracks(p, nslots, seg, &starts);
+  } else {
+    if (upload) {
+      if (!bz_upload_rows(p, !sampling, jones, plan)) return false;
+    } else if (!bz_plan_rows(p, plan)) {
+      return false;
+    }
+    starts = c.track_starts.ptr;
+    nslots = plan.chunks * (int)plan.slots;
+  }
   bz_trace_mark("rows_h2d");
   if (jones) {
     const size_t nj = p.no_timestamps_read * p.antenna_count * c.F * c.nspw * c.nchan;
@@ -758,19 +762,23 @@ bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool f
     if (c.jones_inv.n < 4 * nj && !c.jones_inv.alloc(4 * nj)) return false;
     const vis_complex *jsrc = p.jones_terms;
     if (!c.device_inputs) {
+      // on the copy stream, ahead of the row chunks this call streams next
       if (c.jones_raw.n < 4 * nj && !c.jones_raw.alloc(4 * nj)) return false;
-      BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.jones_raw.ptr, p.jones_terms, sizeof(vis_complex) * 4 * nj, cudaMemcpyHostToDevice, c.stream), false);
+      // the previous call's inversion must have read the buffer before it is refilled
+      BZ_CUDA_TRY_RET(cudaStreamWaitEvent(c.copy_stream, c.ev_jones_read, 0), false);
+      BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.jones_raw.ptr, p.jones_terms, sizeof(vis_complex) * 4 * nj, cudaMemcpyHostToDevice,
+                                      c.copy_stream), false);
+      BZ_CUDA_TRY_RET(cudaEventRecord(c.ev_jones_up, c.copy_stream), false);
+      BZ_CUDA_TRY_RET(cudaStreamWaitEvent(c.stream, c.ev_jones_up, 0), false);
       jsrc = c.jones_raw.ptr;
     }
     bz_trace_mark("jones_alloc_h2d");
     invert_jones_kernel<<<(unsigned)((nj + 255) / 256), 256, 0, c.stream>>>(jsrc, c.jones_inv.ptr, (long long)nj,
                                                                              c.dev_error.ptr);
+    BZ_CUDA_TRY_RET(cudaEventRecord(c.ev_jones_read, c.stream), false);
     c.launches++;
     bz_trace_mark("jones_invert");
   }
-  int seg = 0;
-  const size_t *starts = nullptr;
-  if (!setup_tracks(p, nslots, seg, &starts)) return false;
   // per-facet transforms (FP64, host)
   std::vector<FacetXform> fx(c.F);
   const double ra0 = (double)p.phase_centre_ra, dec0 = (double)p.phase_centre_dec;
@@ -992,6 +1000,41 @@ struct StokesPair {
   int a, b, sign;
 };
 
+// The inverse transform of finalize, planned once per batch size while the library is initialised
+// (finalize and finalize_psf may transform different slice counts).
+static cufftHandle g_fft_plans[2] = {0, 0};
+static int g_fft_batches[2] = {-1, -1};
+
+static cufftHandle fft_plan(int batch) {
+  Context &c = g_ctx;
+  for (int i = 0; i < 2; ++i)
+    if (g_fft_plans[i] && g_fft_batches[i] == batch) return g_fft_plans[i];
+  const int slot = g_fft_plans[0] ? (g_fft_plans[1] ? 0 : 1) : 0;
+  if (g_fft_plans[slot]) cufftDestroy(g_fft_plans[slot]);
+  g_fft_plans[slot] = 0;
+  g_fft_batches[slot] = -1;
+  cufftHandle plan;
+  int dims[2] = {(int)c.ny, (int)c.nx};
+  const int nxy = (int)(c.nx * c.ny);
+#if defined(BULLSEYE_SINGLE)
+  const cufftType type = CUFFT_C2C;
+#else
+  const cufftType type = CUFFT_Z2Z;
+#endif
+  if (cufftPlanMany(&plan, 2, dims, nullptr, 1, nxy, nullptr, 1, nxy, type, batch) != CUFFT_SUCCESS) return 0;
+  g_fft_plans[slot] = plan;
+  g_fft_batches[slot] = batch;
+  return plan;
+}
+
+void bz_release_fft_plans() {
+  for (int i = 0; i < 2; ++i) {
+    if (g_fft_plans[i]) cufftDestroy(g_fft_plans[i]);
+    g_fft_plans[i] = 0;
+    g_fft_batches[i] = -1;
+  }
+}
+
 static void finalize_buffer(vis_complex *host, size_t per_facet_slices, size_t nslices, const char *name,
                             const StokesPair *stokes = nullptr) {
   Context &c = g_ctx;
@@ -1018,14 +1061,8 @@ static void finalize_buffer(vis_complex *host, size_t per_facet_slices, size_t n
   }
   ifftshift_gather_kernel<<<2048, 256, 0, s>>>(shifted.ptr, work.ptr, (int)c.nx, (int)c.ny, (long long)(F * nslices));
   c.launches += 2;  // the gather and the packing kernel (cuFFT's own launches are not counted)
-  cufftHandle plan;
-  int dims[2] = {(int)c.ny, (int)c.nx};
-#if defined(BULLSEYE_SINGLE)
-  cufftType type = CUFFT_C2C;
-#else
-  cufftType type = CUFFT_Z2Z;
-#endif
-  if (cufftPlanMany(&plan, 2, dims, nullptr, 1, (int)nxy, nullptr, 1, (int)nxy, type, (int)(F * nslices)) != CUFFT_SUCCESS) {
+  cufftHandle plan = fft_plan((int)(F * nslices));
+  if (!plan) {
     bz_record_error(BZ_ERR_CUFFT, "%s: cufftPlanMany failed", name);
     return;
   }
@@ -1036,7 +1073,6 @@ static void finalize_buffer(vis_complex *host, size_t per_facet_slices, size_t n
   cufftResult r = cufftExecZ2Z(plan, (cufftDoubleComplex *)work.ptr, (cufftDoubleComplex *)work.ptr, CUFFT_INVERSE);
 #endif
   if (r != CUFFT_SUCCESS) {
-    cufftDestroy(plan);
     bz_record_error(BZ_ERR_CUFFT, "%s: cufftExec failed", name);
     return;
   }
@@ -1056,7 +1092,6 @@ static void finalize_buffer(vis_complex *host, size_t per_facet_slices, size_t n
   BZ_CUDA_TRY(cudaStreamSynchronize(s));
   float ms = 0;
   if (cudaEventElapsedTime(&ms, c.ev_i0, c.ev_i1) == cudaSuccess) c.inv_seconds += ms * 1e-3;
-  cufftDestroy(plan);
   work.release();
   shifted.release();
   packed.release();

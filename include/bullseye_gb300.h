@@ -112,6 +112,16 @@ void bullseye_zero_grids(void);
 /* Measured FP32 FMA throughput of the current GPU in TFLOP/s (roofline denominator). */
 double bullseye_fp32_fma_tflops(int iters);
 
+/* Device memory: every buffer of the library comes from a device memory pool of the library that
+ * keeps freed memory mapped, so releaseLibrary followed by initLibrary (a pipeliner imaging several
+ * runs) reuses memory the GPU has already touched.  This returns the pooled memory to the driver. */
+void bullseye_trim_memory(void);
+/* Host inputs are uploaded in row chunks on a copy stream and sorted by baseline on the device,
+ * each chunk gridded while the next uploads.  With this off, repack_input_data fills
+ * baseline_starting_indexes without permuting the caller's arrays (the reference permutes them,
+ * wrapper.cu:422-452); gridding results do not depend on the row order.  On by default. */
+void bullseye_set_host_repack(int on);
+
 /* Batched, support-aware gridding of every facet of the current chunk: `call` 0 grids like
  * facet_4_cor_corrections, 1 like facet_4_cor, 2 like grid_4_cor; with_sampling != 0 also grids
  * the sampling function (like facet_/grid_sampling_function).  Same results as those calls: each
@@ -128,7 +138,8 @@ int bullseye_grid_batched(gridding_parameters *params, int call, int with_sampli
  * compensation buffer, same size as grids and zeroed by the caller, or null for plain FP32
  * accumulation; a cell's value is then grids + grid_lo; ignored by the 64-bit library) and norms
  * (float64 [nfacets][cube][4]).  Work is queued on the library stream (bullseye_get_stream).
- * row_mask, if not null, is a device array [nfacets][row_count] of bytes: 0 leaves that row out of
+ * row_mask, if not null, is a device array [nfacets][row_count] of bytes (device-resident inputs
+ * only, bullseye_set_device_inputs; rejected with BZ_ERR_UNSUPPORTED otherwise): 0 leaves that row out of
  * that facet (the facet then sees fewer visibilities).  `call` 1 grids like facet_4_cor, 2 like
  * grid_4_cor, 0 like facet_4_cor_corrections (then nfacets must equal the facet count given to
  * initLibrary, which lays out the Jones terms).  Tables (kernel, wavelengths, channels) and rows
