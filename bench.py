@@ -81,9 +81,10 @@ def parse():
     ap.add_argument("--facets", type=int, default=0, help="override the facet count (profiling cases)")
     ap.add_argument("--no-precision", action="store_true", help="skip the per-facet FP32 error report")
     ap.add_argument("--adj-times", type=int, default=0, help="differentiation workload: override the timestep count")
-    ap.add_argument("--workload", default="facets16", choices=["facets16", "uneven", "adjoint"],
+    ap.add_argument("--workload", default="facets16", choices=["facets16", "uneven", "adjoint", "predict"],
                     help="facets16: the 16-facet Jones workload (default); uneven: 96 facets of uneven sizes and masks; "
-                         "adjoint: the differentiation form at scale with a finite-difference check")
+                         "adjoint: the differentiation form at scale with a finite-difference check; "
+                         "predict: degridding 16 facet model images back to the visibilities")
     ap.add_argument("--no-class-profile", action="store_true",
                     help="skip the eager, per-support-class timed step after the timed region")
     ap.add_argument("--eager", action="store_true",
@@ -810,6 +811,96 @@ def uneven_parity(lib, geo, conv1d, sizes, fl, fm, masks, d, torch, no_comp, nbl
     return parity, cpu
 
 
+# ----------------------------------------------------------------------------- prediction
+def predict_main(args):
+    """Prediction (degridding as a forward operator) on the multi-facet workload: 16 model images of
+    1024^2 (point sources, 4 correlations) are divided by the gridding correction, transformed with
+    the inverse of finalize's shifts and degridded to the 44.93 M visibilities with the Jones terms
+    and the facet phases applied forward, summed over facets (bullseye_predict, device inputs,
+    normalised form).  One step = one bullseye_predict call over every (visibility, facet) pair."""
+    import torch
+    from bullseye_gb300.abi import gridding_parameters_type
+    from bullseye_gb300.filters import gridding_correction
+    from bullseye_gb300.library import check, load_library
+    torch.cuda.set_device(0)
+    geo = geometry(N_TIMES)
+    conv, supports = kernel_stack(geo["wmax"])
+    R = geo["uvw"].shape[0]
+    pairs = R * N_CHAN * N_FACETS
+    lib = load_library("GPU", "single")
+    d = device_inputs(geo, torch)
+    dev = torch.device("cuda")
+    # model images: 20 point sources per facet with random fluxes, the same on the 4 correlations
+    rng = np.random.default_rng(31)
+    model = torch.zeros((N_FACETS, 1, 4, NX, NX), dtype=torch.complex64, device=dev)
+    for f in range(N_FACETS):
+        ys, xs = rng.integers(NX // 4, 3 * NX // 4, 20), rng.integers(NX // 4, 3 * NX // 4, 20)
+        flux = torch.as_tensor(rng.uniform(0.1, 2.0, 20), dtype=torch.complex64, device=dev)
+        for k in range(4):
+            model[f, 0, k, torch.as_tensor(ys, device=dev), torch.as_tensor(xs, device=dev)] = flux
+    k0 = np.real(conv[0]).astype(np.float64)
+    taper = torch.as_tensor(gridding_correction(k0, S_HALF, OS, NX), device=dev)
+    arrays = dict(conv=torch.as_tensor(conv, device=dev), lam=torch.as_tensor(geo["lam"].astype(np.float32), device=dev),
+                  en=torch.ones(N_CHAN, dtype=torch.uint8, device=dev), cgi=torch.zeros(N_CHAN, dtype=torch.int64, device=dev),
+                  fc=torch.as_tensor(geo["facets"].astype(np.float32), device=dev))
+    st = gridding_parameters_type("single")()
+    Tables(geo, conv).fill(st, geo, R)
+    set_rows(st, d, lambda t: ctypes.c_void_p(t.data_ptr()))
+    P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    st.conv, st.reference_wavelengths = P(arrays["conv"]), P(arrays["lam"])
+    st.enabled_channels, st.channel_grid_indicies, st.facet_centres = P(arrays["en"]), P(arrays["cgi"]), P(arrays["fc"])
+    st.baseline_starting_indexes = None
+    out = torch.empty((R, N_CHAN, 4), dtype=torch.complex64, device=dev)
+    nbytes = int(lib.bullseye_predict_ws_bytes(ctypes.byref(st)))
+    ws = torch.empty(nbytes + 256, dtype=torch.uint8, device=dev)
+    ws_ptr = ctypes.c_void_p((ws.data_ptr() + 255) // 256 * 256)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        rc = lib.bullseye_predict(ctypes.byref(st), P(model), P(taper), P(taper), 1, 1, P(out), ws_ptr, nbytes,
+                                  ctypes.c_void_p(stream.cuda_stream))
+        if rc:
+            check(lib)
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    check(lib)
+    clocks = ClockSampler(clocks_path("clocks.csv"))
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    clk = clocks.stop()
+    check(lib)
+    fp32_peak = lib.bullseye_fp32_fma_tflops(4096)
+    counts = plane_vis_counts(geo)
+    true_taps = float(np.sum(counts.astype(np.float64) * np.asarray(supports, np.float64) ** 2))
+    # per (vis, facet): the W_p^2 complex grid x conj(tap) products of 4 correlations (8 flops each),
+    # the tap product per cell (6) and the tap sum (1), then the phase and the two 2x2 Jones products
+    step_flops = true_taps * N_FACETS * (8 * 4 + 7) + pairs * (6 * 4 + 128)
+    achieved = step_flops / (ms * 1e-3) / 1e12
+    gather_bytes = true_taps * N_FACETS * 4 * 8  # grid values read per step (mostly from L1 / L2)
+    line = {"metric": "predicted Mvis/s (vis x facet pairs)", "value": pairs / (ms * 1e-3) / 1e6, "unit": "Mvis/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD.replace("facet_4_cor_corrections+facet_sampling_function",
+                                                    "bullseye_predict (normalised, Jones forward)"),
+                       "model": "16 facets x 20 point sources, 4 correlations, detapered, forward FFT every call"},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                         "frac": achieved / fp32_peak if fp32_peak else None,
+                         "flops_rule": "(8 x 4 corr + 7) x W_p^2 per (vis, facet) + 152 for phase and Jones",
+                         "gather_gbs": gather_bytes / (ms * 1e-3) / 1e9,
+                         "gather_rule": "4 corr x 8 B x W_p^2 grid values read per (vis, facet), from L1/L2",
+                         "peak_source": "measured FP32 FMA probe on this GPU"},
+            "clocks": clk, "e2e": None, "cpu_baseline": None}
+    print(json.dumps(line))
+
+
 # ----------------------------------------------------------------------------- differentiation
 ADJ_ANT, ADJ_TIMES, ADJ_CHAN, ADJ_NX, ADJ_PLANES, ADJ_S, ADJ_MINSUP, ADJ_OS, ADJ_CELL = 64, 1000, 32, 4096, 32, 15, 7, 15, 2.0
 
@@ -828,6 +919,7 @@ def adjoint_main(args):
     from bullseye_gb300.autograd import FacetGeometry, facet_grid
     from bullseye_gb300.filters import wproj_kernels
     from bullseye_gb300.imaging import GriddingProblem
+    from bullseye_gb300.library import load_library
     torch.cuda.set_device(0)
     dev = torch.device("cuda")
     dec = np.deg2rad(-30.0)
@@ -841,7 +933,7 @@ def adjoint_main(args):
     lam = synth.C_LIGHT / freqs
     wmax = np.max(np.linalg.norm(uvw, axis=1)) / lam.min()
     fov = ADJ_NX * ADJ_CELL * synth.ARCSEC
-    conv, _ = wproj_kernels(ADJ_S, ADJ_OS, ADJ_PLANES, wmax, fov, min_support=ADJ_MINSUP)
+    conv, adj_supports = wproj_kernels(ADJ_S, ADJ_OS, ADJ_PLANES, wmax, fov, min_support=ADJ_MINSUP)
     dec0 = dec / synth.ARCSEC
 
     def problem(rows, prec, weights=None):
@@ -967,6 +1059,17 @@ def adjoint_main(args):
         an = float(g.real if part == 0 else g.imag)
         errs["jones"].append(abs(fd - an) / scale["jones"])
     vis_pairs = R * ADJ_CHAN
+    # algorithmic flops on each visibility's true w-plane support (one facet): the forward grids
+    # 8 x 4 corr x W_p^2 (+ 152 for phase and Jones); the backward gathers the same footprint
+    # (8 x 4 corr x W_p^2) and applies the chain rule through Jones (about 400 flops per item)
+    true_taps = 0.0
+    sup2 = np.asarray(adj_supports, np.float64) ** 2
+    for lm in lam:
+        pl = np.clip(np.rint(np.abs(uvw[:, 2]) / lm * ((ADJ_PLANES - 1) / wmax)).astype(np.int64), 0, ADJ_PLANES - 1)
+        true_taps += float(sup2[pl].sum())
+    fp32_peak = float(load_library("GPU", "single").bullseye_fp32_fma_tflops(4096))
+    fwd_tf = (true_taps * 32 + vis_pairs * 152) / (f_ms * 1e-3) / 1e12
+    bwd_tf = (true_taps * 32 + vis_pairs * 400) / (b_ms * 1e-3) / 1e12
     line = {"metric": "gridded Mvis/s (vis x facet pairs)", "value": vis_pairs / (f_ms * 1e-3) / 1e6, "unit": "Mvis/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": f_ms + b_ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -974,6 +1077,13 @@ def adjoint_main(args):
                                    f"{ADJ_TIMES} t x {ADJ_CHAN} ch ({vis_pairs / 1e6:.1f}M vis), one {ADJ_NX}^2 facet with "
                                    f"Jones, w-proj {ADJ_PLANES} planes; loss = sum over the central 512^2 pixels of the "
                                    f"(XX+YY) dirty image squared"},
+            "roofline": {"bound": "fp32", "achieved": fwd_tf, "peak": fp32_peak, "unit": "TFLOP/s",
+                         "frac": fwd_tf / fp32_peak if fp32_peak else None, "kernel": "forward (workspace gridding)",
+                         "backward_achieved": bwd_tf, "backward_frac": bwd_tf / fp32_peak if fp32_peak else None,
+                         "backward_gather_gbs": true_taps * 32 / (b_ms * 1e-3) / 1e9,
+                         "flops_rule": "8 x 4 corr x W_p^2 per visibility (true w-plane support) + 152 forward / "
+                                       "about 400 backward for phase, Jones and the chain rule",
+                         "peak_source": "measured FP32 FMA probe on this GPU"},
             "forward_ms": f_ms, "backward_ms": b_ms,
             "backward_mvis_s": vis_pairs / (b_ms * 1e-3) / 1e6, "loss": Lval,
             "finite_differences": {"eps": eps, "coordinates": 200,
@@ -1036,6 +1146,8 @@ def main():
         return uneven_main(args)
     if args.workload == "adjoint":
         return adjoint_main(args)
+    if args.workload == "predict":
+        return predict_main(args)
     global N_CHAN, N_FACETS
     if args.chans:
         N_CHAN = args.chans

@@ -160,12 +160,13 @@ __global__ void bucket_kernel(const int4 *__restrict__ segs, const int *total, i
 }
 
 // ---------------------------------------------------------------- launch variants
+// A thread layout of one support class; NT = 0 marks a layout not chosen for the current build.
 struct Variant {
-  int J;
-  bool wide;
-  int regs;  // register cap of the build
-  int NT, V, grid;
-  size_t smem;
+  int J = 0;
+  bool wide = false;
+  int regs = 0;  // register cap of the build
+  int NT = 0, V = 0, grid = 0;
+  size_t smem = 0;
 };
 
 template <int NC, bool WPROJ, bool COMP>
@@ -343,7 +344,11 @@ bool plan_classes() {
   b.plane_width = pw;
   b.ncls = (int)widths.size();
   if (b.ncls > kMaxClasses) return false;
-  for (int k = 0; k < b.ncls; ++k) b.cls[k].width = widths[k];
+  for (int k = 0; k < b.ncls; ++k) {
+    b.cls[k].width = widths[k];
+    b.cls[k].vis = Variant();  // chosen again (from the tuned decisions) for each call's build
+    b.cls[k].sf = Variant();
+  }
   if (!b.plane_class.alloc(P) || !b.plane_lo.alloc(P)) return false;
   BZ_CUDA_TRY_RET(cudaMemcpy(b.plane_class.ptr, pcls.data(), sizeof(int) * P, cudaMemcpyHostToDevice), false);
   BZ_CUDA_TRY_RET(cudaMemcpy(b.plane_lo.ptr, plo.data(), sizeof(int) * P, cudaMemcpyHostToDevice), false);
@@ -406,6 +411,10 @@ bool launch_class(const GridArgs &base, int k, const Variant &v, int nfacets, co
   a.segment_capacity = (long long)g_bs.segs_cap;
   a.work_count = count;
   a.work_next = next;
+  if (v.NT <= 0 || v.grid <= 0) {
+    bz_record_error(BZ_ERR_CUDA, "batched: no layout chosen for support class %d", a.W);
+    return false;
+  }
   auto kern = seg_kernel<NC, WPROJ, COMP>(v.J, v.wide, v.regs);
   if (!open_smem(kern)) {
     bz_record_error(BZ_ERR_CUDA, "batched: cudaFuncSetAttribute failed");
@@ -768,10 +777,14 @@ bool stream_visibilities(gridding_parameters &p, const GridArgs &va, int nfacets
     vk.starts = c.track_starts.ptr + (size_t)k * plan.slots;
     vk.nslots = (int)plan.slots;
     if (!enqueue_schedule(vk, c.stream, r0, r1 - r0)) return false;
-    if (!classes_tuned(4, wproj, comp)) {
-      BZ_CUDA_TRY_RET(cudaMemcpyAsync(counts.data(), g_bs.class_count.ptr, sizeof(int) * kMaxClasses,
-                                      cudaMemcpyDeviceToHost, c.stream), false);
-      BZ_CUDA_TRY_RET(cudaStreamSynchronize(c.stream), false);
+    if (k == 0) {
+      // every call sets its classes' layouts up for this build (NC, w-projection, compensation) from
+      // the tuned decisions; classes without a decision yet are timed on this chunk's runs
+      if (!classes_tuned(4, wproj, comp)) {
+        BZ_CUDA_TRY_RET(cudaMemcpyAsync(counts.data(), g_bs.class_count.ptr, sizeof(int) * kMaxClasses,
+                                        cudaMemcpyDeviceToHost, c.stream), false);
+        BZ_CUDA_TRY_RET(cudaStreamSynchronize(c.stream), false);
+      }
       if (!run_dispatch(vk, nullptr, wproj, comp, true, counts, c.stream, nfacets, true)) return false;
     }
     return run_dispatch(vk, nullptr, wproj, comp, false, counts, c.stream, nfacets, true);
