@@ -782,7 +782,7 @@ def uneven_parity(lib, geo, conv1d, sizes, fl, fm, masks, d, torch, no_comp, nbl
             timestamp_ids=host["tid"].astype(np.uintp), n_antennas=N_ANT, n_timestamps=geo["n_times"], nx=n, ny=n,
             cell_x=CELL, cell_y=CELL, conv=conv2d, conv_support=S_HALF, conv_oversample=OS, wplanes=WPLANES,
             wmax=float(np.float32(geo["wmax"])), phase_centre=(0.0, float(np.float32(geo["dec0"]))),
-            facet_centres=np.array([[np.float32(ras[i]), np.float32(decs[i])]], np.float64))
+            facet_centres=np.array([[ras[i], decs[i]]], np.float64))  # the GPU's facet centres are FP64
         ref = run_imaging(load_oracle("double"), prob, "facet_4_cor", keep_raw=True)
         g = G[offs[i]:offs[i] + 4 * n * n].reshape(4, n, n).astype(np.complex128)
         a = ref.raw_grid[0, 0]
@@ -1393,6 +1393,13 @@ def main():
             from bullseye_gb300.sharding import max_over_ranks
             dt = max_over_ranks(dt, device="cuda")
         e2e_clk = e2e_clocks.stop()
+        # one more step with phase tracing (it synchronises at phase boundaries, so it is not timed)
+        lib.bullseye_set_tracing(1)
+        e2e_step()
+        buf = ctypes.create_string_buffer(1 << 16)
+        lib.bullseye_trace_report(buf, len(buf))
+        lib.bullseye_set_tracing(0)
+        trace = buf.value.decode(errors="replace")
         lib.bullseye_set_host_repack(1)
         h2d = sum(hnp[k].nbytes for k in ("vis", "weights", "flags", "uvw", "flagged_rows", "field", "spw", "a1",
                                           "a2", "tid", "jones"))
@@ -1402,6 +1409,7 @@ def main():
         e2e = {"value": pairs_per_step * world / dt / 1e6, "unit": "Mvis/s", "h2d_bytes_per_step": int(h2d * world),
                "d2h_bytes_per_step": int(d2h * world), "s_per_step": dt,
                "ms_by_call": {k: round(v / n_e2e, 1) for k, v in parts.items()}, "clocks": e2e_clk,
+               "trace_of_one_step_ms": trace,
                "calls": ("initLibrary, repack_input_data (baseline starts; rows sorted on the device), "
                          "facet_4_cor_corrections, facet_sampling_function (" +
                          ("plain kernels" if args.form == "plain" else "batched support-aware gridder") +

@@ -243,6 +243,30 @@ struct BatchedState {
     unsigned long long used = 0;
   };
   GraphSlot graphs[2];
+  // the support classes of one call are independent (their own work counters and schedule
+  // slices; grids and sums take atomic adds), so they run on parallel branches: a class's CTAs
+  // start on the SMs the previous class's persistent CTAs leave as its queue drains
+  static constexpr int kAux = 4;
+  cudaStream_t aux[kAux] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t fork_ev = nullptr, join_ev[kAux] = {nullptr, nullptr, nullptr, nullptr};
+  bool make_aux() {
+    if (aux[0]) return true;
+    for (int i = 0; i < kAux; ++i)
+      if (cudaStreamCreateWithFlags(&aux[i], cudaStreamNonBlocking) != cudaSuccess ||
+          cudaEventCreateWithFlags(&join_ev[i], cudaEventDisableTiming) != cudaSuccess)
+        return false;
+    return cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming) == cudaSuccess;
+  }
+  void drop_aux() {
+    for (int i = 0; i < kAux; ++i) {
+      if (aux[i]) cudaStreamDestroy(aux[i]);
+      if (join_ev[i]) cudaEventDestroy(join_ev[i]);
+      aux[i] = nullptr;
+      join_ev[i] = nullptr;
+    }
+    if (fork_ev) cudaEventDestroy(fork_ev);
+    fork_ev = nullptr;
+  }
   unsigned long long graph_clock = 0;
   void drop_graphs() {
     for (auto &g : graphs) {
@@ -355,6 +379,10 @@ bool plan_classes() {
   if (!b.class_count.alloc(kMaxClasses) || !b.class_off.alloc(kMaxClasses) || !b.class_cursor.alloc(kMaxClasses) ||
       !b.work_next.alloc(2 * kMaxClasses) || !b.seg_total.alloc(1) || !b.sample_count.alloc(2 * kMaxClasses))
     return false;
+  if (!b.make_aux()) {  // the class branches' streams, made here, outside any stream capture
+    bz_record_error(BZ_ERR_CUDA, "batched: creating the class streams failed");
+    return false;
+  }
   b.planned = true;
   return true;
 }
@@ -524,16 +552,24 @@ bool tune_all(const GridArgs &base, int nfacets, bool sampling, const std::vecto
 template <int NC, bool WPROJ, bool COMP>
 bool launch_all(const GridArgs &base, int nfacets, bool sampling, cudaStream_t st, const std::vector<int> *counts) {
   BatchedState &b = g_bs;
-  for (int k = 0; k < b.ncls; ++k) {
+  // parallel branches (fork on st, join back into st), except in the per-class timed mode
+  const bool branches = !b.profile && b.ncls > 1 && b.aux[0] != nullptr;
+  if (branches) {
+    BZ_CUDA_TRY_RET(cudaEventRecord(b.fork_ev, st), false);
+    for (int i = 0; i < BatchedState::kAux; ++i) BZ_CUDA_TRY_RET(cudaStreamWaitEvent(b.aux[i], b.fork_ev, 0), false);
+  }
+  bool ok = true;
+  for (int k = 0; k < b.ncls && ok; ++k) {
     const Variant &v = sampling ? b.cls[k].sf : b.cls[k].vis;
+    const cudaStream_t ks = branches ? b.aux[k % BatchedState::kAux] : st;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (b.profile) {
       cudaEventCreate(&e0);
       cudaEventCreate(&e1);
       cudaEventRecord(e0, st);
     }
-    const bool ok = launch_class<NC, WPROJ, COMP>(base, k, v, nfacets, b.class_count.ptr + k,
-                                                  b.work_next.ptr + (sampling ? kMaxClasses : 0) + k, st);
+    ok = launch_class<NC, WPROJ, COMP>(base, k, v, nfacets, b.class_count.ptr + k,
+                                       b.work_next.ptr + (sampling ? kMaxClasses : 0) + k, ks);
     if (b.profile) {
       cudaEventRecord(e1, st);
       cudaEventSynchronize(e1);
@@ -543,9 +579,16 @@ bool launch_all(const GridArgs &base, int nfacets, bool sampling, cudaStream_t s
       cudaEventDestroy(e1);
       b.records.push_back({b.cls[k].width, NC, v.J, (int)v.wide | (v.regs << 1), counts ? (*counts)[k] * nfacets : 0, ms});
     }
-    if (!ok) return false;
   }
-  return true;
+  if (branches) {  // always rejoin, so a capture or the stream is left whole
+    for (int i = 0; i < BatchedState::kAux; ++i) {
+      if (cudaEventRecord(b.join_ev[i], b.aux[i]) != cudaSuccess || cudaStreamWaitEvent(st, b.join_ev[i], 0) != cudaSuccess) {
+        bz_record_error(BZ_ERR_CUDA, "batched: joining the class branches failed");
+        ok = false;
+      }
+    }
+  }
+  return ok;
 }
 
 // vis = false launches (and tunes) only the sampling function's classes; va then only feeds the
@@ -605,6 +648,7 @@ bool enqueue_schedule(const GridArgs &va, cudaStream_t st, long long r0 = 0, lon
 void bz_release_batched() {
   BatchedState &b = g_bs;
   b.drop_graphs();
+  b.drop_aux();
   b.plane_class.release(); b.plane_lo.release(); b.row_class.release(); b.nseg.release(); b.seg_off.release();
   b.seg_total.release(); b.class_count.release(); b.class_off.release(); b.class_cursor.release();
   b.work_next.release(); b.sample_count.release(); b.segs.release(); b.sorted.release(); b.facet_table.release();
@@ -786,8 +830,11 @@ bool stream_visibilities(gridding_parameters &p, const GridArgs &va, int nfacets
         BZ_CUDA_TRY_RET(cudaStreamSynchronize(c.stream), false);
       }
       if (!run_dispatch(vk, nullptr, wproj, comp, true, counts, c.stream, nfacets, true)) return false;
+      bz_trace_mark("vis.chunk0_sort_schedule_layouts");
     }
-    return run_dispatch(vk, nullptr, wproj, comp, false, counts, c.stream, nfacets, true);
+    const bool ok = run_dispatch(vk, nullptr, wproj, comp, false, counts, c.stream, nfacets, true);
+    bz_trace_mark("vis.chunk_grid");
+    return ok;
   };
   if (!bz_stream_rows(p, true, jones, plan, chunk)) {
     if (!bz_error_code()) bz_record_error(BZ_ERR_CUDA, "%s: streamed gridding failed", name);

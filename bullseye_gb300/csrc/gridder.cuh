@@ -1185,6 +1185,7 @@ __global__ void __launch_bounds__(512, 1) romein_grid_kernel(const GridArgs a) {
 template <int NC, bool WPROJ, int J, bool COMP, bool WIDE, int REGS = kSegRegs<J>>
 __global__ void __launch_bounds__(512, 1) __maxnreg__(REGS) romein_segment_kernel(const GridArgs a, const int nfacets) {
   __shared__ int s_item;
+  __shared__ int s_first, s_last;  // unmasked row range of the item (facet row masks)
   __shared__ __align__(8) unsigned long long s_tap_bar;
   unsigned phase = 0;
   if (threadIdx.x == 0) bar_init(&s_tap_bar, (unsigned)a.V);
@@ -1192,7 +1193,11 @@ __global__ void __launch_bounds__(512, 1) __maxnreg__(REGS) romein_segment_kerne
   const long long total = (long long)count * nfacets;
   for (;;) {
     __syncthreads();
-    if (threadIdx.x == 0) s_item = atomicAdd(a.work_next, 1);
+    if (threadIdx.x == 0) {
+      s_item = atomicAdd(a.work_next, 1);
+      s_first = 0x7fffffff;
+      s_last = -1;
+    }
     __syncthreads();
     const long long item = s_item;
     if (item >= total) break;
@@ -1208,7 +1213,27 @@ __global__ void __launch_bounds__(512, 1) __maxnreg__(REGS) romein_segment_kerne
       if (threadIdx.x == 0) atomicOr(a.error, DEV_ERR_GRID_INDEX);
       continue;
     }
-    grid_track<NC, WPROJ, J, COMP, WIDE>(a, f_local, sg.z, sg.x, sg.y, &s_tap_bar, phase);
+    long long r0 = sg.x, r1 = sg.y;
+    if (a.facet_row_mask) {
+      // a facet that leaves rows out grids only the item's first to last row it keeps, and skips
+      // the item when it keeps none (the rows in between are still tested in the prologue)
+      const uint8_t *m = a.facet_row_mask + (long long)(a.facet_base + f_local) * a.nrows;
+      int first = 0x7fffffff, last = -1;
+      for (int r = sg.x + (int)threadIdx.x; r < sg.y; r += (int)blockDim.x)
+        if (m[r]) {
+          first = min(first, r);
+          last = max(last, r);
+        }
+      if (last >= 0) {
+        atomicMin(&s_first, first);
+        atomicMax(&s_last, last);
+      }
+      __syncthreads();
+      if (s_last < 0) continue;  // uniform: every thread reads the same shared values
+      r0 = s_first;
+      r1 = (long long)s_last + 1;
+    }
+    grid_track<NC, WPROJ, J, COMP, WIDE>(a, f_local, sg.z, r0, r1, &s_tap_bar, phase);
   }
 }
 

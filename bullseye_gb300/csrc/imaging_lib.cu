@@ -146,6 +146,7 @@ void bz_trace_begin() {
 void bz_trace_mark(const char *phase) {
   if (!g_trace.on) return;
   if (g_ctx.stream) cudaStreamSynchronize(g_ctx.stream);
+  if (g_ctx.copy_stream) cudaStreamSynchronize(g_ctx.copy_stream);
   const auto now = std::chrono::steady_clock::now();
   const double ms = std::chrono::duration<double, std::milli>(now - g_trace.last).count();
   g_trace.last = now;
