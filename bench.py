@@ -94,6 +94,8 @@ def parse():
     ap.add_argument("--sample-baselines", type=int, default=0,
                     help="baselines (all their timesteps) in the CPU-baseline / parity row sample (0: sized by time)")
     ap.add_argument("--clocks-dir", default=None, help="also write the raw nvidia-smi clock samples into this folder")
+    ap.add_argument("--grid-groups", type=int, default=1,
+                    help="e2e: groups of row chunks gridded while later chunks upload (bullseye_set_grid_groups)")
     ap.add_argument("--reference-vs-port", action="store_true",
                     help="time the reference's own CPU build (oracle/_ref, where it is built) against the oracle "
                          "port on the same row sample, and exit (CPU only)")
@@ -1342,6 +1344,23 @@ def main():
         tab2 = Tables(geo, conv)
         tab2.grid, tab2.sf = out_grid.numpy(), out_sf.numpy()
         lib.bullseye_set_host_repack(0)
+        lib.bullseye_set_grid_groups(args.grid_groups)
+
+        def copy_gbs(src, dst):  # one large copy between pinned host and device memory
+            torch.cuda.synchronize()
+            c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            c0.record()
+            dst.copy_(src, non_blocking=True)
+            c1.record()
+            torch.cuda.synchronize()
+            return src.numel() * src.element_size() / (c0.elapsed_time(c1) * 1e-3) / 1e9
+
+        probe_dev = torch.empty(host["jones"].numel(), dtype=host["jones"].dtype, device="cuda")
+        copy_gbs(host["jones"].view(-1), probe_dev)
+        bw = {"pinned_h2d_gbs": copy_gbs(host["jones"].view(-1), probe_dev),
+              "pinned_d2h_gbs": copy_gbs(probe_dev, host["jones"].view(-1)), "bytes": int(host["jones"].nbytes)}
+        del probe_dev
+        torch.cuda.empty_cache()
 
         parts = {}
 
@@ -1401,6 +1420,7 @@ def main():
         lib.bullseye_set_tracing(0)
         trace = buf.value.decode(errors="replace")
         lib.bullseye_set_host_repack(1)
+        lib.bullseye_set_grid_groups(1)
         h2d = sum(hnp[k].nbytes for k in ("vis", "weights", "flags", "uvw", "flagged_rows", "field", "spw", "a1",
                                           "a2", "tid", "jones"))
         h2d += tab.conv.nbytes + tab.grid.nbytes + tab.sf.nbytes  # tables and initial grids (initLibrary)
@@ -1409,7 +1429,7 @@ def main():
         e2e = {"value": pairs_per_step * world / dt / 1e6, "unit": "Mvis/s", "h2d_bytes_per_step": int(h2d * world),
                "d2h_bytes_per_step": int(d2h * world), "s_per_step": dt,
                "ms_by_call": {k: round(v / n_e2e, 1) for k, v in parts.items()}, "clocks": e2e_clk,
-               "trace_of_one_step_ms": trace,
+               "trace_of_one_step_ms": trace, "grid_groups": args.grid_groups, "copy_bandwidth": bw,
                "calls": ("initLibrary, repack_input_data (baseline starts; rows sorted on the device), "
                          "facet_4_cor_corrections, facet_sampling_function (" +
                          ("plain kernels" if args.form == "plain" else "batched support-aware gridder") +

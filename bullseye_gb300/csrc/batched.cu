@@ -243,30 +243,6 @@ struct BatchedState {
     unsigned long long used = 0;
   };
   GraphSlot graphs[2];
-  // the support classes of one call are independent (their own work counters and schedule
-  // slices; grids and sums take atomic adds), so they run on parallel branches: a class's CTAs
-  // start on the SMs the previous class's persistent CTAs leave as its queue drains
-  static constexpr int kAux = 4;
-  cudaStream_t aux[kAux] = {nullptr, nullptr, nullptr, nullptr};
-  cudaEvent_t fork_ev = nullptr, join_ev[kAux] = {nullptr, nullptr, nullptr, nullptr};
-  bool make_aux() {
-    if (aux[0]) return true;
-    for (int i = 0; i < kAux; ++i)
-      if (cudaStreamCreateWithFlags(&aux[i], cudaStreamNonBlocking) != cudaSuccess ||
-          cudaEventCreateWithFlags(&join_ev[i], cudaEventDisableTiming) != cudaSuccess)
-        return false;
-    return cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming) == cudaSuccess;
-  }
-  void drop_aux() {
-    for (int i = 0; i < kAux; ++i) {
-      if (aux[i]) cudaStreamDestroy(aux[i]);
-      if (join_ev[i]) cudaEventDestroy(join_ev[i]);
-      aux[i] = nullptr;
-      join_ev[i] = nullptr;
-    }
-    if (fork_ev) cudaEventDestroy(fork_ev);
-    fork_ev = nullptr;
-  }
   unsigned long long graph_clock = 0;
   void drop_graphs() {
     for (auto &g : graphs) {
@@ -379,10 +355,6 @@ bool plan_classes() {
   if (!b.class_count.alloc(kMaxClasses) || !b.class_off.alloc(kMaxClasses) || !b.class_cursor.alloc(kMaxClasses) ||
       !b.work_next.alloc(2 * kMaxClasses) || !b.seg_total.alloc(1) || !b.sample_count.alloc(2 * kMaxClasses))
     return false;
-  if (!b.make_aux()) {  // the class branches' streams, made here, outside any stream capture
-    bz_record_error(BZ_ERR_CUDA, "batched: creating the class streams failed");
-    return false;
-  }
   b.planned = true;
   return true;
 }
@@ -552,24 +524,16 @@ bool tune_all(const GridArgs &base, int nfacets, bool sampling, const std::vecto
 template <int NC, bool WPROJ, bool COMP>
 bool launch_all(const GridArgs &base, int nfacets, bool sampling, cudaStream_t st, const std::vector<int> *counts) {
   BatchedState &b = g_bs;
-  // parallel branches (fork on st, join back into st), except in the per-class timed mode
-  const bool branches = !b.profile && b.ncls > 1 && b.aux[0] != nullptr;
-  if (branches) {
-    BZ_CUDA_TRY_RET(cudaEventRecord(b.fork_ev, st), false);
-    for (int i = 0; i < BatchedState::kAux; ++i) BZ_CUDA_TRY_RET(cudaStreamWaitEvent(b.aux[i], b.fork_ev, 0), false);
-  }
-  bool ok = true;
-  for (int k = 0; k < b.ncls && ok; ++k) {
+  for (int k = 0; k < b.ncls; ++k) {
     const Variant &v = sampling ? b.cls[k].sf : b.cls[k].vis;
-    const cudaStream_t ks = branches ? b.aux[k % BatchedState::kAux] : st;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (b.profile) {
       cudaEventCreate(&e0);
       cudaEventCreate(&e1);
       cudaEventRecord(e0, st);
     }
-    ok = launch_class<NC, WPROJ, COMP>(base, k, v, nfacets, b.class_count.ptr + k,
-                                       b.work_next.ptr + (sampling ? kMaxClasses : 0) + k, ks);
+    const bool ok = launch_class<NC, WPROJ, COMP>(base, k, v, nfacets, b.class_count.ptr + k,
+                                                  b.work_next.ptr + (sampling ? kMaxClasses : 0) + k, st);
     if (b.profile) {
       cudaEventRecord(e1, st);
       cudaEventSynchronize(e1);
@@ -579,16 +543,9 @@ bool launch_all(const GridArgs &base, int nfacets, bool sampling, cudaStream_t s
       cudaEventDestroy(e1);
       b.records.push_back({b.cls[k].width, NC, v.J, (int)v.wide | (v.regs << 1), counts ? (*counts)[k] * nfacets : 0, ms});
     }
+    if (!ok) return false;
   }
-  if (branches) {  // always rejoin, so a capture or the stream is left whole
-    for (int i = 0; i < BatchedState::kAux; ++i) {
-      if (cudaEventRecord(b.join_ev[i], b.aux[i]) != cudaSuccess || cudaStreamWaitEvent(st, b.join_ev[i], 0) != cudaSuccess) {
-        bz_record_error(BZ_ERR_CUDA, "batched: joining the class branches failed");
-        ok = false;
-      }
-    }
-  }
-  return ok;
+  return true;
 }
 
 // vis = false launches (and tunes) only the sampling function's classes; va then only feeds the
@@ -648,7 +605,6 @@ bool enqueue_schedule(const GridArgs &va, cudaStream_t st, long long r0 = 0, lon
 void bz_release_batched() {
   BatchedState &b = g_bs;
   b.drop_graphs();
-  b.drop_aux();
   b.plane_class.release(); b.plane_lo.release(); b.row_class.release(); b.nseg.release(); b.seg_off.release();
   b.seg_total.release(); b.class_count.release(); b.class_off.release(); b.class_cursor.release();
   b.work_next.release(); b.sample_count.release(); b.segs.release(); b.sorted.release(); b.facet_table.release();
@@ -661,6 +617,9 @@ void bz_release_batched() {
 
 // See include/bullseye_gb300.h.
 extern "C" void bullseye_set_batched_profiling(int on) { g_bs.profile = on != 0; }
+
+// See include/bullseye_gb300.h.
+extern "C" void bullseye_set_grid_groups(int groups) { g_ctx.grid_groups = groups < 1 ? 1 : groups; }
 
 namespace {
 // Self-test of the bounded tap-barrier wait: the barrier expects two arrivals and gets one, so
@@ -806,34 +765,50 @@ bool classes_tuned(int nc, bool wproj, bool comp) {
   return true;
 }
 
-// Host inputs: the visibilities are streamed in row chunks (rows.cu); each chunk's schedule and
-// per-class launches are queued eagerly as soon as its rows are sorted, so the next chunk's upload
-// overlaps them.  The first chunk of a library lifetime whose classes are not tuned yet also tunes.
+// Host inputs: the visibilities are streamed in row chunks (rows.cu): the upload of chunk k + 1
+// overlaps the device sort of chunk k.  With one gridding group (the default) every row is gridded
+// after the last chunk is sorted, by the same graph-replayed launches as device-resident rows;
+// with G groups, the chunks of each group are gridded (eager launches) while the next group's rows
+// upload.  More groups hide more of the upload but split every class launch, and each split adds
+// a launch tail.
 bool stream_visibilities(gridding_parameters &p, const GridArgs &va, int nfacets, bool jones, const char *name) {
   Context &c = g_ctx;
   const bool wproj = va.P > 1, comp = va.grid_lo != nullptr;
   RowsPlan plan;
   if (!bz_plan_rows(p, plan)) return false;
   if (!ensure_capacity(p.row_count, (size_t)plan.chunks * plan.slots * c.nchan)) return false;
+  const int K = plan.chunks, G = std::max(1, std::min(c.grid_groups, K));
+  if (G == 1) {
+    if (!bz_stream_rows(p, true, jones, plan, nullptr)) {
+      if (!bz_error_code()) bz_record_error(BZ_ERR_CUDA, "%s: row upload failed", name);
+      return false;
+    }
+    bz_trace_mark("vis.rows_sorted");
+    return run_batched(va, nullptr, nfacets, va, nfacets, wproj, comp, name, true) == BZ_OK;
+  }
   std::vector<int> counts(kMaxClasses, 0);
+  int k0 = 0;
+  long long g_r0 = 0;
   auto chunk = [&](int k, long long r0, long long r1) -> bool {
+    if (k == k0) g_r0 = r0;
+    if (k + 1 < K && (long long)(k + 1) * G / K == (long long)k * G / K) return true;  // group not complete
     GridArgs vk = va;
-    vk.starts = c.track_starts.ptr + (size_t)k * plan.slots;
-    vk.nslots = (int)plan.slots;
-    if (!enqueue_schedule(vk, c.stream, r0, r1 - r0)) return false;
-    if (k == 0) {
+    vk.starts = c.track_starts.ptr + (size_t)k0 * plan.slots;
+    vk.nslots = (k - k0 + 1) * (int)plan.slots;
+    if (!enqueue_schedule(vk, c.stream, g_r0, r1 - g_r0)) return false;
+    if (k0 == 0) {
       // every call sets its classes' layouts up for this build (NC, w-projection, compensation) from
-      // the tuned decisions; classes without a decision yet are timed on this chunk's runs
+      // the tuned decisions; classes without a decision yet are timed on this group's runs
       if (!classes_tuned(4, wproj, comp)) {
         BZ_CUDA_TRY_RET(cudaMemcpyAsync(counts.data(), g_bs.class_count.ptr, sizeof(int) * kMaxClasses,
                                         cudaMemcpyDeviceToHost, c.stream), false);
         BZ_CUDA_TRY_RET(cudaStreamSynchronize(c.stream), false);
       }
       if (!run_dispatch(vk, nullptr, wproj, comp, true, counts, c.stream, nfacets, true)) return false;
-      bz_trace_mark("vis.chunk0_sort_schedule_layouts");
     }
     const bool ok = run_dispatch(vk, nullptr, wproj, comp, false, counts, c.stream, nfacets, true);
-    bz_trace_mark("vis.chunk_grid");
+    bz_trace_mark("vis.group_grid");
+    k0 = k + 1;
     return ok;
   };
   if (!bz_stream_rows(p, true, jones, plan, chunk)) {

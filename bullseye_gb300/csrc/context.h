@@ -69,6 +69,7 @@ struct Context {
   cudaEvent_t ev_jones_up = nullptr, ev_jones_read = nullptr, ev_ready_vis = nullptr, ev_ready_sf = nullptr;
   cudaEvent_t ev_copied_vis = nullptr, ev_copied_sf = nullptr;
   bool host_repack = true;      // repack_input_data permutes the caller's arrays (the reference's behaviour)
+  int grid_groups = 1;          // groups of row chunks gridded while later chunks upload (1: after all)
   bool norm_pending = false;    // host normalisation terms are published by the next gridding_barrier
   double *norm_host = nullptr;  // pinned copy of the device normalisation sums [F][cube][C]
   cudaEvent_t ev_g0 = nullptr, ev_g1 = nullptr, ev_i0 = nullptr, ev_i1 = nullptr;

@@ -121,6 +121,11 @@ void bullseye_trim_memory(void);
  * baseline_starting_indexes without permuting the caller's arrays (the reference permutes them,
  * wrapper.cu:422-452); gridding results do not depend on the row order.  On by default. */
 void bullseye_set_host_repack(int on);
+/* Host-input visibilities of a batched gridding call are gridded in `groups` groups of row chunks,
+ * each while the next group's rows upload; 1 (the default) grids every row after the last chunk
+ * is sorted, in one set of class launches.  More groups hide more of the upload but split every
+ * class launch, adding a launch tail per group. */
+void bullseye_set_grid_groups(int groups);
 
 /* Batched, support-aware gridding of every facet of the current chunk: `call` 0 grids like
  * facet_4_cor_corrections, 1 like facet_4_cor, 2 like grid_4_cor; with_sampling != 0 also grids

@@ -105,3 +105,23 @@ def test_host_repack_off_leaves_caller_arrays(many_rows, gpu_libs):
     assert np.array_equal(a1, p.antenna1) and np.array_equal(uvw, p.uvw)
     counts = np.bincount(baseline_index(p.antenna1, p.antenna2, p.n_antennas), minlength=p.baseline_count)
     assert np.array_equal(starts, np.concatenate([[0], np.cumsum(counts)]).astype(np.uintp))
+
+
+@pytest.mark.parametrize("precision", ["double", "single"])
+def test_grouped_gridding_matches_oracle(precision, many_rows, gpu_libs, oracle_libs):
+    """bullseye_set_grid_groups(2): the two row chunks of one call are gridded as they arrive."""
+    from bullseye_gb300.library import check
+    p = many_rows.astype(precision)
+    lib = gpu_libs[precision]
+    lib.bullseye_set_grid_groups(2)
+    try:
+        res = run_imaging(_NoHostRepack(lib), p, "facet_4_cor_corrections", repack=True, keep_raw=True, uniform=True,
+                          norm_bins=(2 * p.conv_support + 1) ** 2)
+    finally:
+        lib.bullseye_set_grid_groups(1)
+        lib.bullseye_set_host_repack(1)
+    check(lib)
+    ref = _reference(p, oracle_libs["double"])
+    tol = 1e-12 if precision == "double" else 1e-5
+    assert rel(res.raw_grid, ref.raw_grid) <= tol
+    assert rel(res.sampling, ref.sampling) <= tol
