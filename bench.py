@@ -96,6 +96,9 @@ def parse():
     ap.add_argument("--clocks-dir", default=None, help="also write the raw nvidia-smi clock samples into this folder")
     ap.add_argument("--grid-groups", type=int, default=1,
                     help="e2e: groups of row chunks gridded while later chunks upload (bullseye_set_grid_groups)")
+    ap.add_argument("--host-copy", type=int, default=1, choices=[0, 1],
+                    help="e2e: 1 copies mapped page-locked host buffers with SM kernels, 0 with the copy engines "
+                         "(bullseye_set_host_copy)")
     ap.add_argument("--reference-vs-port", action="store_true",
                     help="time the reference's own CPU build (oracle/_ref, where it is built) against the oracle "
                          "port on the same row sample, and exit (CPU only)")
@@ -1345,6 +1348,7 @@ def main():
         tab2.grid, tab2.sf = out_grid.numpy(), out_sf.numpy()
         lib.bullseye_set_host_repack(0)
         lib.bullseye_set_grid_groups(args.grid_groups)
+        lib.bullseye_set_host_copy(args.host_copy)
 
         def copy_gbs(src, dst):  # one large copy between pinned host and device memory
             torch.cuda.synchronize()
@@ -1359,6 +1363,9 @@ def main():
         copy_gbs(host["jones"].view(-1), probe_dev)
         bw = {"pinned_h2d_gbs": copy_gbs(host["jones"].view(-1), probe_dev),
               "pinned_d2h_gbs": copy_gbs(probe_dev, host["jones"].view(-1)), "bytes": int(host["jones"].nbytes)}
+        del probe_dev
+        probe_dev = torch.empty(host["vis"].numel(), dtype=host["vis"].dtype, device="cuda")
+        bw["vis_h2d_gbs"] = copy_gbs(host["vis"].view(-1), probe_dev)
         del probe_dev
         torch.cuda.empty_cache()
 
@@ -1421,6 +1428,7 @@ def main():
         trace = buf.value.decode(errors="replace")
         lib.bullseye_set_host_repack(1)
         lib.bullseye_set_grid_groups(1)
+        lib.bullseye_set_host_copy(1)
         h2d = sum(hnp[k].nbytes for k in ("vis", "weights", "flags", "uvw", "flagged_rows", "field", "spw", "a1",
                                           "a2", "tid", "jones"))
         h2d += tab.conv.nbytes + tab.grid.nbytes + tab.sf.nbytes  # tables and initial grids (initLibrary)
@@ -1430,6 +1438,7 @@ def main():
                "d2h_bytes_per_step": int(d2h * world), "s_per_step": dt,
                "ms_by_call": {k: round(v / n_e2e, 1) for k, v in parts.items()}, "clocks": e2e_clk,
                "trace_of_one_step_ms": trace, "grid_groups": args.grid_groups, "copy_bandwidth": bw,
+               "host_copy": "SM kernels" if args.host_copy else "copy engines",
                "calls": ("initLibrary, repack_input_data (baseline starts; rows sorted on the device), "
                          "facet_4_cor_corrections, facet_sampling_function (" +
                          ("plain kernels" if args.form == "plain" else "batched support-aware gridder") +

@@ -70,6 +70,8 @@ struct Context {
   cudaEvent_t ev_copied_vis = nullptr, ev_copied_sf = nullptr;
   bool host_repack = true;      // repack_input_data permutes the caller's arrays (the reference's behaviour)
   int grid_groups = 1;          // groups of row chunks gridded while later chunks upload (1: after all)
+  bool host_copy_sm = true;     // bulk copies of mapped page-locked host memory run as SM kernels
+  size_t max_stage_bytes = 0;   // row staging of one chunk, bytes (0: 8 GB)
   bool norm_pending = false;    // host normalisation terms are published by the next gridding_barrier
   double *norm_host = nullptr;  // pinned copy of the device normalisation sums [F][cube][C]
   cudaEvent_t ev_g0 = nullptr, ev_g1 = nullptr, ev_i0 = nullptr, ev_i1 = nullptr;
@@ -154,6 +156,11 @@ bool bz_grid_batched_call(gridding_parameters &p, int mode, bool faceting, const
 // the library stream and record the host time of each phase of a call; off, they do nothing.
 void bz_trace_begin();
 void bz_trace_mark(const char *phase);
+// Whether tracing is on; a free-form trace entry; the CUDA memory kind of a caller's pointer
+// ("pinned", "pageable", "device", "managed") for the trace.
+bool bz_tracing();
+void bz_trace_note(const char *fmt, ...);
+const char *bz_host_kind(const void *p);
 // Support-aware gridding without library state (the workspace entry): bytes of workspace it needs,
 // and the call itself (a: the prepared arguments over the full support; ws: 256-byte aligned).
 size_t bz_support_aware_ws_bytes(long long rows, int nchan, int nslots, int P, int os, int W, bool wproj);
@@ -175,3 +182,10 @@ bool bz_upload_rows(const gridding_parameters &p, bool need_vis, bool need_time,
 bool bz_plan_rows(const gridding_parameters &p, RowsPlan &plan);
 // Forget which host arrays the device rows came from (gridding_barrier: the caller may change them).
 void bz_forget_rows();
+// Device address of host bytes [p, p + n) when they lie in one page-locked allocation mapped into
+// the device's address space; nullptr otherwise (pageable memory, or a range that leaves it).
+const void *bz_mapped_host(const void *p, size_t n);
+// A host <-> device (or device <-> device) copy on stream s: an SM kernel when the host side is
+// mapped page-locked memory and SM copies are on (bullseye_set_host_copy), else cudaMemcpyAsync.
+// false on error (recorded).
+bool bz_copy_async(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind, cudaStream_t s);

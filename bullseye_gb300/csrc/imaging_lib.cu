@@ -155,6 +155,33 @@ void bz_trace_mark(const char *phase) {
   if (g_trace.log.size() < (1u << 16)) g_trace.log += buf;
 }
 
+bool bz_tracing() { return g_trace.on; }
+
+void bz_trace_note(const char *fmt, ...) {
+  if (!g_trace.on) return;
+  char buf[160];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (g_trace.log.size() < (1u << 16)) (g_trace.log += buf) += "; ";
+}
+
+const char *bz_host_kind(const void *p) {
+  cudaPointerAttributes at{};
+  if (!p) return "null";
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return "unknown";
+  }
+  switch (at.type) {
+    case cudaMemoryTypeHost: return "pinned";
+    case cudaMemoryTypeDevice: return "device";
+    case cudaMemoryTypeManaged: return "managed";
+    default: return "pageable";
+  }
+}
+
 // See include/bullseye_gb300.h.
 extern "C" void bullseye_set_tracing(int on) {
   g_trace.on = on != 0;
@@ -417,9 +444,10 @@ extern "C" void initLibrary(gridding_parameters *pp) {
   // grids: the caller's initial contents are uploaded (wrapper.cu:179-186)
   const size_t ng = c.F * c.cube * c.C * nxy;
   if (!c.grid.alloc(ng) || !c.scratch.alloc(std::max(ng, c.F * std::max<size_t>(1, c.sf_count) * nxy))) return;
-  if (p.output_buffer)
-    BZ_CUDA_TRY(cudaMemcpy(c.grid.ptr, p.output_buffer, sizeof(vis_complex) * ng, cudaMemcpyHostToDevice));
-  else
+  if (p.output_buffer) {
+    if (!bz_copy_async(c.grid.ptr, p.output_buffer, sizeof(vis_complex) * ng, cudaMemcpyHostToDevice, c.stream)) return;
+    BZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
+  } else
     BZ_CUDA_TRY(cudaMemset(c.grid.ptr, 0, sizeof(vis_complex) * ng));
 #if defined(BULLSEYE_SINGLE)
   if (!c.grid_lo.alloc(ng)) return;
@@ -428,9 +456,12 @@ extern "C" void initLibrary(gridding_parameters *pp) {
   if (c.want_sf) {
     const size_t ns = c.F * c.sf_count * nxy;
     if (!c.sf.alloc(ns)) return;
-    if (p.sampling_function_buffer)
-      BZ_CUDA_TRY(cudaMemcpy(c.sf.ptr, p.sampling_function_buffer, sizeof(vis_complex) * ns, cudaMemcpyHostToDevice));
-    else
+    if (p.sampling_function_buffer) {
+      if (!bz_copy_async(c.sf.ptr, p.sampling_function_buffer, sizeof(vis_complex) * ns, cudaMemcpyHostToDevice,
+                         c.stream))
+        return;
+      BZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    } else
       BZ_CUDA_TRY(cudaMemset(c.sf.ptr, 0, sizeof(vis_complex) * ns));
     if (!c.sf_out.alloc(ns)) return;
     const size_t na = c.sf_count * nxy;
@@ -692,9 +723,9 @@ static void copy_back_grids(gridding_parameters &p, bool sampling) {
     c.launches++;
     BZ_CUDA_TRY(cudaEventRecord(c.ev_ready_vis, c.stream));
     BZ_CUDA_TRY(cudaStreamWaitEvent(c.copy_stream, c.ev_ready_vis, 0));
-    if (p.output_buffer)
-      BZ_CUDA_TRY(cudaMemcpyAsync(p.output_buffer, c.scratch.ptr, sizeof(vis_complex) * n, cudaMemcpyDeviceToHost,
-                                  c.copy_stream));
+    if (p.output_buffer && !bz_copy_async(p.output_buffer, c.scratch.ptr, sizeof(vis_complex) * n, cudaMemcpyDeviceToHost,
+                                          c.copy_stream))
+      return;
     BZ_CUDA_TRY(cudaMemcpyAsync(c.norm_host, c.norm.ptr, sizeof(double) * c.F * c.cube * c.C, cudaMemcpyDeviceToHost,
                                 c.copy_stream));
     BZ_CUDA_TRY(cudaEventRecord(c.ev_copied_vis, c.copy_stream));
@@ -707,9 +738,9 @@ static void copy_back_grids(gridding_parameters &p, bool sampling) {
     c.launches++;
     BZ_CUDA_TRY(cudaEventRecord(c.ev_ready_sf, c.stream));
     BZ_CUDA_TRY(cudaStreamWaitEvent(c.copy_stream, c.ev_ready_sf, 0));
-    if (p.sampling_function_buffer)
-      BZ_CUDA_TRY(cudaMemcpyAsync(p.sampling_function_buffer, c.sf_out.ptr, sizeof(vis_complex) * n,
-                                  cudaMemcpyDeviceToHost, c.copy_stream));
+    if (p.sampling_function_buffer && !bz_copy_async(p.sampling_function_buffer, c.sf_out.ptr, sizeof(vis_complex) * n,
+                                                     cudaMemcpyDeviceToHost, c.copy_stream))
+      return;
     BZ_CUDA_TRY(cudaEventRecord(c.ev_copied_sf, c.copy_stream));
   }
 }
@@ -767,13 +798,32 @@ bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool f
       if (c.jones_raw.n < 4 * nj && !c.jones_raw.alloc(4 * nj)) return false;
       // the previous call's inversion must have read the buffer before it is refilled
       BZ_CUDA_TRY_RET(cudaStreamWaitEvent(c.copy_stream, c.ev_jones_read, 0), false);
-      BZ_CUDA_TRY_RET(cudaMemcpyAsync(c.jones_raw.ptr, p.jones_terms, sizeof(vis_complex) * 4 * nj, cudaMemcpyHostToDevice,
-                                      c.copy_stream), false);
+      cudaEvent_t t0 = nullptr, t1 = nullptr;
+      if (bz_tracing()) {
+        bz_trace_mark("jones_alloc");
+        cudaEventCreate(&t0);
+        cudaEventCreate(&t1);
+        cudaEventRecord(t0, c.copy_stream);
+      }
+      if (!bz_copy_async(c.jones_raw.ptr, p.jones_terms, sizeof(vis_complex) * 4 * nj, cudaMemcpyHostToDevice,
+                         c.copy_stream))
+        return false;
+      if (t0) {
+        cudaEventRecord(t1, c.copy_stream);
+        cudaEventSynchronize(t1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, t0, t1);
+        bz_trace_note("jones_copy %s%s %.1f MB %.3f ms %.1f GB/s", bz_host_kind(p.jones_terms),
+                      c.host_copy_sm && bz_mapped_host(p.jones_terms, sizeof(vis_complex) * 4 * nj) ? " (SM copy)" : "",
+                      sizeof(vis_complex) * 4.0 * nj / 1e6, ms, sizeof(vis_complex) * 4.0 * nj / (ms * 1e6));
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+      }
       BZ_CUDA_TRY_RET(cudaEventRecord(c.ev_jones_up, c.copy_stream), false);
       BZ_CUDA_TRY_RET(cudaStreamWaitEvent(c.stream, c.ev_jones_up, 0), false);
       jsrc = c.jones_raw.ptr;
     }
-    bz_trace_mark("jones_alloc_h2d");
+    bz_trace_mark("jones_h2d");
     invert_jones_kernel<<<(unsigned)((nj + 255) / 256), 256, 0, c.stream>>>(jsrc, c.jones_inv.ptr, (long long)nj,
                                                                              c.dev_error.ptr);
     BZ_CUDA_TRY_RET(cudaEventRecord(c.ev_jones_read, c.stream), false);
@@ -1049,16 +1099,17 @@ static void finalize_buffer(vis_complex *host, size_t per_facet_slices, size_t n
   cudaStream_t s = c.stream;
   cudaEventRecord(c.ev_i0, s);
   if (stokes) {
-    BZ_CUDA_TRY(cudaMemcpyAsync(work.ptr, host, sizeof(vis_complex) * F * per_facet_slices * nxy, cudaMemcpyHostToDevice,
-                                s));
+    if (!bz_copy_async(work.ptr, host, sizeof(vis_complex) * F * per_facet_slices * nxy, cudaMemcpyHostToDevice, s))
+      return;
     stokes_combine_kernel<<<2048, 256, 0, s>>>(work.ptr, shifted.ptr, (long long)nxy, (int)F, (int)nslices,
                                                (int)(per_facet_slices / nslices), stokes->a, stokes->b, stokes->sign);
     c.launches++;
   } else {
     // upload the first nslices slices of every facet block
     for (size_t f = 0; f < F; ++f)
-      BZ_CUDA_TRY(cudaMemcpyAsync(shifted.ptr + f * nslices * nxy, host + f * per_facet_slices * nxy,
-                                  sizeof(vis_complex) * nslices * nxy, cudaMemcpyHostToDevice, s));
+      if (!bz_copy_async(shifted.ptr + f * nslices * nxy, host + f * per_facet_slices * nxy,
+                         sizeof(vis_complex) * nslices * nxy, cudaMemcpyHostToDevice, s))
+        return;
   }
   ifftshift_gather_kernel<<<2048, 256, 0, s>>>(shifted.ptr, work.ptr, (int)c.nx, (int)c.ny, (long long)(F * nslices));
   c.launches += 2;  // the gather and the packing kernel (cuFFT's own launches are not counted)
@@ -1083,12 +1134,14 @@ static void finalize_buffer(vis_complex *host, size_t per_facet_slices, size_t n
   // transformed complex slices back into their facet blocks, then the packed float32 images at
   // float index (per_facet_slices * nxy) * f, in that order (fft_and_repacking_routines.cpp:85-117)
   for (size_t f = 0; f < F; ++f)
-    BZ_CUDA_TRY(cudaMemcpyAsync(host + f * per_facet_slices * nxy, shifted.ptr + f * nslices * nxy,
-                                sizeof(vis_complex) * nslices * nxy, cudaMemcpyDeviceToHost, s));
+    if (!bz_copy_async(host + f * per_facet_slices * nxy, shifted.ptr + f * nslices * nxy,
+                       sizeof(vis_complex) * nslices * nxy, cudaMemcpyDeviceToHost, s))
+      return;
   float *hf = reinterpret_cast<float *>(host);
   for (size_t f = 0; f < F; ++f)
-    BZ_CUDA_TRY(cudaMemcpyAsync(hf + f * per_facet_slices * nxy, packed.ptr + f * nslices * nxy, sizeof(float) * nslices * nxy,
-                                cudaMemcpyDeviceToHost, s));
+    if (!bz_copy_async(hf + f * per_facet_slices * nxy, packed.ptr + f * nslices * nxy, sizeof(float) * nslices * nxy,
+                       cudaMemcpyDeviceToHost, s))
+      return;
   cudaEventRecord(c.ev_i1, s);
   BZ_CUDA_TRY(cudaStreamSynchronize(s));
   float ms = 0;

@@ -148,16 +148,40 @@ def _contig(a, dtype=None):
     return np.ascontiguousarray(a if dtype is None else a.astype(dtype, copy=False))
 
 
+def pinned_host(offset: int = 0):
+    """A ``host_alloc`` for run_imaging: every array in its own page-locked (pinned torch) buffer,
+    starting ``offset`` bytes into it (an offset that is not a multiple of the element size gives
+    unaligned arrays)."""
+    import torch
+
+    def new(shape, dtype):
+        dtype = np.dtype(dtype)
+        n = int(np.prod(shape)) * dtype.itemsize
+        buf = torch.empty(n + offset, dtype=torch.uint8, pin_memory=True)
+        return buf.numpy()[offset:offset + n].view(dtype).reshape(shape)
+
+    return new
+
+
 def run_imaging(lib, problem: GriddingProblem, call: str, *, chunks: int = 1, repack: bool = False,
                 uniform: bool = False, psf: bool = False, do_finalize: bool = False,
-                norm_bins: int = 1, keep_raw: bool = False) -> ImagingResult:
+                norm_bins: int = 1, keep_raw: bool = False, host_alloc=None) -> ImagingResult:
     """Run the pipeliner's ABI sequence for ``call`` on ``lib`` and return the host outputs.
 
     ``norm_bins`` is the number of float64 normalisation bins per (facet, cube, correlation)
     that the library publishes: 1 for the CPU libraries (wrapper.cpp:102-105), W*W for the
     GPU library layout (wrapper.cu:222-230).  The returned ``normalization`` is summed over
-    bins.  Caller arrays are copied before every call that may modify them.
+    bins.  Caller arrays are copied before every call that may modify them.  ``host_alloc(shape,
+    dtype)`` makes the caller's grids, rows and Jones terms (numpy memory by default; see
+    pinned_host).
     """
+    alloc = host_alloc or (lambda shape, dtype: np.empty(shape, dtype))
+
+    def place(a):
+        out = alloc(a.shape, a.dtype)
+        out[...] = a
+        return out
+
     if call not in GRID_CALLS:
         raise ValueError(f"unknown gridding call {call!r}")
     n_corr, faceting = GRID_CALLS[call]
@@ -168,9 +192,9 @@ def run_imaging(lib, problem: GriddingProblem, call: str, *, chunks: int = 1, re
     nxy = p.nx * p.ny
     S, Ch = p.spws, p.channels
 
-    grid = np.zeros((F, p.cube, n_corr, p.ny, p.nx), dtype=cd)
+    grid = place(np.zeros((F, p.cube, n_corr, p.ny, p.nx), dtype=cd))
     want_sf = uniform or psf
-    sf = np.zeros((F, p.sampling_channel_count, 1, p.ny, p.nx), dtype=cd) if want_sf else None
+    sf = place(np.zeros((F, p.sampling_channel_count, 1, p.ny, p.nx), dtype=cd)) if want_sf else None
 
     enabled = _contig(p.enabled_channels if p.enabled_channels is not None else np.ones(S * Ch, bool), np.bool_)
     cgi = _contig(p.channel_grid_index if p.channel_grid_index is not None else np.zeros(S * Ch, np.uintp), np.uintp)
@@ -221,12 +245,12 @@ def run_imaging(lib, problem: GriddingProblem, call: str, *, chunks: int = 1, re
         lo, hi = int(bounds[ci]), int(bounds[ci + 1])
         lib.gridding_barrier()
         arrs = dict(
-            vis=_contig(p.vis[lo:hi], cd).copy(), uvw=_contig(p.uvw[lo:hi], rd).copy(),
-            wt=_contig(p.weights[lo:hi], rd).copy(), fl=_contig(p.flags[lo:hi], np.bool_).copy(),
-            fr=_contig(p.flagged_rows[lo:hi], np.bool_).copy(), field=_contig(p.field_ids[lo:hi], np.uint32).copy(),
-            spw=_contig(p.spw_ids[lo:hi], np.uint32).copy(), a1=_contig(p.antenna1[lo:hi], np.uint32).copy(),
-            a2=_contig(p.antenna2[lo:hi], np.uint32).copy(),
-            t=_contig(p.timestamp_ids[lo:hi], np.uintp).copy(),
+            vis=place(_contig(p.vis[lo:hi], cd)), uvw=place(_contig(p.uvw[lo:hi], rd)),
+            wt=place(_contig(p.weights[lo:hi], rd)), fl=place(_contig(p.flags[lo:hi], np.bool_)),
+            fr=place(_contig(p.flagged_rows[lo:hi], np.bool_)), field=place(_contig(p.field_ids[lo:hi], np.uint32)),
+            spw=place(_contig(p.spw_ids[lo:hi], np.uint32)), a1=place(_contig(p.antenna1[lo:hi], np.uint32)),
+            a2=place(_contig(p.antenna2[lo:hi], np.uint32)),
+            t=place(_contig(p.timestamp_ids[lo:hi], np.uintp)),
         )
         keep.append(arrs)
         st.visibilities = _ptr(arrs["vis"])
@@ -248,7 +272,7 @@ def run_imaging(lib, problem: GriddingProblem, call: str, *, chunks: int = 1, re
             st.baseline_starting_indexes = _ptr(starts)
             lib.repack_input_data(ctypes.byref(st))
         if call == "facet_4_cor_corrections":
-            jn = _contig(p.jones, cd).copy()
+            jn = place(_contig(p.jones, cd))
             arrs["jones"] = jn
             st.jones_terms = _ptr(jn)
         getattr(lib, call)(ctypes.byref(st))

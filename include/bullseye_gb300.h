@@ -126,6 +126,16 @@ void bullseye_set_host_repack(int on);
  * is sorted, in one set of class launches.  More groups hide more of the upload but split every
  * class launch, adding a launch tail per group. */
 void bullseye_set_grid_groups(int groups);
+/* Bulk copies between the caller's host buffers (rows, Jones terms, grids) and the device: with
+ * mode 1 (the default) a buffer that lies in one page-locked allocation mapped into the device's
+ * address space (cudaHostAlloc, cudaHostRegister, a pinned torch tensor) is copied by an SM kernel
+ * over the coherent CPU-GPU link; other memory, and every copy with mode 0, goes through
+ * cudaMemcpyAsync (the copy engines).  Results are the same either way. */
+void bullseye_set_host_copy(int mode);
+/* Host-input rows gridded in one group are staged on the device as one chunk per call, so each
+ * baseline's rows form one track; a call whose rows exceed `bytes` of staging (0: the default,
+ * 8 GB) is split into even chunks, sorted and tracked chunk by chunk. */
+void bullseye_set_max_stage_bytes(size_t bytes);
 
 /* Batched, support-aware gridding of every facet of the current chunk: `call` 0 grids like
  * facet_4_cor_corrections, 1 like facet_4_cor, 2 like grid_4_cor; with_sampling != 0 also grids

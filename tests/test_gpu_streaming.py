@@ -1,7 +1,8 @@
-"""Host-input gridding streams its rows: chunks of rows are uploaded on a copy stream, sorted by
-baseline on the device and gridded while the next chunk uploads (rows.cu).
+"""Host-input gridding streams its rows: rows are uploaded on a copy stream and sorted by
+baseline on the device, in one chunk per call, or, gridded in groups, in chunks gridded while the
+next chunk uploads (rows.cu).
 
-* 41 antennas x 80 timesteps = 65,600 cross rows, more than one chunk, in Measurement Set order
+* 41 antennas x 80 timesteps = 65,600 cross rows in Measurement Set order
   (time-major); repack_input_data either permutes the caller's arrays (the reference's behaviour,
   the default) or, with bullseye_set_host_repack(0), only fills the baseline starts.  Both must
   match the FP64 oracle to 1e-12 (64-bit library) and 1e-5 (32-bit), with Jones terms and
@@ -62,7 +63,7 @@ def _reference(p, oracle):
 @pytest.mark.parametrize("form", ["batched", "plain"])
 @pytest.mark.parametrize("chunks", [1, 2])
 def test_streamed_rows_match_oracle(precision, host_repack, form, chunks, many_rows, gpu_libs, oracle_libs):
-    """chunks = 1: one call of 65,600 rows, streamed in two row chunks; chunks = 2: two calls."""
+    """chunks = 1: one call of 65,600 rows; chunks = 2: two calls."""
     from bullseye_gb300.library import check
     p = many_rows.astype(precision)
     lib = gpu_libs[precision]
