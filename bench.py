@@ -96,6 +96,9 @@ def parse():
     ap.add_argument("--clocks-dir", default=None, help="also write the raw nvidia-smi clock samples into this folder")
     ap.add_argument("--grid-groups", type=int, default=1,
                     help="e2e: groups of row chunks gridded while later chunks upload (bullseye_set_grid_groups)")
+    ap.add_argument("--no-records", action="store_true",
+                    help="batched form: prepare every staged visibility in the class launches instead of by the "
+                         "visibility-record kernel (bullseye_set_visibility_records(0))")
     ap.add_argument("--host-copy", type=int, default=1, choices=[0, 1],
                     help="e2e: 1 copies mapped page-locked host buffers with SM kernels, 0 with the copy engines "
                          "(bullseye_set_host_copy)")
@@ -185,6 +188,9 @@ def class_profile(lib, step, counts, plane_width):
     for i in range(min(cnt, n)):
         vis, t = taps.get(int(width[i]), (0, 0.0))
         flops = t * (N_FACETS * 8 * 4 if nc[i] == 4 else 8)
+        if int(width[i]) == 0:  # the visibility-record kernel that precedes the build's class launches
+            rows.append({"kernel": "record_kernel", "corr": int(nc[i]), "ms": float(ms[i])})
+            continue
         rows.append({"width": int(width[i]), "corr": int(nc[i]), "J": int(J[i]), "wide": bool(wide[i] & 1),
                      "registers": int(wide[i]) >> 1,
                      "work_items": int(items[i]), "vis": vis, "ms": float(ms[i]),
@@ -617,6 +623,7 @@ def uneven_main(args):
         facets[f] = BullseyeFacet(float(ra_as), float(dec_as), CELL, CELL, n, n, off)
         off += 4 * n * n
     lib = load_library("GPU", "single")
+    lib.bullseye_set_visibility_records(0 if args.no_records else 1)
     d = device_inputs(geo, torch)
     grids = torch.zeros(off, dtype=torch.complex64, device="cuda")
     lo = torch.zeros(off, dtype=torch.complex64, device="cuda")
@@ -833,6 +840,7 @@ def predict_main(args):
     R = geo["uvw"].shape[0]
     pairs = R * N_CHAN * N_FACETS
     lib = load_library("GPU", "single")
+    lib.bullseye_set_visibility_records(0 if args.no_records else 1)
     d = device_inputs(geo, torch)
     dev = torch.device("cuda")
     # model images: 20 point sources per facet with random fluxes, the same on the 4 correlations
@@ -1203,6 +1211,7 @@ def main():
     from bullseye_gb300.abi import gridding_parameters_type
     from bullseye_gb300.library import check, load_library
     lib = load_library("GPU", "single")
+    lib.bullseye_set_visibility_records(0 if args.no_records else 1)
     d = device_inputs(geo, torch)
     torch.cuda.synchronize()
 

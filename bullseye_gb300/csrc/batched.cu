@@ -159,6 +159,234 @@ __global__ void bucket_kernel(const int4 *__restrict__ segs, const int *total, i
   }
 }
 
+// Exclusive scan of the scheduled segments' row counts by one block: rec_off[i] = rows of the
+// segments before i (in class order), rec_off[n] = all rows; n = the segments of every class.
+__global__ void rec_offsets_kernel(const int4 *__restrict__ sorted, const int *__restrict__ class_count, int ncls,
+                                   long long *__restrict__ rec_off) {
+  __shared__ long long part[1024];
+  int n = 0;
+  for (int k = 0; k < ncls; ++k) n += class_count[k];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int per = (n + nt - 1) / nt;
+  const int lo = min(n, tid * per), hi = min(n, lo + per);
+  long long sum = 0;
+  for (int i = lo; i < hi; ++i) sum += sorted[i].y - sorted[i].x;
+  part[tid] = sum;
+  __syncthreads();
+  for (int off = 1; off < nt; off <<= 1) {
+    const long long v = tid >= off ? part[tid - off] : 0;
+    __syncthreads();
+    part[tid] += v;
+    __syncthreads();
+  }
+  long long run = tid ? part[tid - 1] : 0;
+  for (int i = lo; i < hi; ++i) {
+    rec_off[i] = run;
+    run += sorted[i].y - sorted[i].x;
+  }
+  if (tid == nt - 1) rec_off[n] = part[nt - 1];
+}
+
+// Facets a warp of the record kernel takes at once (its per-facet range and sums sit in shared
+// memory); more facets are taken in blocks, each block reloading the segment's rows.
+constexpr int kRecordFacetBlock = 32;
+constexpr int kRecordWarps = 8;
+
+template <int NC>
+constexpr size_t record_smem_bytes() {
+  return (size_t)kRecordWarps * kRecordFacetBlock * (NC * sizeof(double) + sizeof(int2) + sizeof(int) + sizeof(DfFacet));
+}
+
+// Visibility records of every scheduled segment, one warp per segment taking segments from a
+// counter.  Each lane loads one row of the segment (load_row) and writes its record for every
+// facet (facet_record: the in-place gridder's prologue, so the same cells, taps, corrections and
+// weights) at rec_off[si] x F + f x len + row, with the footprint residues for the segment's class
+// width.  Per facet the warp keeps, in shared memory, the first and last valid row (the work item's
+// range) and the normalisation sums of the current grid group (added to the global sums when the
+// group changes and when the segment ends).  A segment whose records would pass `capacity` is left
+// to the segment kernel's in-place prologue.
+template <int NC, bool WPROJ>
+__global__ void __launch_bounds__(kRecordWarps * 32) record_kernel(
+    const GridArgs a, const int4 *__restrict__ sorted, const int *__restrict__ class_count, int ncls,
+    const long long *__restrict__ rec_off, const int *__restrict__ widths, int nfacets, GridRec<NC> *__restrict__ out,
+    long long capacity, int2 *__restrict__ range, long long range_items, int *next) {
+  extern __shared__ __align__(16) unsigned char rk_smem[];
+  constexpr int FB = kRecordFacetBlock;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double *s_norm = reinterpret_cast<double *>(rk_smem) + (size_t)warp * FB * NC;                  // [FB][NC]
+  int2 *s_rng = reinterpret_cast<int2 *>(rk_smem + (size_t)kRecordWarps * FB * NC * sizeof(double)) +
+                (size_t)warp * FB;                                                                 // [FB]
+  int *s_ng = reinterpret_cast<int *>(rk_smem + (size_t)kRecordWarps * FB * (NC * sizeof(double) + sizeof(int2))) +
+              (size_t)warp * FB;                                                                   // [FB]
+  // single precision: the facets' double-float constants for the segment's spw
+  DfFacet *s_df = reinterpret_cast<DfFacet *>(rk_smem + (size_t)kRecordWarps * FB *
+                                                           (NC * sizeof(double) + sizeof(int2) + sizeof(int))) +
+                  (size_t)warp * FB;                                                               // [FB]
+  (void)s_df;
+  int nseg = 0;
+  for (int k = 0; k < ncls; ++k) nseg += class_count[k];
+  const double plane_scale = WPROJ ? (double)(a.P - 1) / a.wmax : 0.0;
+  const bool want_norm = a.norm != nullptr;
+  for (;;) {
+    int si = 0;
+    if (lane == 0) si = atomicAdd(next, 1);
+    si = __shfl_sync(0xffffffffu, si, 0);
+    if (si >= nseg) break;
+    const int4 sg = sorted[si];
+    if (sg.x < 0 || sg.x > sg.y || (long long)sg.y > a.nrows || sg.z < 0 || sg.z >= a.nchan || sg.w < 0 ||
+        sg.w >= ncls) {
+      if (lane == 0) atomicOr(a.error, DEV_ERR_GRID_INDEX);
+      continue;
+    }
+    const int len = sg.y - sg.x;
+    if ((rec_off[si] + len) * nfacets > capacity) continue;
+    GridRec<NC> *seg_out = out + rec_off[si] * nfacets;
+    // residues mod the class width by a multiply-high (exact for corners below 2^26), corrected
+    const unsigned Wc = (unsigned)widths[sg.w];
+    const unsigned mag = 0xffffffffu / Wc + 1u;
+    // the segment's spw (its first row's): rows of that spw use the double-float cell choice
+    unsigned dspw = 0xffffffffu;
+    double dinv = 0.0;
+#if defined(BULLSEYE_SINGLE)
+    {
+      const unsigned s0 = a.spw[sg.x];
+      if (len > 0 && s0 < (unsigned)a.nspw) {
+        dspw = s0;
+        dinv = 1.0 / (double)a.wavelengths[(long long)s0 * a.nchan + sg.z];
+      }
+    }
+#endif
+    for (int f0 = 0; f0 < nfacets; f0 += FB) {
+      const int fb = min(FB, nfacets - f0);
+      for (int j = lane; j < fb; j += 32) {
+        s_rng[j] = make_int2(0x7fffffff, 0);
+        s_ng[j] = -1;
+#pragma unroll
+        for (int k = 0; k < NC; ++k) s_norm[j * NC + k] = 0.0;
+#if defined(BULLSEYE_SINGLE)
+        if (dspw != 0xffffffffu) df_facet(a.facets[f0 + j], dinv, a.os, s_df[j]);
+#endif
+      }
+      __syncwarp();
+      unsigned cspw = 0xffffffffu;
+      double inv = 0.0;
+      for (int b = 0; b < len; b += 32) {
+        const int i = b + lane;
+        RowInputs<NC> ri;
+        load_row<NC>(a, sg.z, (long long)sg.x + i, i < len, ri);
+        if (ri.use && ri.spw != cspw) {
+          cspw = ri.spw;
+          inv = 1.0 / (double)a.wavelengths[ri.sc];
+        }
+        // the w plane does not depend on the facet: choose_cells' FP64 expression, once per row
+        const bool use_df = ri.use && ri.spw == dspw;
+        int plane_df = 0;
+        if (WPROJ && use_df) {
+          const double pl = rint(fabs(ri.wm) * (inv * plane_scale));
+          plane_df = (pl >= 0.0 && pl < (double)a.P) ? (int)pl : -1;
+        }
+        for (int fj = 0; fj < fb; ++fj) {
+          const int f = f0 + fj;
+          VisRec<NC> rec;
+          facet_record<NC, WPROJ>(a, f, sg.z, (long long)sg.x + i, ri, inv, rec, plane_scale,
+                                  use_df ? &s_df[fj] : nullptr, plane_df);
+          const bool v = i < len && rec.valid;
+          if (i < len) {
+            GridRec<NC> g;
+            if (v) {
+              const unsigned u0 = (unsigned)rec.u0, v0 = (unsigned)rec.v0;
+              int ru = (int)(u0 - __umulhi(u0, mag) * Wc), rv = (int)(v0 - __umulhi(v0, mag) * Wc);
+              ru += ru < 0 ? (int)Wc : 0;
+              rv += rv < 0 ? (int)Wc : 0;
+              g.u0 = rec.u0; g.v0 = rec.v0; g.ru = ru; g.rv = rv;
+              g.g = rec.g; g.valid = 1; g.fu = rec.fu; g.fv = rec.fv;
+#pragma unroll
+              for (int k = 0; k < NC; ++k) g.vis[k] = rec.vis[k];
+            } else {
+              g.u0 = g.v0 = g.ru = g.rv = g.g = g.valid = g.fu = g.fv = 0;
+#pragma unroll
+              for (int k = 0; k < NC; ++k) g.vis[k].re = g.vis[k].im = 0;
+            }
+            seg_out[(long long)f * len + i] = g;
+          }
+          const unsigned m = __ballot_sync(0xffffffffu, v);
+          if (!m) continue;
+          if (lane == 0) {
+            int2 r = s_rng[fj];
+            if (r.x == 0x7fffffff) r.x = b + __ffs(m) - 1;
+            r.y = b + 32 - __clz(m);
+            s_rng[fj] = r;
+          }
+          if (!want_norm) continue;
+          NormTerm t[NC];
+          const int gv = v ? rec.g : -1;
+          if (v) {
+            NormTerm nt;
+#if defined(BULLSEYE_SINGLE)
+            if (a.tap_sums_f) {  // single precision: the row sums rounded to FP32, multiplied in FP32
+              const float *su = a.tap_sums_f + 2 * ((long long)rec.plane * a.tap_f + rec.fu0);
+              const float *sv = a.tap_sums_f + 2 * ((long long)rec.plane * a.tap_f + rec.fv0);
+              nt = fmaf(su[0], sv[0], -__fmul_rn(su[1], sv[1]));
+            } else
+#endif
+            {
+              const double *su = a.tap_sums + 2 * ((long long)rec.plane * a.tap_f + rec.fu0);
+              const double *sv = a.tap_sums + 2 * ((long long)rec.plane * a.tap_f + rec.fv0);
+              nt = (NormTerm)(su[0] * sv[0] - su[1] * sv[1]);
+            }
+#pragma unroll
+            for (int k = 0; k < NC; ++k) t[k] = (NormTerm)rec.cw[k] * nt;
+          } else {
+#pragma unroll
+            for (int k = 0; k < NC; ++k) t[k] = 0;
+          }
+          const int g0 = __shfl_sync(0xffffffffu, gv, __ffs(m) - 1);
+          const long long fslice = (long long)(a.facet_base + f) * a.groups;
+          if (__all_sync(0xffffffffu, gv < 0 || gv == g0)) {
+            if (lane == 0 && s_ng[fj] != g0) {
+              if (s_ng[fj] >= 0) {
+#pragma unroll
+                for (int k = 0; k < NC; ++k)
+                  if (s_norm[fj * NC + k] != 0.0) atomicAdd(&a.norm[(fslice + s_ng[fj]) * NC + k], s_norm[fj * NC + k]);
+              }
+#pragma unroll
+              for (int k = 0; k < NC; ++k) s_norm[fj * NC + k] = 0.0;
+              s_ng[fj] = g0;
+            }
+            // a warp's 32 terms are summed in the working precision (positive terms: a relative
+            // error of a few FP32 units at most), the sums of the warps in FP64
+#pragma unroll
+            for (int k = 0; k < NC; ++k) {
+              NormTerm x = t[k];
+#pragma unroll
+              for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+              if (lane == 0) s_norm[fj * NC + k] += (double)x;
+            }
+          } else if (v) {
+#pragma unroll
+            for (int k = 0; k < NC; ++k)
+              if (t[k] != 0) atomicAdd(&a.norm[(fslice + gv) * NC + k], (double)t[k]);
+          }
+        }
+      }
+      __syncwarp();
+      // the block's work-item ranges and remaining sums
+      for (int j = lane; j < fb; j += 32) {
+        const long long item = (long long)si * nfacets + f0 + j;
+        const int2 r = s_rng[j];
+        if (item < range_items) range[item] = r.x == 0x7fffffff ? make_int2(0, 0) : r;
+        if (want_norm && s_ng[j] >= 0) {
+          const long long fslice = (long long)(a.facet_base + f0 + j) * a.groups;
+#pragma unroll
+          for (int k = 0; k < NC; ++k)
+            if (s_norm[j * NC + k] != 0.0) atomicAdd(&a.norm[(fslice + s_ng[j]) * NC + k], s_norm[j * NC + k]);
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
 // ---------------------------------------------------------------- launch variants
 // A thread layout of one support class; NT = 0 marks a layout not chosen for the current build.
 struct Variant {
@@ -260,6 +488,15 @@ struct BatchedState {
   };
   std::vector<ClassRecord> records;
   std::vector<int> plane_width;  // class width of every w plane (plan_classes)
+  // precomputed visibility records (record_kernel): the buffer and its budget, the per-segment
+  // record offsets, the per-item valid ranges, the class widths on the device, a work counter
+  bool vrec_on = true;
+  size_t vrec_budget = 0;        // bytes; 0: 30 % of the device's memory
+  DevBuf<unsigned char> vrec;
+  DevBuf<long long> vrec_off;    // [segs_cap + 1]
+  DevBuf<int2> vrec_range;
+  long long vrec_range_items = 0;
+  DevBuf<int> cls_width, vrec_next;
 };
 BatchedState g_bs;
 
@@ -349,6 +586,12 @@ bool plan_classes() {
     b.cls[k].vis = Variant();  // chosen again (from the tuned decisions) for each call's build
     b.cls[k].sf = Variant();
   }
+  {
+    int wd[kMaxClasses] = {0};
+    for (int k = 0; k < b.ncls; ++k) wd[k] = widths[k];
+    if (!b.cls_width.alloc(kMaxClasses)) return false;
+    BZ_CUDA_TRY_RET(cudaMemcpy(b.cls_width.ptr, wd, sizeof(wd), cudaMemcpyHostToDevice), false);
+  }
   if (!b.plane_class.alloc(P) || !b.plane_lo.alloc(P)) return false;
   BZ_CUDA_TRY_RET(cudaMemcpy(b.plane_class.ptr, pcls.data(), sizeof(int) * P, cudaMemcpyHostToDevice), false);
   BZ_CUDA_TRY_RET(cudaMemcpy(b.plane_lo.ptr, plo.data(), sizeof(int) * P, cudaMemcpyHostToDevice), false);
@@ -395,6 +638,83 @@ bool open_smem(Kern kern) {
     return false;
   return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes) ==
          cudaSuccess;
+}
+
+// Sizes the visibility-record buffers for a call of `rows` rows over nfacets facets (before any
+// capture: the captured launches hold their addresses).  The records take at most the record
+// budget and the free memory; segments past the capacity are gridded in place.  `segments` (the
+// schedule's segment count, 0 when unknown) sizes the per-item range table.
+bool ensure_records(int nfacets, long long rows, int nchan, long long segments) {
+  BatchedState &b = g_bs;
+  if (!b.vrec_on || !b.conv_w.ptr || rows <= 0) return true;
+  size_t fr = 0, tot = 0;
+  if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+    cudaGetLastError();
+    return true;
+  }
+  const size_t budget = b.vrec_budget ? b.vrec_budget : tot / 10 * 3;
+  const double need = (double)std::max(nfacets, 1) * (double)rows * nchan * sizeof(GridRec<4>);
+  const void *before[3] = {b.vrec.ptr, b.vrec_off.ptr, b.vrec_range.ptr};
+  const double room = (double)b.vrec.n + (double)fr * 0.8;
+  const size_t want = (size_t)(std::min(need, std::min((double)budget, room)) / 256) * 256;
+  if (want > b.vrec.n && want >= (1u << 20)) {
+    b.vrec.release();
+    if (!b.vrec.alloc(want)) return false;
+  }
+  if (b.vrec_off.n < b.segs_cap + 1 && !b.vrec_off.alloc(b.segs_cap + 1)) return false;
+  const long long seg = segments > 0 ? segments + segments / 4 + 4096 : std::min<long long>((long long)b.segs_cap, 1 << 20);
+  const long long items = seg * std::max(nfacets, 1);
+  if (items > b.vrec_range_items) {
+    if (!b.vrec_range.alloc((size_t)items)) return false;
+    b.vrec_range_items = items;
+  }
+  if (!b.vrec_next.ptr && !b.vrec_next.alloc(1)) return false;
+  if (before[0] != b.vrec.ptr || before[1] != b.vrec_off.ptr || before[2] != b.vrec_range.ptr) b.drop_graphs();
+  return true;
+}
+
+template <int NC>
+void set_record_args(GridArgs &a) {
+  BatchedState &b = g_bs;
+  a.records = b.vrec.ptr;
+  a.rec_off = b.vrec_off.ptr;
+  a.item_range = b.vrec_range.ptr;
+  a.rec_capacity = (long long)(b.vrec.n / sizeof(GridRec<NC>));
+  a.range_capacity = b.vrec_range_items;
+}
+
+// The visibility records of this build's work items (all classes) ahead of its class launches;
+// `out` is `base` with the record arguments, or `base` itself when records are off or cannot be
+// used (no record buffer, no support-window table, or normalisation without kernel row sums).
+template <int NC, bool WPROJ>
+bool launch_records(const GridArgs &base, int nfacets, cudaStream_t st, GridArgs &out) {
+  BatchedState &b = g_bs;
+  out = base;
+  if (!b.vrec_on || !b.vrec.ptr || !b.vrec_off.ptr || !b.vrec_range.ptr || !b.conv_w.ptr || !b.cls_width.ptr ||
+      (base.norm && !base.tap_sums))
+    return true;
+  GridArgs a = base;
+  a.plane_lo = b.plane_lo.ptr;
+  a.conv_w = b.conv_w.ptr;
+  a.conv_w_stride = b.conv_w_stride;
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  BZ_CUDA_TRY_RET(cudaMemsetAsync(b.vrec_next.ptr, 0, sizeof(int), st), false);
+  rec_offsets_kernel<<<1, 1024, 0, st>>>(b.sorted.ptr, b.class_count.ptr, b.ncls, b.vrec_off.ptr);
+  record_kernel<NC, WPROJ><<<sms * 4, kRecordWarps * 32, record_smem_bytes<NC>(), st>>>(
+      a, b.sorted.ptr, b.class_count.ptr, b.ncls, b.vrec_off.ptr,
+                                                    b.cls_width.ptr, nfacets, reinterpret_cast<GridRec<NC> *>(b.vrec.ptr),
+                                                    (long long)(b.vrec.n / sizeof(GridRec<NC>)), b.vrec_range.ptr,
+                                                    b.vrec_range_items, b.vrec_next.ptr);
+  g_ctx.launches += 2;
+  BZ_CUDA_TRY_RET(cudaGetLastError(), false);
+  set_record_args<NC>(out);
+  return true;
 }
 
 template <int NC, bool WPROJ, bool COMP>
@@ -514,16 +834,38 @@ bool tune_class(const GridArgs &base, int k, int nfacets, Variant &out, int host
 
 template <int NC, bool WPROJ, bool COMP>
 bool tune_all(const GridArgs &base, int nfacets, bool sampling, const std::vector<int> &counts) {
+  GridArgs tb = base, rb;
+  tb.norm = nullptr;  // tuning launches leave the normalisation alone
+  if (!launch_records<NC, WPROJ>(tb, nfacets, g_ctx.stream, rb)) return false;
   for (int k = 0; k < g_bs.ncls; ++k) {
     Variant &v = sampling ? g_bs.cls[k].sf : g_bs.cls[k].vis;
-    if (!tune_class<NC, WPROJ, COMP>(base, k, nfacets, v, counts[k])) return false;
+    if (!tune_class<NC, WPROJ, COMP>(rb, k, nfacets, v, counts[k])) return false;
   }
   return true;
 }
 
 template <int NC, bool WPROJ, bool COMP>
-bool launch_all(const GridArgs &base, int nfacets, bool sampling, cudaStream_t st, const std::vector<int> *counts) {
+bool launch_all(const GridArgs &base_in, int nfacets, bool sampling, cudaStream_t st, const std::vector<int> *counts) {
   BatchedState &b = g_bs;
+  GridArgs base;
+  {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (b.profile) {
+      cudaEventCreate(&e0);
+      cudaEventCreate(&e1);
+      cudaEventRecord(e0, st);
+    }
+    if (!launch_records<NC, WPROJ>(base_in, nfacets, st, base)) return false;
+    if (b.profile) {
+      cudaEventRecord(e1, st);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      if (base.records) b.records.push_back({0, NC, 0, 0, 0, ms});  // width 0: the record kernel
+    }
+  }
   for (int k = 0; k < b.ncls; ++k) {
     const Variant &v = sampling ? b.cls[k].sf : b.cls[k].vis;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -610,6 +952,8 @@ void bz_release_batched() {
   b.work_next.release(); b.sample_count.release(); b.segs.release(); b.sorted.release(); b.facet_table.release();
   b.conv_w.release();
   b.conv_w_stride = 0;
+  b.vrec.release(); b.vrec_off.release(); b.vrec_range.release(); b.cls_width.release(); b.vrec_next.release();
+  b.vrec_range_items = 0;
   b.rows_cap = b.tracks_cap = b.segs_cap = 0;
   b.planned = false;
   b.ncls = 0;
@@ -620,6 +964,15 @@ extern "C" void bullseye_set_batched_profiling(int on) { g_bs.profile = on != 0;
 
 // See include/bullseye_gb300.h.
 extern "C" void bullseye_set_grid_groups(int groups) { g_ctx.grid_groups = groups < 1 ? 1 : groups; }
+
+// See include/bullseye_gb300.h.
+extern "C" void bullseye_set_visibility_records(int on) {
+  if (g_bs.vrec_on != (on != 0)) g_bs.drop_graphs();
+  g_bs.vrec_on = on != 0;
+}
+
+// See include/bullseye_gb300.h.
+extern "C" void bullseye_set_record_budget(size_t bytes) { g_bs.vrec_budget = bytes; }
 
 namespace {
 // Self-test of the bounded tap-barrier wait: the barrier expects two arrivals and gets one, so
@@ -691,12 +1044,16 @@ int run_batched(const GridArgs &va, const GridArgs *sa, int nfacets, const GridA
   key[sizeof(GridArgs) * 2 + 2] = (unsigned char)vis;
   std::memcpy(key.data() + sizeof(GridArgs) * 2 + 4, &nfacets, sizeof(int));
 
+  // the eager schedule's class counts; the record buffers are sized from them before any tuning
+  // or capture
   auto schedule_counts = [&](std::vector<int> &counts) -> bool {
     if (!enqueue_schedule(va, c.stream)) return false;
     BZ_CUDA_TRY_RET(cudaMemcpyAsync(counts.data(), b.class_count.ptr, sizeof(int) * kMaxClasses, cudaMemcpyDeviceToHost,
                                     c.stream), false);
     BZ_CUDA_TRY_RET(cudaStreamSynchronize(c.stream), false);
-    return true;
+    long long nseg = 0;
+    for (int k = 0; k < b.ncls; ++k) nseg += counts[k];
+    return ensure_records(std::max(nfacets, tune_facets), va.nrows, va.nchan, nseg);
   };
   if (b.profile) {
     std::vector<int> counts(kMaxClasses, 0);
@@ -743,7 +1100,8 @@ int run_batched(const GridArgs &va, const GridArgs *sa, int nfacets, const GridA
   slot->used = ++b.graph_clock;
   bz_trace_mark("schedule_tune_capture");
   BZ_CUDA_TRY_RET(cudaGraphLaunch(slot->exec, c.stream), BZ_ERR_CUDA);
-  c.launches += 6 + (long long)b.ncls * ((vis ? 1 : 0) + (sf ? 1 : 0));
+  const int rec = b.vrec_on && b.vrec.ptr && b.conv_w.ptr ? 2 : 0;  // record offsets + record kernel per build
+  c.launches += 6 + (long long)(b.ncls + rec) * ((vis ? 1 : 0) + (sf ? 1 : 0));
   return BZ_OK;
 }
 
@@ -787,6 +1145,7 @@ bool stream_visibilities(gridding_parameters &p, const GridArgs &va, int nfacets
     return run_batched(va, nullptr, nfacets, va, nfacets, wproj, comp, name, true) == BZ_OK;
   }
   std::vector<int> counts(kMaxClasses, 0);
+  if (!ensure_records(nfacets, (long long)p.row_count, (int)c.nchan, 0)) return false;
   int k0 = 0;
   long long g_r0 = 0;
   auto chunk = [&](int k, long long r0, long long r1) -> bool {

@@ -98,6 +98,7 @@ struct Context {
   // sum over the W taps of every (plane, tap offset) kernel row, FP64 complex [P][2 os + 1][2]:
   // a visibility's normalisation term is Re(S[plane][fu] * S[plane][fv])
   DevBuf<double> tap_sums;
+  DevBuf<float> tap_sums_f;  // the same rounded to FP32 (the single-precision record kernel)
   size_t tap_f = 0;
   // the kernel table regrouped by tap offset, [P][tap_f][W] (real or complex like conv): the W taps
   // a visibility reads are contiguous, so staging them is a coalesced copy

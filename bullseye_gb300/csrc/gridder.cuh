@@ -95,6 +95,7 @@ struct GridArgs {
   const size_t *cgi;
   const void *conv;              // real [K] or complex [P][K]
   const double *tap_sums;        // FP64 complex [P][tap_f] row sums of the kernel, or null
+  const float *tap_sums_f;       // the same rounded to FP32 (the single-precision record kernel), or null
   int tap_f;
   const void *conv_t;            // kernel regrouped by tap offset [P][tap_f][W], or null
   const void *conv_w;            // support-window rows [P][tap_f][conv_w_stride], or null (see
@@ -125,6 +126,12 @@ struct GridArgs {
   const int *segment_base;       // persistent mode: index of this launch's first segment (device)
   long long segment_capacity;    // persistent mode: entries in segments
   int *work_next;                // persistent mode: work-item counter (device, zeroed before launch)
+  // persistent mode with precomputed visibility records (or null: records are computed in place)
+  const void *records;           // GridRec<NC> of every work item, item (si, f) at rec_off[si] x F + f x len
+  const long long *rec_off;      // per scheduled segment: records of the segments before it
+  const int2 *item_range;        // per work item si x F + f: its valid records [x, y) (x >= y: none)
+  long long rec_capacity;        // records the buffer holds (a segment past it is gridded in place)
+  long long range_capacity;      // entries of item_range (items past it grid all their records)
   unsigned imaging_field;
   double u_scale, v_scale, gcx, gcy, wmax;
 };
@@ -158,6 +165,16 @@ struct __align__(16) VisRec {
   int plane, fu0, fv0, pad0;  // w plane; tap offsets before the support-window shift
   cplx vis[NC];            // weighted, corrected, rotated visibility
   acc_real cw[NC];         // weight x flag per correlation (normalisation)
+};
+
+// What the multiply-add loop reads of a staged visibility: a VisRec without its normalisation
+// fields.  The visibility-record kernel writes one per (row, facet, channel) of a call; the
+// persistent segment kernel then stages them by bulk copies (sizes a multiple of 16 bytes).
+template <int NC>
+struct __align__(16) GridRec {
+  int u0, v0, ru, rv;      // footprint corner and its residues mod the class width
+  int g, valid, fu, fv;    // grid group, validity, support-window table rows
+  cplx vis[NC];            // weighted, corrected, rotated visibility
 };
 
 __device__ __forceinline__ void load_tap(const void *conv, long long idx, acc_real &t) {
@@ -440,6 +457,362 @@ __device__ __forceinline__ bool choose_cells(double um, double vm, double wm, co
   return true;
 }
 
+// ------------------------------------------------------------ double-float cell choice
+// Single-precision library, record kernel: the cell, tap and phase choice of choose_cells with
+// pairs of floats in place of FP64 (GB300 issues FP64 at 1/64 of FP32, and the FP64 pipe bounds a
+// prologue that keeps about 40 FP64 operations per visibility and facet).  A pair hi + lo
+// (|lo| <= ulp(hi) / 2) carries about 48 significant bits; sums use Knuth's error-free TwoSum,
+// products the FMA form of Dekker's TwoProduct (products by __fmul_rn, which is never contracted
+// into an FMA).  Per facet and spw the FP64 constants are split into pairs once (DfFacet); each
+// visibility then needs FP32 arithmetic only.  Roundings decide on the exact high part and use
+// the low part at ties, so cells and taps agree with the FP64 choice except where the two
+// computations round a value within about 1e-12 pixel of a boundary differently.
+struct DF {
+  float hi, lo;
+};
+struct DfFacet {
+  DF pu, pv, pw;  // phase: dl / lambda, dm / lambda, dn / lambda (turns per metre)
+  DF su, sv;      // pixels per metre: (1 / lambda) x u_scale, (1 / lambda) x v_scale
+  DF ut, vt;      // planar uv transform terms
+  int gcx, gcy;   // footprint-corner offsets nx/2 - s, ny/2 - s
+  float osf;      // oversampling factor
+};
+#if defined(BULLSEYE_SINGLE)
+__device__ __forceinline__ DF df_split(double x) {
+  DF r;
+  r.hi = (float)x;
+  r.lo = (float)(x - (double)r.hi);
+  return r;
+}
+__device__ __forceinline__ DF df_quick(float a, float b) {  // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return DF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ DF df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return DF{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  const DF s = df_two_sum(a.hi, b.hi);
+  return df_quick(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ DF df_mul_f(DF a, float b) {
+  const float p = __fmul_rn(a.hi, b);
+  const float e = fmaf(a.lo, b, fmaf(a.hi, b, -p));
+  return df_quick(p, e);
+}
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  const float e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, fmaf(a.hi, b.hi, -p)));
+  return df_quick(p, e);
+}
+
+// Round half to even, and the int of an integer-valued float, for |x| < 2^22: adding 1.5 x 2^23
+// leaves unit spacing, so the sum is the rounded value and its bits count it (FP32 adds on the
+// FMA pipe instead of the rounding and conversion instructions).
+__device__ __forceinline__ float rint22(float x) { return __fsub_rn(__fadd_rn(x, 12582912.f), 12582912.f); }
+__device__ __forceinline__ int int22(float k) { return __float_as_int(__fadd_rn(k, 12582912.f)) - 0x4B400000; }
+__device__ __forceinline__ float floor22(float x) {
+  const float r = rint22(x);
+  return r > x ? __fsub_rn(r, 1.f) : r;
+}
+
+__device__ __forceinline__ void df_facet(const FacetXform &fx, double inv, int os, DfFacet &k) {
+  k.osf = (float)os;
+  k.pu = df_split(fx.dl * inv);
+  k.pv = df_split(fx.dm * inv);
+  k.pw = df_split(fx.dn * inv);
+  k.su = df_split(inv * fx.u_scale);
+  k.sv = df_split(inv * fx.v_scale);
+  k.ut = df_split(fx.u_term);
+  k.vt = df_split(fx.v_term);
+  k.gcx = (int)fx.gcx;
+  k.gcy = (int)fx.gcy;
+}
+
+// Rounds x (|x| < 2^22) to the nearest integer, halves to even like rint (round = true), or down
+// like floor; d = x - r as a pair.  hi - r is exact (Sterbenz), and a low part cannot carry x past
+// the next rounding boundary unless hi sits on it.
+__device__ __forceinline__ void df_round(DF x, bool round, float &r, DF &d) {
+  if (round) {
+    r = rint22(x.hi);
+    const float h = __fsub_rn(x.hi, r);
+    if (h == 0.5f && x.lo > 0.f) {
+      r = __fadd_rn(r, 1.f);
+      d = DF{-0.5f, x.lo};
+    } else if (h == -0.5f && x.lo < 0.f) {
+      r = __fsub_rn(r, 1.f);
+      d = DF{0.5f, x.lo};
+    } else {
+      d = DF{h, x.lo};
+    }
+  } else {
+    r = floor22(x.hi);
+    const float h = __fsub_rn(x.hi, r);
+    if (h == 0.f && x.lo < 0.f) {
+      r = __fsub_rn(r, 1.f);
+      d = DF{1.f, x.lo};
+    } else {
+      d = DF{h, x.lo};
+    }
+  }
+}
+
+// trunc((1 - d) x os) for 1 - d > 0 (the tap offset), with the low part deciding at integers.
+__device__ __forceinline__ int df_tap(DF d, float osf) {
+  DF e = df_two_sum(1.f, -d.hi);
+  e = df_quick(e.hi, __fsub_rn(e.lo, d.lo));
+  e = df_mul_f(e, osf);
+  float k = floor22(e.hi);
+  if (e.hi == k && e.lo < 0.f) k = __fsub_rn(k, 1.f);
+  return int22(k);
+}
+
+// choose_cells with the facet's pairs k and the row's w plane (computed per row in FP64: it does
+// not depend on the facet; -1 when out of range).
+template <bool WPROJ>
+__device__ __forceinline__ bool choose_cells_df(float um, float vm, float wm, const DfFacet &k, int plane, bool phase,
+                                                bool uvx, int nx, int ny, int Wf, int P, int os, cplx &ph,
+                                                CellChoice &out) {
+  ph.re = 1;
+  ph.im = 0;
+  if (phase) {
+    const DF t = df_add(df_add(df_mul_f(k.pu, um), df_mul_f(k.pv, vm)), df_mul_f(k.pw, wm));
+    const float r = fabsf(t.hi) < 4194304.f ? rint22(t.hi) : rintf(t.hi);
+    const float f = __fadd_rn(__fsub_rn(t.hi, r), t.lo);
+    float sn, cs;
+    sincospif(2.0f * f, &sn, &cs);
+    ph.re = cs;
+    ph.im = sn;
+  }
+  DF u, v;
+  if (uvx) {
+    const DF pu = df_mul_f(k.ut, wm), pv = df_mul_f(k.vt, wm);
+    u = df_mul(df_add(DF{um, 0.f}, DF{-pu.hi, -pu.lo}), k.su);
+    v = df_mul(df_add(DF{vm, 0.f}, DF{-pv.hi, -pv.lo}), k.sv);
+  } else {
+    u = df_mul_f(k.su, um);
+    v = df_mul_f(k.sv, vm);
+  }
+  out.flip = WPROJ && wm < 0;
+  if (out.flip) {
+    u = DF{-u.hi, -u.lo};
+    v = DF{-v.hi, -v.lo};
+  }
+  // corners far off the grid (or not finite) are rejected before rounding
+  if (!(fabsf(u.hi) < 4194304.f && fabsf(v.hi) < 4194304.f)) return false;
+  float ru, rv;
+  DF du_f, dv_f;
+  df_round(u, WPROJ, ru, du_f);
+  df_round(v, WPROJ, rv, dv_f);
+  const int du = int22(ru) + k.gcx, dv = int22(rv) + k.gcy;
+  if (!(du >= 0 && dv >= 0 && du + (Wf + 2) < nx && dv + (Wf + 2) < ny && plane >= 0 && plane < P)) return false;
+  out.fu = df_tap(du_f, k.osf);
+  out.fv = df_tap(dv_f, k.osf);
+  out.du = du;
+  out.dv = dv;
+  out.plane = plane;
+  return true;
+}
+#endif
+
+// The facet-independent part of a visibility's prologue: one (row, channel)'s checks and inputs.
+template <int NC>
+struct RowInputs {
+  bool use;            // in range, channel enabled, spw and grid group valid, Jones indices valid
+  bool row_ok;         // not flagged, in the imaging field
+  unsigned spw;
+  int g;               // grid group (cube channel)
+  long long sc;        // spw x nchan + channel
+  long long jt1, jt2;  // Jones rows t x nant + antenna (four correlations with Jones)
+  double um, vm, wm;
+  vis_real uvw_in[3];  // as stored (the double-float cell choice starts from them)
+  cplx vis[NC];
+  acc_real wt[NC];
+  bool fl[NC];
+};
+
+template <int NC>
+__device__ __forceinline__ void load_row(const GridArgs &a, int chan, long long row, bool in_range, RowInputs<NC> &ri) {
+  ri.use = false;
+  if (!in_range) return;
+  const int c = chan;
+  const unsigned spw = a.spw[row];
+  if (spw >= (unsigned)a.nspw) {
+    atomicOr(a.error, DEV_ERR_GRID_INDEX);
+    return;
+  }
+  const long long sc = (long long)spw * a.nchan + c;
+  if (!a.enabled[sc]) return;
+  const size_t g = a.cgi[sc];
+  if (g >= (size_t)a.groups) {
+    atomicOr(a.error, DEV_ERR_GRID_INDEX);
+    return;
+  }
+  ri.spw = spw;
+  ri.sc = sc;
+  ri.g = (int)g;
+  ri.uvw_in[0] = a.uvw[3 * row];
+  ri.uvw_in[1] = a.uvw[3 * row + 1];
+  ri.uvw_in[2] = a.uvw[3 * row + 2];
+  ri.um = (double)ri.uvw_in[0];
+  ri.vm = (double)ri.uvw_in[1];
+  ri.wm = (double)ri.uvw_in[2];
+  ri.row_ok = !a.flagged_rows[row] && (a.field[row] == a.imaging_field);
+  const long long base = ((long long)row * a.nchan + c) * a.npol;
+  if (a.mode == CORR_SAMPLING) {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) { ri.vis[k].re = 1; ri.vis[k].im = 0; ri.wt[k] = 1; ri.fl[k] = false; }
+  } else if (NC == 1 || NC == 2) {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+      int pi = (k == 0) ? a.pol0 : a.pol1;
+      vis_complex vv = a.vis[base + pi];
+      ri.vis[k].re = vv.re; ri.vis[k].im = vv.im;
+      ri.wt[k] = (acc_real)a.weights[base + pi];
+      ri.fl[k] = a.flags[base + pi] != 0;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+      vis_complex vv = a.vis[base + k];
+      ri.vis[k].re = vv.re; ri.vis[k].im = vv.im;
+      ri.wt[k] = (acc_real)a.weights[base + k];
+      ri.fl[k] = a.flags[base + k] != 0;
+    }
+  }
+  ri.jt1 = ri.jt2 = 0;
+  if (NC == 4 && a.mode == CORR_QUAD_JONES) {
+    const long long t = (long long)a.time_ids[row];
+    const unsigned a1 = a.ant1[row], a2 = a.ant2[row];
+    if (t < 0 || t >= a.ntimes || a1 >= (unsigned)a.nant || a2 >= (unsigned)a.nant) {
+      atomicOr(a.error, DEV_ERR_JONES_INDEX);
+      return;
+    }
+    ri.jt1 = t * a.nant + a1;
+    ri.jt2 = t * a.nant + a2;
+  }
+  ri.use = true;
+}
+
+// The facet part of the prologue: the row's Jones correction for facet f_local, weights and flags,
+// cells, taps, phase rotation and flip, into rec (valid = 0 when the row is left out of the facet
+// or its footprint is off the grid).  inv = 1 / lambda of the row's channel.
+template <int NC, bool WPROJ>
+__device__ __forceinline__ void facet_record(const GridArgs &a, int f_local, int chan, long long row,
+                                             const RowInputs<NC> &ri, double inv, VisRec<NC> &rec,
+                                             const double plane_scale, const DfFacet *dk = nullptr,
+                                             int plane_df = -1) {
+  rec.valid = 0;
+  if (!ri.use) return;
+  const int c = chan;
+  const int fglob = a.facet_base + f_local;
+  // a row left out of this facet (uneven facet layouts) is skipped like an off-grid visibility
+  if (a.facet_row_mask && !a.facet_row_mask[(long long)fglob * a.nrows + row]) return;
+  const FacetXform &fx = a.facets[f_local];
+  cplx vis[NC];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) vis[k] = ri.vis[k];
+  if (NC == 4 && a.mode == CORR_QUAD_JONES) {
+    // V <- J_p^-1 (V J_q^-H)   (correlation_gridding_policies.h:523-542; terms pre-inverted)
+    const long long i1 = (((ri.jt1 * a.nfacets_total + fglob) * a.nspw + ri.spw) * a.nchan + c) * 4;
+    const long long i2 = (((ri.jt2 * a.nfacets_total + fglob) * a.nspw + ri.spw) * a.nchan + c) * 4;
+    cplx P[4], Q[4], T[4], O[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      vis_complex p = a.jones_inv[i1 + k], q = a.jones_inv[i2 + k];
+      P[k].re = p.re; P[k].im = p.im;
+      Q[k].re = q.re; Q[k].im = q.im;
+    }
+    // hermitian transpose of Q
+    cplx qh[4];
+    qh[0].re = Q[0].re; qh[0].im = -Q[0].im;
+    qh[1].re = Q[2].re; qh[1].im = -Q[2].im;
+    qh[2].re = Q[1].re; qh[2].im = -Q[1].im;
+    qh[3].re = Q[3].re; qh[3].im = -Q[3].im;
+    jmul(vis, qh, T);
+    jmul(P, T, O);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) vis[k] = O[k];
+  }
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
+    bool keep = !(ri.fl[k] || !ri.row_ok);
+    acc_real cw = keep ? ri.wt[k] : (acc_real)0;
+    rec.cw[k] = cw;
+    vis[k].re *= cw;
+    vis[k].im *= cw;
+  }
+  CellChoice cell;
+  cplx ph;
+#if defined(BULLSEYE_SINGLE)
+  if (dk) {
+    if (!choose_cells_df<WPROJ>((float)ri.uvw_in[0], (float)ri.uvw_in[1], (float)ri.uvw_in[2], *dk, plane_df,
+                                a.phase != 0, a.uvx != 0, fx.nx, fx.ny, a.W_full ? a.W_full : a.W, a.P, a.os, ph,
+                                cell))
+      return;
+  } else
+#endif
+  {
+    ChanCache cc;
+    cc.spw = ri.spw;
+    cc.inv = inv;
+    cc.su = inv * fx.u_scale;
+    cc.sv = inv * fx.v_scale;
+    cc.sw = inv * plane_scale;
+    if (!choose_cells<WPROJ>(ri.um, ri.vm, ri.wm, cc, fx, a.phase != 0, a.uvx != 0, fx.u_scale, fx.v_scale,
+                             plane_scale, fx.gcx, fx.gcy, fx.nx, fx.ny, a.W_full ? a.W_full : a.W, a.P, a.os, ph, cell))
+      return;
+  }
+  if (a.phase) {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) vis[k] = cmul(vis[k], ph);
+  }
+  if (cell.flip) {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) vis[k].im = -vis[k].im;
+  }
+  const long long plane = cell.plane;
+  int du = cell.du, dv = cell.dv;
+  rec.fu = cell.fu;
+  rec.fv = cell.fv;
+  rec.fu0 = cell.fu;
+  rec.fv0 = cell.fv;
+  int lo = 0;
+  if (a.plane_lo) {
+    // support-aware: grid only the plane's nonzero window of a.W taps (the taps outside it are
+    // exactly zero), shifting the footprint corner and the tap offsets by the window start
+    lo = a.plane_lo[plane];
+    du += lo;
+    dv += lo;
+    rec.fu += lo * a.os;
+    rec.fv += lo * a.os;
+  }
+  if (a.conv_w) {
+    // start of the (plane, tap offset) row of the support-window table (window start included)
+    rec.fu = (int)(((long long)plane * a.tap_f + cell.fu) * a.conv_w_stride);
+    rec.fv = (int)(((long long)plane * a.tap_f + cell.fv) * a.conv_w_stride);
+  } else if (a.conv_t) {
+    // index of the first staged tap in the regrouped table
+    const int Wfull = a.W_full ? a.W_full : a.W;
+    rec.fu = (int)(((long long)plane * a.tap_f + cell.fu) * Wfull + lo);
+    rec.fv = (int)(((long long)plane * a.tap_f + cell.fv) * Wfull + lo);
+  }
+  rec.plane = (int)plane;
+  rec.u0 = du;
+  rec.v0 = dv;
+  rec.ru = du % a.W;
+  rec.rv = dv % a.W;
+  rec.g = ri.g;
+#pragma unroll
+  for (int k = 0; k < NC; ++k) rec.vis[k] = vis[k];
+  rec.valid = 1;
+}
+
+// One visibility's prologue in one facet, in one piece for the in-place gridder (fewer values live
+// at once than load_row + facet_record, which the record kernel uses; both make the same record
+// from the same arithmetic).  cc keeps the per-channel constants while the spw stays the same.
 template <int NC, bool WPROJ>
 __device__ __forceinline__ void prologue(const GridArgs &a, int f_local, int chan, long long row, bool in_range,
                                          VisRec<NC> &rec, ChanCache &cc, const double plane_scale) {
@@ -612,11 +985,19 @@ __host__ __device__ inline int tap_row_v(int W, int J) {
   return (W + J - 1 + E - 1) / E * E;
 }
 
-// Bytes before the tap arrays: V staged records, their normalisation state (partial sums, grid
-// group), the V + 1 run starts of the chunk; rounded up to 16.
+// Bytes before the tap arrays, rounded up to 16: computed in place, V staged records, their
+// normalisation state (partial sums, grid group) and the V + 1 run starts of the chunk; from
+// precomputed records, two buffers of V GridRecs (one filled while the other is gridded) and the
+// run starts.  A launch reserves the larger, so each work item may take either form.
+template <int NC>
+__host__ __device__ inline size_t stage_head_per_vis() {
+  const size_t own = sizeof(VisRec<NC>) + sizeof(NormAcc) * NC + 2 * sizeof(int);
+  const size_t pre = 2 * sizeof(GridRec<NC>) + sizeof(int);
+  return own > pre ? own : pre;
+}
 template <int NC>
 __host__ __device__ inline size_t stage_head_bytes(int V) {
-  return ((sizeof(VisRec<NC>) + sizeof(NormAcc) * NC + 2 * sizeof(int)) * (size_t)V + sizeof(int) + 15) / 16 * 16;
+  return (stage_head_per_vis<NC>() * (size_t)V + sizeof(int) + 15) / 16 * 16;
 }
 
 template <int NC, bool WPROJ>
@@ -634,7 +1015,7 @@ __host__ inline int grid_chunk_size(int W, int nthreads, int J, int regs = 128) 
   size_t budget = std::min<size_t>(200 * 1024, smem_sm / ctas - 1024);
   const size_t fixed = flush_queue_bytes<NC>((nthreads + 31) / 32) + 64 + sizeof(int) + 15;
   budget = budget > fixed ? budget - fixed : 0;
-  const size_t per = sizeof(VisRec<NC>) + sizeof(NormAcc) * NC + 2 * sizeof(int) +
+  const size_t per = stage_head_per_vis<NC>() +
                      sizeof(typename TapT<WPROJ>::type) * (size_t)(tap_row_u<WPROJ>(W) + tap_row_v<WPROJ>(W, J));
   return std::max(1, (int)std::min<size_t>(nthreads, budget / per));
 }
@@ -724,8 +1105,8 @@ __device__ __forceinline__ void norm_slot(const GridArgs &a, const VisRec<NC> &r
 // Runs of a staged chunk, found by one warp: maximal stretches of valid staged visibilities with
 // one footprint corner and grid group (a Romein thread keeps its cells across a run); an invalid
 // slot is a run of its own.  runs[0..n) are the first slots of the runs, runs[n] = nv.
-template <int NC>
-__device__ __forceinline__ void find_runs(const VisRec<NC> *recs, int nv, int *runs, int *nruns) {
+template <class Rec>
+__device__ __forceinline__ void find_runs(const Rec *recs, int nv, int *runs, int *nruns) {
   const int lane = threadIdx.x & 31;
   int count = 0;
   for (int b = 0; b < nv; b += 32) {
@@ -841,6 +1222,9 @@ __device__ __forceinline__ bool bar_wait(unsigned long long *bar, unsigned parit
   }
   return false;
 }
+// Orders this thread's earlier shared-memory accesses (and those a CTA barrier published to it)
+// before its following bulk copies into shared memory.
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
 // One bulk (TMA) copy global -> shared of `bytes` (16-byte aligned addresses, a multiple of 16
 // bytes) that completes its bytes on the barrier.
 __device__ __forceinline__ void bulk_copy(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
@@ -853,8 +1237,8 @@ __device__ __forceinline__ void bulk_copy(void *dst, const void *src, unsigned b
 // Bulk-copy staging of a chunk's taps from the support-window table: staging slot tid copies its
 // visibility's column row (TUS taps) and row row (TVS taps, the repeated leading taps included) as
 // two bulk copies and arrives on the barrier with their bytes; an empty slot arrives without bytes.
-template <int NC, bool WPROJ>
-__device__ __forceinline__ void stage_taps_bulk(const GridArgs &a, const VisRec<NC> *recs, int nv, int TUS, int TVS,
+template <int NC, bool WPROJ, class Rec>
+__device__ __forceinline__ void stage_taps_bulk(const GridArgs &a, const Rec *recs, int nv, int TUS, int TVS,
                                                 typename TapT<WPROJ>::type *tu, typename TapT<WPROJ>::type *tv,
                                                 unsigned long long *bar) {
   typedef typename TapT<WPROJ>::type tap_t;
@@ -931,8 +1315,8 @@ __device__ __forceinline__ void norm_from_taps(const GridArgs &a, const VisRec<N
 // compensated flush in single precision; the queue is drained when it fills and at the end of the
 // track).  Every lane of a warp with any owned cell calls this, so the queue drains are
 // warp-uniform.
-template <int NC, bool WPROJ, int J, bool COMP>
-__device__ __forceinline__ void grid_runs(const GridArgs &a, const VisRec<NC> *recs,
+template <int NC, bool WPROJ, int J, bool COMP, class Rec>
+__device__ __forceinline__ void grid_runs(const GridArgs &a, const Rec *recs,
                                           const typename TapT<WPROJ>::type *tu,
                                           const typename TapT<WPROJ>::type *tv, const int *runs, int nruns,
                                           int TUS, int TVS, int du, int strip, unsigned rows_mask, long long fbase,
@@ -1089,7 +1473,7 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
       stage_taps_bulk<NC, WPROJ>(a, recs, nv, TUS, TVS, tu, tv, bar);
     else
       stage_taps<NC, WPROJ>(a, recs, nv, J, TUS, TVS, tu, tv);
-    if (warp_id == 0) find_runs<NC>(recs, nv, s_runs, &s_nruns);
+    if (warp_id == 0) find_runs(recs, nv, s_runs, &s_nruns);
     if (want_norm && a.tap_sums && tid < nv) norm_slot<NC>(a, recs[tid], tid, s_nacc, s_ng, fslice);
     if (bulk) {
       // every thread observes the phase (the copies' data is visible to the threads that do);
@@ -1148,6 +1532,110 @@ __device__ __forceinline__ void grid_track(const GridArgs &a, const int f_local,
   }
 }
 
+// One work item from precomputed records: its n records (src, 16-byte aligned) are staged V at a
+// time by one bulk copy each into two buffers used in turn, the next chunk's copy in flight while
+// the current chunk's taps arrive and its runs are gridded; the tap rows are bulk copies as in
+// grid_track.  No prologue and no normalisation here (the record kernel did both).  rbar are the
+// two record barriers (one arrival each), rphase their phase parities (bit b for buffer b); a
+// copy is only issued for a chunk of this item, so none is in flight when the item ends.
+template <int NC, bool WPROJ, int J, bool COMP, bool WIDE>
+__device__ __forceinline__ void grid_track_pre(const GridArgs &a, const int f_local, const GridRec<NC> *src, int n,
+                                               unsigned long long *rbar, unsigned &rphase, unsigned long long *bar,
+                                               unsigned &phase) {
+  typedef typename TapT<WPROJ>::type tap_t;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int V = a.V, W = a.W;
+  const int TUS = tap_row_u<WPROJ>(W), TVS = tap_row_v<WPROJ>(W, J);
+  GridRec<NC> *rb = reinterpret_cast<GridRec<NC> *>(smem_raw);  // [2][V]
+  int *s_runs = reinterpret_cast<int *>(rb + 2 * V);             // [V + 1]
+  tap_t *tu = reinterpret_cast<tap_t *>(smem_raw + stage_head_bytes<NC>(V));
+  tap_t *tv = tu + V * TUS;
+  unsigned char *qbase = reinterpret_cast<unsigned char *>(tv + V * TVS);
+  qbase = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(qbase) + 15) & ~(uintptr_t)15);
+  const int warp_id = threadIdx.x >> 5, nwarps = (blockDim.x + 31) >> 5;
+  FlushRec<NC> *fq = reinterpret_cast<FlushRec<NC> *>(qbase) + warp_id * kFlushQueueCap;
+  int *fqn = reinterpret_cast<int *>(qbase + nwarps * sizeof(FlushRec<NC>) * kFlushQueueCap) + warp_id * 4;
+  if (COMP && (threadIdx.x & 31) == 0) *fqn = 0;
+  __shared__ int s_nruns_pre;
+  if (n <= 0) return;
+
+  const FacetXform &fxt = a.facets[f_local];
+  const int gnx = fxt.nx;
+  const long long nxy = (long long)fxt.nx * fxt.ny;
+  const long long fbase = fxt.grid_base;
+  const int tid = threadIdx.x;
+  int du, strip;
+  bool owner;
+  owner_map<WIDE>(tid, W, J, du, strip, owner);
+  unsigned rows_mask = 0;
+#pragma unroll
+  for (int j = 0; j < J; ++j)
+    if (strip * J + j < W) rows_mask |= 1u << j;
+  if (!owner) rows_mask = 0;
+  const bool grids = __any_sync(0xffffffffu, rows_mask != 0);
+
+  OwnerState<NC, J> st;
+#pragma unroll
+  for (int j = 0; j < J; ++j) {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) { st.acc[j][k].re = 0; st.acc[j][k].im = 0; }
+  }
+  st.dirty = 0;
+  st.cg = -1;
+  st.pu0 = -1;
+  st.pv0 = -1;
+  st.ou = 0;
+  st.ov0 = 0;
+
+  const int nchunks = (n + V - 1) / V;
+  if (tid == 0) {
+    // the buffers may last have been written by plain stores (an item prepared in place)
+    fence_proxy_async();
+    const unsigned bytes = (unsigned)(sizeof(GridRec<NC>) * (size_t)min(V, n));
+    bar_arrive_tx(&rbar[0], bytes);
+    bulk_copy(rb, src, bytes, &rbar[0]);
+  }
+  int cur = 0;
+  for (int c = 0; c < nchunks; ++c, cur ^= 1) {
+    const int nv = min(V, n - c * V);
+    const unsigned par = (rphase >> cur) & 1u;
+    if (!bar_wait(&rbar[cur], par)) {
+      atomicOr(a.error, DEV_ERR_WAIT_TIMEOUT);
+      bar_wait(&rbar[cur], par);
+    }
+    rphase ^= 1u << cur;
+    const GridRec<NC> *recs = rb + cur * V;
+    stage_taps_bulk<NC, WPROJ>(a, recs, nv, TUS, TVS, tu, tv, bar);
+    if (tid == 0 && c + 1 < nchunks) {
+      // the other buffer was last read by the previous chunk, which every thread has finished
+      const unsigned bytes = (unsigned)(sizeof(GridRec<NC>) * (size_t)min(V, n - (c + 1) * V));
+      fence_proxy_async();
+      bar_arrive_tx(&rbar[cur ^ 1], bytes);
+      bulk_copy(rb + (cur ^ 1) * V, src + (size_t)(c + 1) * V, bytes, &rbar[cur ^ 1]);
+    }
+    if (warp_id == 0) find_runs(recs, nv, s_runs, &s_nruns_pre);
+    if (!bar_wait(bar, phase)) {
+      atomicOr(a.error, DEV_ERR_WAIT_TIMEOUT);
+      bar_wait(bar, phase);
+    }
+    phase ^= 1u;
+    __syncthreads();
+    if (grids)
+      grid_runs<NC, WPROJ, J, COMP>(a, recs, tu, tv, s_runs, s_nruns_pre, TUS, TVS, du, strip, rows_mask, fbase, nxy,
+                                    gnx, fq, fqn, st);
+    __syncthreads();
+  }
+  if (COMP && grids) drain_queue<NC>(a, nxy, fq, fqn);
+  if (st.dirty) {
+#pragma unroll
+    for (int j = 0; j < J; ++j) {
+      const int oy = st.ov0 + j >= W ? st.ov0 + j - W : st.ov0 + j;
+      if (st.dirty & (1u << j))
+        flush_cell<NC, COMP>(a, fbase + (long long)st.cg * NC * nxy, nxy, gnx, st.pu0 + st.ou, st.pv0 + oy, st.acc[j]);
+    }
+  }
+}
+
 // Default register budget of the persistent segment kernel: the J = 4 layout (32 accumulator
 // registers) is capped at 80 registers per thread so that more warps stay resident; J = 8 keeps the
 // 128 that 512 threads allow.  The w-projection visibility launches also offer J = 4 builds at 64 and
@@ -1187,8 +1675,13 @@ __global__ void __launch_bounds__(512, 1) __maxnreg__(REGS) romein_segment_kerne
   __shared__ int s_item;
   __shared__ int s_first, s_last;  // unmasked row range of the item (facet row masks)
   __shared__ __align__(8) unsigned long long s_tap_bar;
-  unsigned phase = 0;
-  if (threadIdx.x == 0) bar_init(&s_tap_bar, (unsigned)a.V);
+  __shared__ __align__(8) unsigned long long s_rec_bar[2];
+  unsigned phase = 0, rphase = 0;
+  if (threadIdx.x == 0) {
+    bar_init(&s_tap_bar, (unsigned)a.V);
+    bar_init(&s_rec_bar[0], 1);
+    bar_init(&s_rec_bar[1], 1);
+  }
   const int count = *a.work_count;
   const long long total = (long long)count * nfacets;
   for (;;) {
@@ -1212,6 +1705,27 @@ __global__ void __launch_bounds__(512, 1) __maxnreg__(REGS) romein_segment_kerne
     if (sg.x < 0 || sg.x > sg.y || (long long)sg.y > a.nrows || sg.z < 0 || sg.z >= a.nchan) {
       if (threadIdx.x == 0) atomicOr(a.error, DEV_ERR_GRID_INDEX);
       continue;
+    }
+    if (a.records) {
+      // records of this item, when the record kernel had room for its segment: only the item's
+      // first to last valid record (all of them past the range table)
+      const long long len = (long long)sg.y - sg.x;
+      const long long first = a.rec_off[si] * nfacets;
+      if ((a.rec_off[si] + len) * nfacets <= a.rec_capacity) {
+        const long long it = si * nfacets + f_local;
+        int lo = 0, hi = (int)len;
+        if (it < a.range_capacity) {
+          const int2 rg = a.item_range[it];
+          lo = rg.x;
+          hi = rg.y;
+        }
+        if (lo < hi) {
+          const GridRec<NC> *src =
+              reinterpret_cast<const GridRec<NC> *>(a.records) + first + (long long)f_local * len + lo;
+          grid_track_pre<NC, WPROJ, J, COMP, WIDE>(a, f_local, src, hi - lo, s_rec_bar, rphase, &s_tap_bar, phase);
+        }
+        continue;
+      }
     }
     long long r0 = sg.x, r1 = sg.y;
     if (a.facet_row_mask) {

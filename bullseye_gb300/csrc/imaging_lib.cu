@@ -415,6 +415,9 @@ extern "C" void initLibrary(gridding_parameters *pp) {
       }
     if (!c.tap_sums.alloc(sums.size())) return;
     BZ_CUDA_TRY(cudaMemcpy(c.tap_sums.ptr, sums.data(), sizeof(double) * sums.size(), cudaMemcpyHostToDevice));
+    std::vector<float> sums_f(sums.begin(), sums.end());
+    if (!c.tap_sums_f.alloc(sums_f.size())) return;
+    BZ_CUDA_TRY(cudaMemcpy(c.tap_sums_f.ptr, sums_f.data(), sizeof(float) * sums_f.size(), cudaMemcpyHostToDevice));
     // regrouped table: entry (plane, f, j) = conv[plane][f + j os], zero past the row
     const size_t ncomp = wproj ? 2 : 1;
     std::vector<vis_real> regrouped(ncomp * c.P * c.tap_f * W, (vis_real)0);
@@ -486,7 +489,7 @@ extern "C" void releaseLibrary() {
   if (c.stream) cudaStreamSynchronize(c.stream);
   if (c.copy_stream) cudaStreamSynchronize(c.copy_stream);
   // buffers go back to the library's memory pool (ordered on the library stream)
-  c.conv.release(); c.tap_sums.release(); c.conv_t.release(); c.wavelengths.release(); c.facet_centres.release(); c.enabled.release();
+  c.conv.release(); c.tap_sums.release(); c.tap_sums_f.release(); c.conv_t.release(); c.wavelengths.release(); c.facet_centres.release(); c.enabled.release();
   c.cgi.release(); c.sf_cgi.release(); c.vis.release(); c.weights.release(); c.uvw.release();
   c.flags.release(); c.flagged_rows.release(); c.field.release(); c.spw.release(); c.ant1.release();
   c.ant2.release(); c.time_ids.release(); c.starts.release(); c.jones_raw.release(); c.jones_inv.release();
@@ -875,6 +878,7 @@ bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool f
   a.cgi = sampling ? c.sf_cgi.ptr : c.cgi.ptr;
   a.conv = c.conv.ptr;
   a.tap_sums = c.tap_sums.ptr;
+  a.tap_sums_f = c.tap_sums_f.ptr;
   a.tap_f = (int)c.tap_f;
   a.conv_t = c.conv_t.ptr;
   a.facets = table.ptr;

@@ -70,6 +70,8 @@ EXTENSIONS = {
     "bullseye_set_grid_groups": (None, [ctypes.c_int]),
     "bullseye_set_host_copy": (None, [ctypes.c_int]),
     "bullseye_set_max_stage_bytes": (None, [ctypes.c_size_t]),
+    "bullseye_set_visibility_records": (None, [ctypes.c_int]),
+    "bullseye_set_record_budget": (None, [ctypes.c_size_t]),
     "bullseye_reset_counters": (None, []),
     "bullseye_zero_grids": (None, []),
     "bullseye_set_gridding_correction": (None, [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t]),

@@ -136,6 +136,15 @@ void bullseye_set_host_copy(int mode);
  * baseline's rows form one track; a call whose rows exceed `bytes` of staging (0: the default,
  * 8 GB) is split into even chunks, sorted and tracked chunk by chunk. */
 void bullseye_set_max_stage_bytes(size_t bytes);
+/* Visibility records (on by default): before its per-class launches, a batched call writes one
+ * record per (row, facet, channel) of its work (footprint corner, tap rows, grid group, and the
+ * weighted, Jones-corrected, phase-rotated visibility, 64 bytes in single precision) and its
+ * normalisation sums, by a kernel that takes every row in parallel; the class launches then stage
+ * records and tap rows by bulk copies only.  The records take at most the record budget (0: the
+ * default, 30 % of the device's memory) and the free memory; work past it is prepared in place, as
+ * with records off.  Results are the same either way. */
+void bullseye_set_visibility_records(int on);
+void bullseye_set_record_budget(size_t bytes);
 
 /* Batched, support-aware gridding of every facet of the current chunk: `call` 0 grids like
  * facet_4_cor_corrections, 1 like facet_4_cor, 2 like grid_4_cor; with_sampling != 0 also grids
