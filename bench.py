@@ -1428,6 +1428,7 @@ def main():
             from bullseye_gb300.sharding import max_over_ranks
             dt = max_over_ranks(dt, device="cuda")
         e2e_clk = e2e_clocks.stop()
+        ms_by_call = {k: round(v / n_e2e, 1) for k, v in parts.items()}
         # one more step with phase tracing (it synchronises at phase boundaries, so it is not timed)
         lib.bullseye_set_tracing(1)
         e2e_step()
@@ -1445,7 +1446,7 @@ def main():
         d2h = tab.grid.nbytes + tab.sf.nbytes + N_FACETS * NX * NX * (8 + 4)
         e2e = {"value": pairs_per_step * world / dt / 1e6, "unit": "Mvis/s", "h2d_bytes_per_step": int(h2d * world),
                "d2h_bytes_per_step": int(d2h * world), "s_per_step": dt,
-               "ms_by_call": {k: round(v / n_e2e, 1) for k, v in parts.items()}, "clocks": e2e_clk,
+               "ms_by_call": ms_by_call, "clocks": e2e_clk,
                "trace_of_one_step_ms": trace, "grid_groups": args.grid_groups, "copy_bandwidth": bw,
                "host_copy": "SM kernels" if args.host_copy else "copy engines",
                "calls": ("initLibrary, repack_input_data (baseline starts; rows sorted on the device), "

@@ -834,9 +834,14 @@ bool tune_class(const GridArgs &base, int k, int nfacets, Variant &out, int host
 
 template <int NC, bool WPROJ, bool COMP>
 bool tune_all(const GridArgs &base, int nfacets, bool sampling, const std::vector<int> &counts) {
-  GridArgs tb = base, rb;
+  // records for the timing runs only when some class has work and no layout decided yet (a
+  // decided class takes its layout without launching)
+  bool timing = false;
+  for (int k = 0; k < g_bs.ncls; ++k)
+    if (counts[k] > 0 && !g_bs.tuned.count(std::make_tuple(g_bs.cls[k].width, NC, (int)WPROJ, (int)COMP))) timing = true;
+  GridArgs tb = base, rb = base;
   tb.norm = nullptr;  // tuning launches leave the normalisation alone
-  if (!launch_records<NC, WPROJ>(tb, nfacets, g_ctx.stream, rb)) return false;
+  if (timing && !launch_records<NC, WPROJ>(tb, nfacets, g_ctx.stream, rb)) return false;
   for (int k = 0; k < g_bs.ncls; ++k) {
     Variant &v = sampling ? g_bs.cls[k].sf : g_bs.cls[k].vis;
     if (!tune_class<NC, WPROJ, COMP>(rb, k, nfacets, v, counts[k])) return false;

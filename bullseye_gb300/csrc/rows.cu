@@ -130,9 +130,19 @@ __global__ void link_copy_kernel(const unsigned char *__restrict__ src, unsigned
   const size_t head = mis < n ? mis : n;
   const size_t units = (n - head) / unit;
   if (unit == 16) {
+    // four independent 16-byte loads in flight per thread before their stores (the link's latency
+    // is long); the tail goes one unit at a time
     const int4 *s = reinterpret_cast<const int4 *>(src + head);
     int4 *d = reinterpret_cast<int4 *>(dst + head);
-    for (size_t i = tid; i < units; i += stride) d[i] = s[i];
+    size_t i = tid;
+    for (; i + 3 * stride < units; i += 4 * stride) {
+      const int4 a0 = s[i], a1 = s[i + stride], a2 = s[i + 2 * stride], a3 = s[i + 3 * stride];
+      d[i] = a0;
+      d[i + stride] = a1;
+      d[i + 2 * stride] = a2;
+      d[i + 3 * stride] = a3;
+    }
+    for (; i < units; i += stride) d[i] = s[i];
   } else if (unit == 4) {
     const unsigned *s = reinterpret_cast<const unsigned *>(src + head);
     unsigned *d = reinterpret_cast<unsigned *>(dst + head);
