@@ -65,6 +65,7 @@ struct Context {
   cudaStream_t stream = nullptr;
   // host <-> device copies of the row chunks and the grids overlap the library stream's kernels
   cudaStream_t copy_stream = nullptr;
+  cudaStream_t jones_stream = nullptr;  // the Jones terms' upload, beside the rows on the copy stream
   cudaEvent_t ev_stage_full[2] = {nullptr, nullptr}, ev_stage_free[2] = {nullptr, nullptr};
   cudaEvent_t ev_jones_up = nullptr, ev_jones_read = nullptr, ev_ready_vis = nullptr, ev_ready_sf = nullptr;
   cudaEvent_t ev_copied_vis = nullptr, ev_copied_sf = nullptr;

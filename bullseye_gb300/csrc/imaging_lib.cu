@@ -147,6 +147,7 @@ void bz_trace_mark(const char *phase) {
   if (!g_trace.on) return;
   if (g_ctx.stream) cudaStreamSynchronize(g_ctx.stream);
   if (g_ctx.copy_stream) cudaStreamSynchronize(g_ctx.copy_stream);
+  if (g_ctx.jones_stream) cudaStreamSynchronize(g_ctx.jones_stream);
   const auto now = std::chrono::steady_clock::now();
   const double ms = std::chrono::duration<double, std::milli>(now - g_trace.last).count();
   g_trace.last = now;
@@ -296,6 +297,7 @@ extern "C" void gridding_barrier() {
   if (!g_ctx.initialized || !g_ctx.stream) return;
   cudaError_t e = cudaStreamSynchronize(g_ctx.stream);
   if (e == cudaSuccess && g_ctx.copy_stream) e = cudaStreamSynchronize(g_ctx.copy_stream);
+  if (e == cudaSuccess && g_ctx.jones_stream) e = cudaStreamSynchronize(g_ctx.jones_stream);
   if (e != cudaSuccess) {
     bz_record_error(BZ_ERR_CUDA, "gridding_barrier: %s", cudaGetErrorString(e));
     return;
@@ -366,6 +368,7 @@ extern "C" void initLibrary(gridding_parameters *pp) {
   }
   BZ_CUDA_TRY(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
   BZ_CUDA_TRY(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
+  BZ_CUDA_TRY(cudaStreamCreateWithFlags(&c.jones_stream, cudaStreamNonBlocking));
   for (cudaEvent_t *ev : {&c.ev_stage_full[0], &c.ev_stage_full[1], &c.ev_stage_free[0], &c.ev_stage_free[1], &c.ev_jones_up,
                           &c.ev_jones_read, &c.ev_ready_vis, &c.ev_ready_sf, &c.ev_copied_vis, &c.ev_copied_sf})
     BZ_CUDA_TRY(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
@@ -488,6 +491,7 @@ extern "C" void releaseLibrary() {
   if (!c.initialized) return;
   if (c.stream) cudaStreamSynchronize(c.stream);
   if (c.copy_stream) cudaStreamSynchronize(c.copy_stream);
+  if (c.jones_stream) cudaStreamSynchronize(c.jones_stream);
   // buffers go back to the library's memory pool (ordered on the library stream)
   c.conv.release(); c.tap_sums.release(); c.tap_sums_f.release(); c.conv_t.release(); c.wavelengths.release(); c.facet_centres.release(); c.enabled.release();
   c.cgi.release(); c.sf_cgi.release(); c.vis.release(); c.weights.release(); c.uvw.release();
@@ -513,6 +517,8 @@ extern "C" void releaseLibrary() {
   }
   if (c.copy_stream) cudaStreamDestroy(c.copy_stream);
   c.copy_stream = nullptr;
+  if (c.jones_stream) cudaStreamDestroy(c.jones_stream);
+  c.jones_stream = nullptr;
   if (c.stream) cudaStreamDestroy(c.stream);
   c.stream = nullptr;
   if (c.norm_host) cudaFreeHost(c.norm_host);
@@ -797,22 +803,22 @@ bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool f
     if (c.jones_inv.n < 4 * nj && !c.jones_inv.alloc(4 * nj)) return false;
     const vis_complex *jsrc = p.jones_terms;
     if (!c.device_inputs) {
-      // on the copy stream, ahead of the row chunks this call streams next
+      // on its own stream, beside the row upload on the copy stream
       if (c.jones_raw.n < 4 * nj && !c.jones_raw.alloc(4 * nj)) return false;
       // the previous call's inversion must have read the buffer before it is refilled
-      BZ_CUDA_TRY_RET(cudaStreamWaitEvent(c.copy_stream, c.ev_jones_read, 0), false);
+      BZ_CUDA_TRY_RET(cudaStreamWaitEvent(c.jones_stream, c.ev_jones_read, 0), false);
       cudaEvent_t t0 = nullptr, t1 = nullptr;
       if (bz_tracing()) {
         bz_trace_mark("jones_alloc");
         cudaEventCreate(&t0);
         cudaEventCreate(&t1);
-        cudaEventRecord(t0, c.copy_stream);
+        cudaEventRecord(t0, c.jones_stream);
       }
       if (!bz_copy_async(c.jones_raw.ptr, p.jones_terms, sizeof(vis_complex) * 4 * nj, cudaMemcpyHostToDevice,
-                         c.copy_stream))
+                         c.jones_stream))
         return false;
       if (t0) {
-        cudaEventRecord(t1, c.copy_stream);
+        cudaEventRecord(t1, c.jones_stream);
         cudaEventSynchronize(t1);
         float ms = 0;
         cudaEventElapsedTime(&ms, t0, t1);
@@ -822,7 +828,7 @@ bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool f
         cudaEventDestroy(t0);
         cudaEventDestroy(t1);
       }
-      BZ_CUDA_TRY_RET(cudaEventRecord(c.ev_jones_up, c.copy_stream), false);
+      BZ_CUDA_TRY_RET(cudaEventRecord(c.ev_jones_up, c.jones_stream), false);
       BZ_CUDA_TRY_RET(cudaStreamWaitEvent(c.stream, c.ev_jones_up, 0), false);
       jsrc = c.jones_raw.ptr;
     }

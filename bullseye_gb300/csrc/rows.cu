@@ -7,7 +7,7 @@
 //
 // Host copies.  Bulk copies of the caller's page-locked buffers run as SM kernels over the
 // coherent CPU-GPU link (bz_copy_async): copy-engine transfers of host buffers that have sat idle
-// between calls were measured at 13-30 GB/s, SM copies of the same buffers at 145-211 GB/s.
+// between calls were measured at 13-30 GB/s, SM copies of the same buffers at 110-211 GB/s.
 //
 // Rows.  A gridding call with host inputs uploads its rows (in the caller's order) into a staging
 // buffer on a copy stream; on the library stream they are sorted by baseline slot (a stable radix
@@ -78,6 +78,7 @@ void bz_dev_free(void *p) {
 extern "C" void bullseye_trim_memory(void) {
   if (g_ctx.stream) cudaStreamSynchronize(g_ctx.stream);
   if (g_ctx.copy_stream) cudaStreamSynchronize(g_ctx.copy_stream);
+  if (g_ctx.jones_stream) cudaStreamSynchronize(g_ctx.jones_stream);
   cudaMemPool_t pool = device_pool();
   if (pool) cudaMemPoolTrimTo(pool, 0);
 }
@@ -130,17 +131,17 @@ __global__ void link_copy_kernel(const unsigned char *__restrict__ src, unsigned
   const size_t head = mis < n ? mis : n;
   const size_t units = (n - head) / unit;
   if (unit == 16) {
-    // four independent 16-byte loads in flight per thread before their stores (the link's latency
-    // is long); the tail goes one unit at a time
+    // eight independent 16-byte loads in flight per thread before their stores (the link's
+    // latency is long); the tail goes one unit at a time
     const int4 *s = reinterpret_cast<const int4 *>(src + head);
     int4 *d = reinterpret_cast<int4 *>(dst + head);
     size_t i = tid;
-    for (; i + 3 * stride < units; i += 4 * stride) {
-      const int4 a0 = s[i], a1 = s[i + stride], a2 = s[i + 2 * stride], a3 = s[i + 3 * stride];
-      d[i] = a0;
-      d[i + stride] = a1;
-      d[i + 2 * stride] = a2;
-      d[i + 3 * stride] = a3;
+    for (; i + 7 * stride < units; i += 8 * stride) {
+      int4 a[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) a[q] = s[i + q * stride];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) d[i + q * stride] = a[q];
     }
     for (; i < units; i += stride) d[i] = s[i];
   } else if (unit == 4) {
