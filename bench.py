@@ -180,7 +180,7 @@ def class_profile(lib, step, counts, plane_width):
         step()
     finally:
         lib.bullseye_set_batched_profiling(0)
-    n = 32
+    n = 128
     arrs = [np.zeros(n, np.int32) for _ in range(5)] + [np.zeros(n, np.float32)]
     cnt = lib.bullseye_batched_profile(*[a.ctypes.data_as(ctypes.c_void_p) for a in arrs], n)
     width, nc, J, wide, items, ms = arrs
@@ -687,7 +687,7 @@ def uneven_main(args):
         torch.cuda.synchronize()
     finally:
         lib.bullseye_set_batched_profiling(0)
-    nrec = 32
+    nrec = 128
     arrs = [np.zeros(nrec, np.int32) for _ in range(5)] + [np.zeros(nrec, np.float32)]
     cnt = lib.bullseye_batched_profile(*[a.ctypes.data_as(ctypes.c_void_p) for a in arrs], nrec)
     width, _, Jl, _, items, cms = arrs

@@ -30,7 +30,7 @@ using namespace bz;
 
 namespace {
 
-constexpr int kMaxClasses = 16;
+constexpr int kMaxClasses = 32;
 
 // Rows [r0, r0 + n) of R: cls[c * R + r].
 __global__ void classify_kernel(const vis_real *__restrict__ uvw, const unsigned *__restrict__ spw,
@@ -506,10 +506,17 @@ BatchedState g_bs;
 // the window keeps every s that can reach a nonzero sample for some fu in that range, so the
 // taps left out are exactly zero.  Only the class widths some plane uses get a launch.
 // Candidate class widths for full support W, ascending; the last is W itself.
-std::vector<int> class_candidates(int W) {
+// The library's batched calls (fine = true) take every even width from 16: each class launch
+// grids its planes' windows with less padding, and only the widths some plane uses are launched.
+// The workspace entry launches every candidate and keeps the coarser list.
+std::vector<int> class_candidates(int W, bool fine = false) {
   std::vector<int> cand;
-  for (int w : {16, 18, 20, 22, 24, 28, 32, 36, 40, 44, 48, 56})
-    if (w < W) cand.push_back(w);
+  if (fine) {
+    for (int w = 16; w < W && (int)cand.size() < kMaxClasses - 1; w += 2) cand.push_back(w);
+  } else {
+    for (int w : {16, 18, 20, 22, 24, 28, 32, 36, 40, 44, 48, 56})
+      if (w < W) cand.push_back(w);
+  }
   cand.push_back(W);
   return cand;
 }
@@ -519,7 +526,7 @@ bool plan_classes() {
   BatchedState &b = g_bs;
   const int W = (int)c.W, os = (int)c.os, K = (int)c.K, P = (int)c.P;
   const bool wproj = c.P > 1;
-  const std::vector<int> cand = class_candidates(W);
+  const std::vector<int> cand = class_candidates(W, true);
   const int fu_min = wproj ? (int)std::floor(0.5 * os - 1e-6) : 0;
   const int fu_max = wproj ? (int)std::floor(1.5 * os + 1e-6) : os;
   std::vector<int> pw(P), plo(P);
