@@ -535,9 +535,12 @@ def precision_report():
     ref = run_imaging(lib64, p64, "facet_4_cor", repack=True, do_finalize=True)
     check(lib64)
     lib32 = load_library("GPU", "single")
+    from bullseye_gb300.geometry import offgrid_pairs
     out = {"workload": "config-1 observation, 80 km disc, 4 facets 4096^2 at 0/0.5/1/2 deg, PSWF W=7 os=63, "
                        "facet_4_cor, XX dirty image", "reference": "64-bit library on the same input values",
-           "rows": p32.rows}
+           "rows": p32.rows,
+           # samples whose footprint leaves each facet's grid (the reference drops them uncounted)
+           "offgrid_samples_per_facet": [int(x) for x in offgrid_pairs(p64)]}
     for comp in (1, 0):
         lib32.bullseye_set_compensated(comp)
         res = run_imaging(lib32, p32, "facet_4_cor", repack=True, do_finalize=True)

@@ -190,7 +190,14 @@ bool bz_copy_async(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind
       const uintptr_t x = (uintptr_t)from ^ (uintptr_t)to;
       const int unit = (x & 15) == 0 ? 16 : (x & 3) == 0 ? 4 : 1;
       const size_t units = (bytes + unit - 1) / unit;
-      const unsigned blocks = (unsigned)std::min<size_t>((units + 511) / 512, 152 * 4);
+      static int sms = 0;  // four 512-thread CTAs per SM at most
+      if (!sms) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            sms <= 0)
+          sms = 1;
+      }
+      const unsigned blocks = (unsigned)std::min<size_t>((units + 511) / 512, (size_t)sms * 4);
       link_copy_kernel<<<blocks, 512, 0, s>>>(from, to, bytes, unit);
       c.launches++;
       BZ_CUDA_TRY_RET(cudaGetLastError(), false);

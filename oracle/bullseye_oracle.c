@@ -197,6 +197,30 @@ struct modes {
     int conv;     /* enum conv_mode */
 };
 
+/* Test instrumentation (not in the reference): when set, the AA and w-projection branches write
+ * every (facet, row, channel)'s footprint corner and tap offsets {du, dv, fu, fv} (-1 x 4 when the
+ * reference rejects it) into g_tap_log[((f x rows + row) x channels + c) x 4 ...] instead of
+ * gridding it, so that a test can compare the cell choices of the two precisions. */
+static long long *g_tap_log = NULL;
+static size_t g_tap_log_n = 0;
+
+void oracle_record_taps(long long *log, size_t n) {
+    g_tap_log = log;
+    g_tap_log_n = n;
+}
+
+static int record_taps(gp_t *p, size_t f, size_t row, size_t c, int ok, size_t du, size_t dv, size_t fu, size_t fv) {
+    if (!g_tap_log) return 0;
+    const size_t i = ((f * p->row_count + row) * p->channel_count + c) * 4;
+    if (i + 3 < g_tap_log_n) {
+        g_tap_log[i] = ok ? (long long)du : -1;
+        g_tap_log[i + 1] = ok ? (long long)dv : -1;
+        g_tap_log[i + 2] = ok ? (long long)fu : -1;
+        g_tap_log[i + 3] = ok ? (long long)fv : -1;
+    }
+    return 1;
+}
+
 static void grid_one_facet(gp_t *p, const struct modes *md, size_t f) {
     const size_t W = (p->conv_support << 1) + 1;
     const size_t padded = W + 2;
@@ -335,6 +359,9 @@ static void grid_one_facet(gp_t *p, const struct modes *md, size_t f) {
                 size_t du = (size_t)RLRINT(tu), dv = (size_t)RLRINT(tv);
                 size_t fu = (size_t)((1 - uvl.u + (real_t)RLRINT(uvl.u)) * (real_t)os);
                 size_t fv = (size_t)((1 - uvl.v + (real_t)RLRINT(uvl.v)) * (real_t)os);
+                if (record_taps(p, f, row, c, !(dv + padded >= p->ny || du + padded >= p->nx || dv >= p->ny || du >= p->nx),
+                                du, dv, fu, fv))
+                    goto next;
                 if (dv + padded >= p->ny || du + padded >= p->nx || dv >= p->ny || du >= p->nx) goto next;
                 size_t cv = fv;
                 for (size_t sv = 0; sv < W; ++sv) {
@@ -365,6 +392,11 @@ static void grid_one_facet(gp_t *p, const struct modes *md, size_t f) {
                 size_t fv = (size_t)((1 - uvl.v + (real_t)RLRINT(uvl.v)) * (real_t)os);
                 size_t plane = (size_t)RLRINT(RFABS(uvl.w) / (float)p->wmax_est * (real_t)(p->wplanes - 1));
                 size_t foff = plane * K * K;
+                if (record_taps(p, f, row, c,
+                                !(dv + padded >= p->ny || du + padded >= p->nx || dv >= p->ny || du >= p->nx ||
+                                  plane >= p->wplanes),
+                                du, dv, fu, fv))
+                    goto next;
                 if (dv + padded >= p->ny || du + padded >= p->nx || dv >= p->ny || du >= p->nx ||
                     plane >= p->wplanes) goto next;
                 const rc_t *tab = (const rc_t *)p->conv;
