@@ -116,10 +116,11 @@ double bullseye_fp32_fma_tflops(int iters);
  * keeps freed memory mapped, so releaseLibrary followed by initLibrary (a pipeliner imaging several
  * runs) reuses memory the GPU has already touched.  This returns the pooled memory to the driver. */
 void bullseye_trim_memory(void);
-/* Host inputs are uploaded in row chunks on a copy stream and sorted by baseline on the device,
- * each chunk gridded while the next uploads.  With this off, repack_input_data fills
- * baseline_starting_indexes without permuting the caller's arrays (the reference permutes them,
- * wrapper.cu:422-452); gridding results do not depend on the row order.  On by default. */
+/* Host inputs are uploaded on a copy stream and sorted by baseline on the device (one chunk per
+ * call unless bullseye_set_max_stage_bytes or bullseye_set_grid_groups splits it).  With this off,
+ * repack_input_data fills baseline_starting_indexes without permuting the caller's arrays (the
+ * reference permutes them, wrapper.cu:422-452); gridding results do not depend on the row order.
+ * On by default. */
 void bullseye_set_host_repack(int on);
 /* Host-input visibilities of a batched gridding call are gridded in `groups` groups of row chunks,
  * each while the next group's rows upload; 1 (the default) grids every row after the last chunk
