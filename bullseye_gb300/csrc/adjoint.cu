@@ -60,15 +60,34 @@ struct AdjointArgs {
   const size_t *cgi;
   const void *conv;
   const vis_real *facet_centres;  // [F][2] arcsec, or null (no faceting)
-  const vis_complex *grad_grid;   // [F][cube][4][ny][nx]
+  const vis_complex *grad_grid;   // [F][cube][4][ny][nx], or [F][cube][ny][nx][4] with grid_interleaved
   vis_complex *grad_vis;          // [R][Ch][4]
   vis_complex *grad_jones;        // like jones, accumulated; or null
   long long nrows;
   int nchan, nspw, nant, ntimes, nfacets, cube, nx, ny, W, os, K, P, faceting;
   int normalise;  // prediction: divide each facet's gathered value by the real part of its tap sum
+  int grid_interleaved;  // prediction from its own model grids: a cell's 4 correlations are adjacent
   unsigned imaging_field;
   double u_scale, v_scale, gcx, gcy, wmax, ra0, dec0;
 };
+
+// The 4 adjacent correlations of one cell (32 bytes in single precision, 16-byte aligned): two
+// 16-byte loads.
+__device__ __forceinline__ void load_cell4(const vis_complex *p, cplx out[4]) {
+#if defined(BULLSEYE_SINGLE)
+  const float4 a = *reinterpret_cast<const float4 *>(p), b = *reinterpret_cast<const float4 *>(p + 2);
+  out[0].re = a.x; out[0].im = a.y;
+  out[1].re = a.z; out[1].im = a.w;
+  out[2].re = b.x; out[2].im = b.y;
+  out[3].re = b.z; out[3].im = b.w;
+#else
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    out[k].re = p[k].re;
+    out[k].im = p[k].im;
+  }
+#endif
+}
 
 __device__ __forceinline__ cplx cconj(cplx a) {
   a.im = -a.im;
@@ -280,6 +299,7 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
         const long long fv = (long long)plane * a.K + __shfl_sync(0xffffffffu, cell.fv, it);
         const long long git = __shfl_sync(0xffffffffu, (long long)g, it);
         const long long slice0 = ((long long)f * a.cube + git) * 4;
+        const long long cube0 = ((long long)f * a.cube + git) * nxy;  // interleaved layout
         // lane walks the cells lane, lane + 32, ... of the plane's nonzero window as (ju, jv)
         // without division
         const int2 w2 = win[plane];
@@ -302,14 +322,19 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
           const cplx ct = cconj(tap);
           if (want_ts) TS += tap.re;
           const long long cidx = (long long)(v0 + jv) * a.nx + (u0 + ju);
+          cplx gc[4];
+          if (PREDICT && a.grid_interleaved) {
+            load_cell4(a.grad_grid + (cube0 + cidx) * 4, gc);
+          } else {
 #pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            const vis_complex gg = a.grad_grid[(slice0 + k) * nxy + cidx];
-            cplx gc;
-            gc.re = gg.re;
-            gc.im = gg.im;
-            D[k] = cadd(D[k], cmul(gc, ct));
+            for (int k = 0; k < 4; ++k) {
+              const vis_complex gg = a.grad_grid[(slice0 + k) * nxy + cidx];
+              gc[k].re = gg.re;
+              gc[k].im = gg.im;
+            }
           }
+#pragma unroll
+          for (int k = 0; k < 4; ++k) D[k] = cadd(D[k], cmul(gc[k], ct));
         }
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -503,15 +528,18 @@ __global__ void predict_taper_shift_kernel(const vis_complex *__restrict__ img, 
   }
 }
 
-// After the forward transform: numpy's fftshift, dst[y][x] = src[(y-ny/2)%ny][(x-nx/2)%nx].
+// After the forward transform: numpy's fftshift, cell (y, x) = src[(y-ny/2)%ny][(x-nx/2)%nx], written
+// with the 4 correlations of a cell adjacent, dst[(f cube + g)][y][x][k] for source slice
+// (f cube + g) x 4 + k (the gather then reads a cell's correlations with two 16-byte loads).
 __global__ void predict_fftshift_kernel(const vis_complex *__restrict__ src, vis_complex *__restrict__ dst, int nx,
                                         int ny, long long slices) {
   const long long nxy = (long long)nx * ny, total = nxy * slices;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-    const long long s = i / nxy, r = i - s * nxy;
+    const int k = (int)(i & 3);
+    const long long cell = i >> 2, q = cell / nxy, r = cell - q * nxy;
     const int y = (int)(r / nx), x = (int)(r - (long long)y * nx);
     const int sy = (y + ny - ny / 2) % ny, sx = (x + nx - nx / 2) % nx;
-    dst[i] = src[s * nxy + (long long)sy * nx + sx];
+    dst[i] = src[(q * 4 + k) * nxy + (long long)sy * nx + sx];
   }
 }
 
@@ -641,6 +669,7 @@ extern "C" int bullseye_predict(const gridding_parameters *params, const void *m
   }
   AdjointArgs a = degrid_args(p, faceting);
   a.grad_grid = grids;
+  a.grid_interleaved = from_grid ? 0 : 1;  // the model grids made above interleave the correlations
   a.grad_vis = static_cast<vis_complex *>(vis_out);
   a.normalise = (flags & kPredictNormalise) ? 1 : 0;
   const int rc = launch_degrid<true>(a, p.wplanes > 1, st);
