@@ -71,6 +71,12 @@ struct AdjointArgs {
   double u_scale, v_scale, gcx, gcy, wmax, ra0, dec0;
 };
 
+// Dynamic shared memory of the gather kernel: the facet transforms, the w planes' windows, then
+// (16-byte aligned) each warp's staged taps.
+__host__ __device__ inline size_t degrid_taps_offset(int nfacets, int P) {
+  return (sizeof(FacetXform) * (size_t)nfacets + sizeof(int2) * (size_t)P + 15) / 16 * 16;
+}
+
 // The 4 adjacent correlations of one cell (32 bytes in single precision, 16-byte aligned): two
 // 16-byte loads.
 __device__ __forceinline__ void load_cell4(const vis_complex *p, cplx out[4]) {
@@ -209,6 +215,9 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
   }
   __syncthreads();
   const int lane = threadIdx.x & 31;
+  // this warp's staged column and row taps of the item it gathers ([2][W])
+  cplx *s_taps = reinterpret_cast<cplx *>(smem_raw + degrid_taps_offset(a.nfacets, a.P)) +
+                 (size_t)(threadIdx.x >> 5) * 2 * a.W;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   const int W = a.W;
@@ -305,6 +314,12 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
         const int2 w2 = win[plane];
         const int ww = w2.y - w2.x + 1;
         if (ww <= 0) continue;  // an all-zero kernel row: the item's sums stay zero
+        // the item's W column taps and W row taps, once per item instead of once per cell
+        for (int j = lane; j < ww; j += 32) {
+          s_taps[j] = tap_at<WPROJ>(a.conv, fu + (long long)(w2.x + j) * a.os);
+          s_taps[a.W + j] = tap_at<WPROJ>(a.conv, fv + (long long)(w2.x + j) * a.os);
+        }
+        __syncwarp();
         cplx D[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) { D[k].re = 0; D[k].im = 0; }
@@ -317,8 +332,7 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
             ++jv;
             if (jv >= wend) break;
           }
-          const cplx tap =
-              cmul(tap_at<WPROJ>(a.conv, fu + (long long)ju * a.os), tap_at<WPROJ>(a.conv, fv + (long long)jv * a.os));
+          const cplx tap = cmul(s_taps[ju - w2.x], s_taps[a.W + jv - w2.x]);
           const cplx ct = cconj(tap);
           if (want_ts) TS += tap.re;
           const long long cidx = (long long)(v0 + jv) * a.nx + (u0 + ju);
@@ -353,6 +367,7 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
           for (int k = 0; k < 4; ++k) myD[k] = D[k];
           myTS = TS;
         }
+        __syncwarp();  // every lane has read the staged taps before the next item's
       }
       if (!ok) continue;
       if (PREDICT) {
@@ -491,7 +506,7 @@ AdjointArgs degrid_args(const gridding_parameters &p, int faceting) {
 // Zeroes the output, then one persistent-style launch of the gather (32 items per warp pass).
 template <bool PREDICT>
 int launch_degrid(const AdjointArgs &a, bool wproj, cudaStream_t st) {
-  const size_t smem = sizeof(FacetXform) * (size_t)a.nfacets + sizeof(int2) * (size_t)a.P;
+  const size_t smem = degrid_taps_offset(a.nfacets, a.P) + (size_t)8 * 2 * a.W * sizeof(cplx);  // 8 warps
   if (smem > 200 * 1024) return BZ_ERR_UNSUPPORTED;
   if (cudaMemsetAsync(a.grad_vis, 0, sizeof(vis_complex) * (size_t)a.nrows * a.nchan * 4, st) != cudaSuccess) return BZ_ERR_CUDA;
   if (a.nrows == 0) return BZ_OK;
