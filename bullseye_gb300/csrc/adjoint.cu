@@ -324,18 +324,20 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
 #pragma unroll
         for (int k = 0; k < 4; ++k) { D[k].re = 0; D[k].im = 0; }
         acc_real TS = 0;
-        int ju = w2.x + lane % ww, jv = w2.x + lane / ww;
-        const int sju = 32 % ww, sjv = 32 / ww, wend = w2.y + 1;
-        for (; jv < wend; ju += sju, jv += sjv) {
-          if (ju >= wend) {
-            ju -= ww;
-            ++jv;
-            if (jv >= wend) break;
-          }
-          const cplx tap = cmul(s_taps[ju - w2.x], s_taps[a.W + jv - w2.x]);
+        // (ru, rv): the lane's cell relative to the window corner; off: its offset in the grid.
+        // The trip count is fixed before the loop, so prediction's loads of consecutive cells
+        // overlap (two cells per iteration); the adjoint's four strided slices run one cell at a time.
+        const int ncell = ww * ww, sju = 32 % ww, sjv = 32 / ww;
+        int ru = lane % ww, rv = lane / ww;
+        const long long corner = (long long)(v0 + w2.x) * a.nx + (u0 + w2.x);
+        long long off = (long long)rv * a.nx + ru;
+        const long long step = (long long)sjv * a.nx + sju, wrap = (long long)a.nx - ww;
+#pragma unroll(PREDICT ? 2 : 1)
+        for (int idx = lane; idx < ncell; idx += 32) {
+          const cplx tap = cmul(s_taps[ru], s_taps[a.W + rv]);
           const cplx ct = cconj(tap);
           if (want_ts) TS += tap.re;
-          const long long cidx = (long long)(v0 + jv) * a.nx + (u0 + ju);
+          const long long cidx = corner + off;
           cplx gc[4];
           if (PREDICT && a.grid_interleaved) {
             load_cell4(a.grad_grid + (cube0 + cidx) * 4, gc);
@@ -349,6 +351,14 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
           }
 #pragma unroll
           for (int k = 0; k < 4; ++k) D[k] = cadd(D[k], cmul(gc[k], ct));
+          ru += sju;
+          rv += sjv;
+          off += step;
+          if (ru >= ww) {  // one wrap at most: sju < ww, or ww > 32 and sju = 32
+            ru -= ww;
+            ++rv;
+            off += wrap;
+          }
         }
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
