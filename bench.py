@@ -839,7 +839,8 @@ def predict_main(args):
     from bullseye_gb300.filters import gridding_correction
     from bullseye_gb300.library import check, load_library
     torch.cuda.set_device(0)
-    geo = geometry(N_TIMES)
+    n_times = max(8, int(N_TIMES * args.time_frac))  # fewer timesteps only for profiling captures
+    geo = geometry(n_times)
     conv, supports = kernel_stack(geo["wmax"])
     R = geo["uvw"].shape[0]
     pairs = R * N_CHAN * N_FACETS
@@ -907,7 +908,8 @@ def predict_main(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD.replace("facet_4_cor_corrections+facet_sampling_function",
                                                     "bullseye_predict (normalised, Jones forward)"),
-                       "model": "16 facets x 20 point sources, 4 correlations, detapered, forward FFT every call"},
+                       "model": "16 facets x 20 point sources, 4 correlations, detapered, forward FFT every call",
+                       **({} if n_times == N_TIMES else {"timesteps": n_times})},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                          "frac": achieved / fp32_peak if fp32_peak else None,
                          "flops_rule": "(8 x 4 corr + 7) x W_p^2 per (vis, facet) + 152 for phase and Jones",
