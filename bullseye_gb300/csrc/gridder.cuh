@@ -618,6 +618,57 @@ __device__ __forceinline__ bool choose_cells_df(float um, float vm, float wm, co
 #endif
 
 // The facet-independent part of a visibility's prologue: one (row, channel)'s checks and inputs.
+// Four consecutive values starting at a multiple of four elements (a 2x2 Jones term; a row's four
+// correlations, weights or flags): vector loads when the array's base allows them (`vec`, the same
+// for every thread of a launch), element loads otherwise (a caller's device array may sit at any
+// element boundary).
+__device__ __forceinline__ bool vec16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+__device__ __forceinline__ void load_c4(const vis_complex *p, bool vec, cplx out[4]) {
+  if (vec) {
+#if defined(BULLSEYE_SINGLE)
+    const float4 x = __ldg(reinterpret_cast<const float4 *>(p)), y = __ldg(reinterpret_cast<const float4 *>(p) + 1);
+    out[0].re = x.x; out[0].im = x.y; out[1].re = x.z; out[1].im = x.w;
+    out[2].re = y.x; out[2].im = y.y; out[3].re = y.z; out[3].im = y.w;
+#else
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const double2 v = __ldg(reinterpret_cast<const double2 *>(p) + k);
+      out[k].re = v.x; out[k].im = v.y;
+    }
+#endif
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      out[k].re = p[k].re;
+      out[k].im = p[k].im;
+    }
+  }
+}
+__device__ __forceinline__ void load_r4(const vis_real *p, bool vec, acc_real out[4]) {
+  if (vec) {
+#if defined(BULLSEYE_SINGLE)
+    const float4 x = __ldg(reinterpret_cast<const float4 *>(p));
+    out[0] = x.x; out[1] = x.y; out[2] = x.z; out[3] = x.w;
+#else
+    const double2 x = __ldg(reinterpret_cast<const double2 *>(p)), y = __ldg(reinterpret_cast<const double2 *>(p) + 1);
+    out[0] = x.x; out[1] = x.y; out[2] = y.x; out[3] = y.y;
+#endif
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) out[k] = (acc_real)p[k];
+  }
+}
+__device__ __forceinline__ void load_f4(const uint8_t *p, bool vec, bool out[4]) {
+  if (vec) {
+    const unsigned x = __ldg(reinterpret_cast<const unsigned *>(p));
+#pragma unroll
+    for (int k = 0; k < 4; ++k) out[k] = ((x >> (8 * k)) & 0xffu) != 0;  // little-endian byte k
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) out[k] = p[k] != 0;
+  }
+}
+
 template <int NC>
 struct RowInputs {
   bool use;            // in range, channel enabled, spw and grid group valid, Jones indices valid
@@ -664,7 +715,13 @@ __device__ __forceinline__ void load_row(const GridArgs &a, int chan, long long 
   if (a.mode == CORR_SAMPLING) {
 #pragma unroll
     for (int k = 0; k < NC; ++k) { ri.vis[k].re = 1; ri.vis[k].im = 0; ri.wt[k] = 1; ri.fl[k] = false; }
-  } else if (NC == 1 || NC == 2) {
+  } else if constexpr (NC == 4) {
+    // a row's 4 correlations start at a multiple of 4 elements when npol = 4
+    const bool v4 = a.npol == 4;
+    load_c4(a.vis + base, v4 && vec16(a.vis), ri.vis);
+    load_r4(a.weights + base, v4 && vec16(a.weights), ri.wt);
+    load_f4(a.flags + base, v4 && (reinterpret_cast<uintptr_t>(a.flags) & 3) == 0, ri.fl);
+  } else {
 #pragma unroll
     for (int k = 0; k < NC; ++k) {
       int pi = (k == 0) ? a.pol0 : a.pol1;
@@ -672,14 +729,6 @@ __device__ __forceinline__ void load_row(const GridArgs &a, int chan, long long 
       ri.vis[k].re = vv.re; ri.vis[k].im = vv.im;
       ri.wt[k] = (acc_real)a.weights[base + pi];
       ri.fl[k] = a.flags[base + pi] != 0;
-    }
-  } else {
-#pragma unroll
-    for (int k = 0; k < NC; ++k) {
-      vis_complex vv = a.vis[base + k];
-      ri.vis[k].re = vv.re; ri.vis[k].im = vv.im;
-      ri.wt[k] = (acc_real)a.weights[base + k];
-      ri.fl[k] = a.flags[base + k] != 0;
     }
   }
   ri.jt1 = ri.jt2 = 0;
@@ -719,12 +768,9 @@ __device__ __forceinline__ void facet_record(const GridArgs &a, int f_local, int
     const long long i1 = (((ri.jt1 * a.nfacets_total + fglob) * a.nspw + ri.spw) * a.nchan + c) * 4;
     const long long i2 = (((ri.jt2 * a.nfacets_total + fglob) * a.nspw + ri.spw) * a.nchan + c) * 4;
     cplx P[4], Q[4], T[4], O[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      vis_complex p = a.jones_inv[i1 + k], q = a.jones_inv[i2 + k];
-      P[k].re = p.re; P[k].im = p.im;
-      Q[k].re = q.re; Q[k].im = q.im;
-    }
+    const bool jv = vec16(a.jones_inv);
+    load_c4(a.jones_inv + i1, jv, P);
+    load_c4(a.jones_inv + i2, jv, Q);
     // hermitian transpose of Q
     cplx qh[4];
     qh[0].re = Q[0].re; qh[0].im = -Q[0].im;
