@@ -223,6 +223,7 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
   const int W = a.W;
   const long long nxy = (long long)a.nx * a.ny;
   const double plane_scale = WPROJ ? (double)(a.P - 1) / a.wmax : 0.0;
+  const bool jones_vec = vec16(a.jones);  // 16-byte loads of the 2x2 terms (every term starts at 4 x 8 bytes)
 
   // Each warp takes 32 consecutive (row, channel) items at a time.  Lane i does the scalar work
   // of item i: its loads, the FP64 geometry, the Jones inverses and the chain rule.  FP64 and the
@@ -394,11 +395,8 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
         }
         if (a.jones) {
           cplx Pm[4], Qm[4], T[4], O[4];
-#pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            Pm[k].re = a.jones[i1 + k].re; Pm[k].im = a.jones[i1 + k].im;
-            Qm[k].re = a.jones[i2 + k].re; Qm[k].im = a.jones[i2 + k].im;
-          }
+          load_c4(a.jones + i1, jones_vec, Pm);
+          load_c4(a.jones + i2, jones_vec, Qm);
           mat2(Pm, false, X, false, T);  // J_p M
           mat2(T, false, Qm, true, O);   // (J_p M) J_q^H
 #pragma unroll
@@ -412,20 +410,18 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
       // chain rule back to V (and the Jones terms), each lane for its own item
       cplx Pm[4], Qm[4];
       if (a.jones) {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          Pm[k].re = a.jones[i1 + k].re; Pm[k].im = a.jones[i1 + k].im;
-          Qm[k].re = a.jones[i2 + k].re; Qm[k].im = a.jones[i2 + k].im;
-        }
+        load_c4(a.jones + i1, jones_vec, Pm);
+        load_c4(a.jones + i2, jones_vec, Qm);
         if (!inv2(Pm) || !inv2(Qm)) continue;  // a singular term: no gradient through it
       }
       const bool row_ok = !a.flagged_rows[row] && a.field[row] == a.imaging_field;
       acc_real cw[4];
+      bool fl[4];
+      load_r4(a.weights + base, vec16(a.weights), cw);
+      load_f4(a.flags + base, (reinterpret_cast<uintptr_t>(a.flags) & 3) == 0, fl);
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const bool keep = row_ok && !a.flags[base + k];
-        cw[k] = keep ? (acc_real)a.weights[base + k] : (acc_real)0;
-      }
+      for (int k = 0; k < 4; ++k)
+        if (!row_ok || fl[k]) cw[k] = (acc_real)0;
       cplx gM[4];
       const cplx cph = cconj(ph);
 #pragma unroll
@@ -444,11 +440,7 @@ __global__ void __launch_bounds__(256) degrid_adjoint_kernel(const AdjointArgs a
         for (int k = 0; k < 4; ++k) gV[k] = cadd(gV[k], G1[k]);
         if (a.grad_jones) {
           cplx V[4];
-#pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            V[k].re = a.vis[base + k].re;
-            V[k].im = a.vis[base + k].im;
-          }
+          load_c4(a.vis + base, vec16(a.vis), V);
           cplx VQ[4], M[4], gp[4], gq[4];
           mat2(V, false, Qm, true, VQ);  // V Q^H
           mat2(Pm, false, VQ, false, M);  // M = P V Q^H
