@@ -255,6 +255,8 @@ __global__ void __launch_bounds__(kRecordWarps * 32) record_kernel(
         dinv = 1.0 / (double)a.wavelengths[(long long)s0 * a.nchan + sg.z];
       }
     }
+#else
+    (void)dinv;  // the 64-bit library keeps the FP64 cell choice
 #endif
     for (int f0 = 0; f0 < nfacets; f0 += FB) {
       const int fb = min(FB, nfacets - f0);
@@ -343,6 +345,7 @@ __global__ void __launch_bounds__(kRecordWarps * 32) record_kernel(
           const int g0 = __shfl_sync(0xffffffffu, gv, __ffs(m) - 1);
           const long long fslice = (long long)(a.facet_base + f) * a.groups;
           if (__all_sync(0xffffffffu, gv < 0 || gv == g0)) {
+            __syncwarp();  // the lanes' earlier additions to s_norm are seen by lane 0
             if (lane == 0 && s_ng[fj] != g0) {
               if (s_ng[fj] >= 0) {
 #pragma unroll
@@ -353,15 +356,20 @@ __global__ void __launch_bounds__(kRecordWarps * 32) record_kernel(
               for (int k = 0; k < NC; ++k) s_norm[fj * NC + k] = 0.0;
               s_ng[fj] = g0;
             }
+            __syncwarp();  // lane 0's reset is seen by the lanes that add below
             // a warp's 32 terms are summed in the working precision (positive terms: a relative
-            // error of a few FP32 units at most), the sums of the warps in FP64
+            // error of a few FP32 units at most), the sums of the warps in FP64.  The butterfly
+            // leaves the same sum in every lane (each step adds the same two partials), and lane k
+            // adds correlation k: the NC FP64 additions are one warp instruction, not NC.
+            NormTerm mine = 0;
 #pragma unroll
             for (int k = 0; k < NC; ++k) {
               NormTerm x = t[k];
 #pragma unroll
               for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
-              if (lane == 0) s_norm[fj * NC + k] += (double)x;
+              if (lane == k) mine = x;
             }
+            if (lane < NC) s_norm[fj * NC + lane] += (double)mine;
           } else if (v) {
 #pragma unroll
             for (int k = 0; k < NC; ++k)
