@@ -1346,6 +1346,7 @@ extern "C" int bullseye_grid_batched_facets(gridding_parameters *pp, const bulls
   va.facets = b.facet_table.ptr;
   va.nfacets_total = nfacets;
   va.facet_base = 0;
+  va.jones_inv_t = nullptr;  // its facet count is the library's, not this call's
   va.facet_row_mask = row_mask;
   va.grid = static_cast<vis_complex *>(grids);
   va.grid_lo = nullptr;

@@ -125,6 +125,7 @@ struct Context {
   size_t rows_key_count = 0;
   bool rows_with_vis = false, rows_with_time = false;
   DevBuf<vis_complex> jones_raw, jones_inv;
+  DevBuf<vis_complex> jones_inv_t;  // the inverses time-innermost, for the batched record kernel (optional)
   DevBuf<FacetXform> facets, facets_sf;
   // grids
   // sf holds the caller's initial sampling grids [facets][sf][ny][nx]; every facet receives the

@@ -88,6 +88,7 @@ struct GridArgs {
   const unsigned *ant2;
   const size_t *time_ids;
   const vis_complex *jones_inv;  // inverted 2x2 terms [T][A][F][S][Ch][4]
+  const vis_complex *jones_inv_t;  // the same terms time-innermost, [A][S][Ch][F][T][4], or null (record kernel)
   const size_t *starts;          // baseline row starts [slots + 1] or null (fixed segments)
   // per-run tables (device)
   const vis_real *wavelengths;
@@ -676,7 +677,8 @@ struct RowInputs {
   unsigned spw;
   int g;               // grid group (cube channel)
   long long sc;        // spw x nchan + channel
-  long long jt1, jt2;  // Jones rows t x nant + antenna (four correlations with Jones)
+  long long jt1, jt2;  // Jones rows t x nant + antenna; with jones_inv_t, ((antenna x S + spw) x Ch + channel) x F
+  long long tt;        // the row's time index (with jones_inv_t)
   double um, vm, wm;
   vis_real uvw_in[3];  // as stored (the double-float cell choice starts from them)
   cplx vis[NC];
@@ -731,7 +733,7 @@ __device__ __forceinline__ void load_row(const GridArgs &a, int chan, long long 
       ri.fl[k] = a.flags[base + pi] != 0;
     }
   }
-  ri.jt1 = ri.jt2 = 0;
+  ri.jt1 = ri.jt2 = ri.tt = 0;
   if (NC == 4 && a.mode == CORR_QUAD_JONES) {
     const long long t = (long long)a.time_ids[row];
     const unsigned a1 = a.ant1[row], a2 = a.ant2[row];
@@ -739,8 +741,14 @@ __device__ __forceinline__ void load_row(const GridArgs &a, int chan, long long 
       atomicOr(a.error, DEV_ERR_JONES_INDEX);
       return;
     }
-    ri.jt1 = t * a.nant + a1;
-    ri.jt2 = t * a.nant + a2;
+    if (a.jones_inv_t) {
+      ri.jt1 = (((long long)a1 * a.nspw + spw) * a.nchan + c) * a.nfacets_total;
+      ri.jt2 = (((long long)a2 * a.nspw + spw) * a.nchan + c) * a.nfacets_total;
+      ri.tt = t;
+    } else {
+      ri.jt1 = t * a.nant + a1;
+      ri.jt2 = t * a.nant + a2;
+    }
   }
   ri.use = true;
 }
@@ -764,13 +772,21 @@ __device__ __forceinline__ void facet_record(const GridArgs &a, int f_local, int
 #pragma unroll
   for (int k = 0; k < NC; ++k) vis[k] = ri.vis[k];
   if (NC == 4 && a.mode == CORR_QUAD_JONES) {
-    // V <- J_p^-1 (V J_q^-H)   (correlation_gridding_policies.h:523-542; terms pre-inverted)
-    const long long i1 = (((ri.jt1 * a.nfacets_total + fglob) * a.nspw + ri.spw) * a.nchan + c) * 4;
-    const long long i2 = (((ri.jt2 * a.nfacets_total + fglob) * a.nspw + ri.spw) * a.nchan + c) * 4;
+    // V <- J_p^-1 (V J_q^-H)   (correlation_gridding_policies.h:523-542; terms pre-inverted).
+    // With the time-innermost copy, the 32 rows of a warp (consecutive times of one baseline and
+    // channel) read one contiguous run of terms per antenna and facet.
     cplx P[4], Q[4], T[4], O[4];
-    const bool jv = vec16(a.jones_inv);
-    load_c4(a.jones_inv + i1, jv, P);
-    load_c4(a.jones_inv + i2, jv, Q);
+    if (a.jones_inv_t) {
+      const bool jv = vec16(a.jones_inv_t);
+      load_c4(a.jones_inv_t + ((ri.jt1 + fglob) * a.ntimes + ri.tt) * 4, jv, P);
+      load_c4(a.jones_inv_t + ((ri.jt2 + fglob) * a.ntimes + ri.tt) * 4, jv, Q);
+    } else {
+      const long long i1 = (((ri.jt1 * a.nfacets_total + fglob) * a.nspw + ri.spw) * a.nchan + c) * 4;
+      const long long i2 = (((ri.jt2 * a.nfacets_total + fglob) * a.nspw + ri.spw) * a.nchan + c) * 4;
+      const bool jv = vec16(a.jones_inv);
+      load_c4(a.jones_inv + i1, jv, P);
+      load_c4(a.jones_inv + i2, jv, Q);
+    }
     // hermitian transpose of Q
     cplx qh[4];
     qh[0].re = Q[0].re; qh[0].im = -Q[0].im;

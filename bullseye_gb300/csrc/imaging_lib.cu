@@ -496,7 +496,7 @@ extern "C" void releaseLibrary() {
   c.conv.release(); c.tap_sums.release(); c.tap_sums_f.release(); c.conv_t.release(); c.wavelengths.release(); c.facet_centres.release(); c.enabled.release();
   c.cgi.release(); c.sf_cgi.release(); c.vis.release(); c.weights.release(); c.uvw.release();
   c.flags.release(); c.flagged_rows.release(); c.field.release(); c.spw.release(); c.ant1.release();
-  c.ant2.release(); c.time_ids.release(); c.starts.release(); c.jones_raw.release(); c.jones_inv.release();
+  c.ant2.release(); c.time_ids.release(); c.starts.release(); c.jones_raw.release(); c.jones_inv.release(); c.jones_inv_t.release();
   c.facets.release(); c.facets_sf.release(); c.grid.release(); c.grid_lo.release(); c.sf.release(); c.sf_acc.release(); c.sf_lo.release();
   c.scratch.release(); c.sf_out.release(); c.norm.release(); c.dev_error.release(); c.corr_x.release(); c.corr_y.release();
   for (StageBuf &g : c.stage) {
@@ -794,6 +794,7 @@ bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool f
     nslots = plan.chunks * (int)plan.slots;
   }
   bz_trace_mark("rows_h2d");
+  bool jones_t_valid = false;
   if (jones) {
     const size_t nj = p.no_timestamps_read * p.antenna_count * c.F * c.nspw * c.nchan;
     if (!p.jones_terms || nj == 0) {
@@ -833,8 +834,24 @@ bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool f
       jsrc = c.jones_raw.ptr;
     }
     bz_trace_mark("jones_h2d");
+    // the batched gridder's record kernel reads a time-innermost copy (the 32 rows of a warp are
+    // consecutive times): allocated when there is room, never an error when there is not
+    if (c.batched_calls && c.jones_inv_t.n < 4 * nj) {
+      c.jones_inv_t.release();
+      void *pt = nullptr;
+      if (bz_dev_alloc(&pt, sizeof(vis_complex) * 4 * nj)) {
+        c.jones_inv_t.ptr = static_cast<vis_complex *>(pt);
+        c.jones_inv_t.n = 4 * nj;
+      } else {
+        cudaGetLastError();
+      }
+    }
+    vis_complex *jt = c.batched_calls && c.jones_inv_t.n >= 4 * nj ? c.jones_inv_t.ptr : nullptr;
+    const JonesDims jd{(long long)p.no_timestamps_read, (long long)p.antenna_count, (long long)c.F, (long long)c.nspw,
+                       (long long)c.nchan};
     invert_jones_kernel<<<(unsigned)((nj + 255) / 256), 256, 0, c.stream>>>(jsrc, c.jones_inv.ptr, (long long)nj,
-                                                                             c.dev_error.ptr);
+                                                                             c.dev_error.ptr, jt, jd);
+    jones_t_valid = jt != nullptr;
     BZ_CUDA_TRY_RET(cudaEventRecord(c.ev_jones_read, c.stream), false);
     c.launches++;
     bz_trace_mark("jones_invert");
@@ -879,6 +896,7 @@ bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool f
     a.ant1 = c.ant1.ptr; a.ant2 = c.ant2.ptr; a.time_ids = c.time_ids.ptr;
   }
   a.jones_inv = jones ? c.jones_inv.ptr : nullptr;
+  a.jones_inv_t = jones && jones_t_valid ? c.jones_inv_t.ptr : nullptr;
   a.starts = starts;
   a.wavelengths = c.wavelengths.ptr; a.enabled = c.enabled.ptr;
   a.cgi = sampling ? c.sf_cgi.ptr : c.cgi.ptr;

@@ -5,12 +5,31 @@
 
 namespace bz {
 
+// Time-innermost position of term i of a [T][A][F][S][Ch] table: [A][S][Ch][F][T].
+struct JonesDims {
+  long long T, A, F, S, C;
+};
+__device__ __forceinline__ long long jones_time_major(long long i, const JonesDims &d) {
+  const long long c = i % d.C;
+  long long r = i / d.C;
+  const long long s = r % d.S;
+  r /= d.S;
+  const long long f = r % d.F;
+  r /= d.F;
+  const long long a = r % d.A;
+  const long long t = r / d.A;
+  return (((a * d.S + s) * d.C + c) * d.F + f) * d.T + t;
+}
+
 // Invert every 2x2 Jones matrix (jones_2x2.h:86-126).  Singular matrices (determinant exactly
-// zero) are replaced by zeros and flagged; the reference throws instead.
+// zero) are replaced by zeros and flagged; the reference throws instead.  With out_t, each
+// inverse is also written time-innermost (the record kernel's copy).
 __global__ void invert_jones_kernel(const vis_complex *__restrict__ in, vis_complex *__restrict__ out,
-                                    long long n, int *error) {
+                                    long long n, int *error, vis_complex *__restrict__ out_t = nullptr,
+                                    JonesDims dims = JonesDims{0, 0, 0, 0, 0}) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  vis_complex *o2 = out_t ? out_t + 4 * jones_time_major(i, dims) : nullptr;
   typedef vis_real T;
   vis_complex a = in[4 * i], b = in[4 * i + 1], c = in[4 * i + 2], d = in[4 * i + 3];
   T dr = (a.re * d.re - a.im * d.im) - (b.re * c.re - b.im * c.im);
@@ -19,6 +38,7 @@ __global__ void invert_jones_kernel(const vis_complex *__restrict__ in, vis_comp
   if (dr == (T)0 && di == (T)0) {
     atomicOr(error, 4);
     out[4 * i] = z; out[4 * i + 1] = z; out[4 * i + 2] = z; out[4 * i + 3] = z;
+    if (o2) { o2[0] = z; o2[1] = z; o2[2] = z; o2[3] = z; }
     return;
   }
   // 1 / det with scaling (Smith's method) to avoid overflow
@@ -38,10 +58,12 @@ __global__ void invert_jones_kernel(const vis_complex *__restrict__ in, vis_comp
     o.im = x.re * yi + x.im * yr;
     return o;
   };
-  out[4 * i] = mul(d, ir, ii);
-  out[4 * i + 1] = mul(b, -ir, -ii);
-  out[4 * i + 2] = mul(c, -ir, -ii);
-  out[4 * i + 3] = mul(a, ir, ii);
+  const vis_complex r0 = mul(d, ir, ii), r1 = mul(b, -ir, -ii), r2 = mul(c, -ir, -ii), r3 = mul(a, ir, ii);
+  out[4 * i] = r0;
+  out[4 * i + 1] = r1;
+  out[4 * i + 2] = r2;
+  out[4 * i + 3] = r3;
+  if (o2) { o2[0] = r0; o2[1] = r1; o2[2] = r2; o2[3] = r3; }
 }
 
 // out = hi + lo (compensated grid resolution), element-wise over complex values.
