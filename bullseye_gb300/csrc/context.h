@@ -81,6 +81,7 @@ struct Context {
   bool compensated = true;  // FP32: compensated (hi/lo) grid accumulation
   bool device_inputs = false;  // row arrays, Jones terms and baseline starts are device pointers
   bool batched_calls = true;   // 4-correlation and sampling-function exports run the batched gridder
+  bool jones_time_major = true;  // batched calls: the record kernel reads a time-innermost Jones copy
   long long launches = 0;      // kernels launched by this library since initLibrary
   cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;  // around the last gridder launch
   bool kernel_timing_pending = false;

@@ -128,6 +128,12 @@ extern "C" void bullseye_set_compensated(int on) { g_ctx.compensated = on != 0; 
 // See include/bullseye_gb300.h.
 extern "C" void bullseye_set_batched_calls(int on) { g_ctx.batched_calls = on != 0; }
 
+// See include/bullseye_gb300.h.
+extern "C" void bullseye_set_jones_time_major(int on) {
+  g_ctx.jones_time_major = on != 0;
+  if (!on) g_ctx.jones_inv_t.release();  // stream-ordered: after the calls already queued
+}
+
 // ---------------------------------------------------------------- phase tracing
 namespace {
 struct Trace {
@@ -836,7 +842,8 @@ bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool f
     bz_trace_mark("jones_h2d");
     // the batched gridder's record kernel reads a time-innermost copy (the 32 rows of a warp are
     // consecutive times): allocated when there is room, never an error when there is not
-    if (c.batched_calls && c.jones_inv_t.n < 4 * nj) {
+    const bool want_t = c.batched_calls && c.jones_time_major;
+    if (want_t && c.jones_inv_t.n < 4 * nj) {
       c.jones_inv_t.release();
       void *pt = nullptr;
       if (bz_dev_alloc(&pt, sizeof(vis_complex) * 4 * nj)) {
@@ -846,7 +853,7 @@ bool bz_prepare_grid_args(const gridding_parameters &p, int nc, int mode, bool f
         cudaGetLastError();
       }
     }
-    vis_complex *jt = c.batched_calls && c.jones_inv_t.n >= 4 * nj ? c.jones_inv_t.ptr : nullptr;
+    vis_complex *jt = want_t && c.jones_inv_t.n >= 4 * nj ? c.jones_inv_t.ptr : nullptr;
     const JonesDims jd{(long long)p.no_timestamps_read, (long long)p.antenna_count, (long long)c.F, (long long)c.nspw,
                        (long long)c.nchan};
     invert_jones_kernel<<<(unsigned)((nj + 255) / 256), 256, 0, c.stream>>>(jsrc, c.jones_inv.ptr, (long long)nj,

@@ -72,6 +72,7 @@ EXTENSIONS = {
     "bullseye_set_max_stage_bytes": (None, [ctypes.c_size_t]),
     "bullseye_set_visibility_records": (None, [ctypes.c_int]),
     "bullseye_set_record_budget": (None, [ctypes.c_size_t]),
+    "bullseye_set_jones_time_major": (None, [ctypes.c_int]),
     "bullseye_reset_counters": (None, []),
     "bullseye_zero_grids": (None, []),
     "bullseye_set_gridding_correction": (None, [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t]),

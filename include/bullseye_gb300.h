@@ -146,6 +146,13 @@ void bullseye_set_max_stage_bytes(size_t bytes);
  * with records off.  Results are the same either way. */
 void bullseye_set_visibility_records(int on);
 void bullseye_set_record_budget(size_t bytes);
+/* Jones terms of the batched record kernel (on by default): the inversion also writes the inverses
+ * time-innermost ([antenna][spw][channel][facet][time][4], 16 bytes per complex term in double
+ * precision, 8 in single), so that a warp's rows (consecutive times of one baseline) read one
+ * contiguous run per antenna and facet.  It takes a second copy of the terms' memory, allocated
+ * when there is room; off (or without room), the record kernel reads the original table.  Results
+ * are the same either way. */
+void bullseye_set_jones_time_major(int on);
 
 /* Batched, support-aware gridding of every facet of the current chunk: `call` 0 grids like
  * facet_4_cor_corrections, 1 like facet_4_cor, 2 like grid_4_cor; with_sampling != 0 also grids

@@ -8,7 +8,9 @@ terms, w-projection, faceting and uniform weighting:
 
 * records on (the default): every work item from records;
 * records off (bullseye_set_visibility_records(0)): every work item prepared in place;
-* a 1 MB record budget: the first segments from records, the rest in place, in the same launches.
+* a 1 MB record budget: the first segments from records, the rest in place, in the same launches;
+* records reading the original [T][A][F][S][Ch] Jones table instead of the time-innermost copy
+  (bullseye_set_jones_time_major(0)).
 """
 import pytest
 
@@ -38,7 +40,7 @@ def _reference(p, oracle):
 
 
 @pytest.mark.parametrize("precision", ["double", "single"])
-@pytest.mark.parametrize("form", ["records", "in_place", "partial"])
+@pytest.mark.parametrize("form", ["records", "in_place", "partial", "jones_original_layout"])
 def test_record_forms_match_oracle(precision, form, problem, gpu_libs, oracle_libs):
     from bullseye_gb300.library import check
     p = problem.astype(precision)
@@ -46,12 +48,14 @@ def test_record_forms_match_oracle(precision, form, problem, gpu_libs, oracle_li
     lib.bullseye_set_batched_calls(1)
     lib.bullseye_set_visibility_records(0 if form == "in_place" else 1)
     lib.bullseye_set_record_budget((1 << 20) if form == "partial" else 0)
+    lib.bullseye_set_jones_time_major(0 if form == "jones_original_layout" else 1)
     try:
         res = run_imaging(lib, p, "facet_4_cor_corrections", keep_raw=True, uniform=True,
                           norm_bins=(2 * p.conv_support + 1) ** 2)
     finally:
         lib.bullseye_set_visibility_records(1)
         lib.bullseye_set_record_budget(0)
+        lib.bullseye_set_jones_time_major(1)
     check(lib)
     ref = _reference(p, oracle_libs["double"])
     tol = 1e-12 if precision == "double" else 1e-5
