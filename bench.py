@@ -55,11 +55,11 @@ WORKLOAD = ("facet_4_cor_corrections+facet_sampling_function, 27 ant x 2000 t x 
 
 
 # DRAM traffic of one batched step (dram__bytes_read.sum + dram__bytes_write.sum, every launch of
-# the step), captured with ncu on the 16-channel, 4-facet cut of this workload (12.98 GB for
+# the step), captured with ncu on the 16-channel, 4-facet cut of this workload (11.20 GB for
 # 44.93 M vis-facet pairs, visibility records included) and scaled by vis-facet pairs: an upper
 # estimate for the full step, where 16 facets rather than 4 share each row's loads.
-TRAFFIC_BYTES_PER_PAIR = 12.98e9 / 44928000
-TRAFFIC_SOURCE = ("ncu dram bytes of one eager step of the 16-channel 4-facet case (12.98 GB / 44.93 M pairs, "
+TRAFFIC_BYTES_PER_PAIR = 11.20e9 / 44928000
+TRAFFIC_SOURCE = ("ncu dram bytes of one eager step of the 16-channel 4-facet case (11.20 GB / 44.93 M pairs, "
                   "visibility records written and read once), scaled by vis-facet pairs (upper estimate: more "
                   "facets share each row's loads)")
 
