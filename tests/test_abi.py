@@ -25,6 +25,24 @@ def declared_symbols():
     return sorted(set(re.findall(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\([^;{]*\)\s*;", text)))
 
 
+@pytest.mark.parametrize("lang", ["c99", "c++17"])
+def test_header_compiles_as_plain_c_and_cpp(lang, tmp_path):
+    """The boundary header is what a cgo / ctypes / JNI binding includes: it must stand alone in C
+    (no C++ types) and in C++, warning-free."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc" if lang == "c99" else "g++")
+    if cc is None:
+        pytest.skip("no host compiler")
+    src = tmp_path / ("use.c" if lang == "c99" else "use.cpp")
+    # the struct is opaque in the header (callers pass the reference's struct by pointer)
+    src.write_text('#include "bullseye_gb300.h"\nint main(void) { gridding_parameters *p = 0; return p != 0; }\n')
+    cmd = [cc, "-std=" + lang, "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(REPO, "include"),
+           "-c", str(src), "-o", str(tmp_path / "use.o")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 def test_header_declares_every_reference_export():
     syms = declared_symbols()
     for name in REFERENCE_EXPORTS:
